@@ -1,0 +1,210 @@
+/*
+ * tailor_gb300.h -- C ABI of the GB300 BiGlobal hot path.
+ *
+ * One context (tlr_ctx) holds one stability problem on one GPU: the FD-q
+ * rules, the prepared grid and base flow, and every derived device array.
+ * The entry points mirror the reference's stage objects, each of which
+ * takes ProblemData and fills a *Diagnostics struct:
+ *
+ *   tlr_metrics               Metrics::compute          (Metrics.hpp:69-70)
+ *   tlr_baseflow_derivatives  BaseFlowDerivatives::compute
+ *                                               (BaseFlowDerivatives.hpp:95-96)
+ *   tlr_assemble              GlobalOperator::assemble  (GlobalOperator.hpp:53-54)
+ *   tlr_apply_bc              BoundaryConditions::apply (BoundaryConditions.hpp:59-60)
+ *   tlr_spmv                  MatMult on the BAIJ operators (PETSc, implicit)
+ *   tlr_solve                 EigenSolver::solve        (EigenSolver.hpp:56-67)
+ *
+ * Every call returns a tlr_status (0 = success).  Failures carry the
+ * reference's error category and message text (tlr_last_error); stage
+ * ordering is enforced like the reference's PETSC_ERR_ARG_WRONGSTATE
+ * preconditions.  All device work of a context runs on its own CUDA
+ * stream; one host thread per context.
+ *
+ * Layout (shared by all arrays crossing this ABI):
+ *   node n = j * ny + i, i = wall-normal xi index (bounded rule),
+ *   j = spanwise eta index (periodic rule) -- the reference's natural
+ *   k_j_dof ordering (Prepare.cpp:496-497, 537-552);
+ *   complex numbers are interleaved (re, im) doubles;
+ *   BSR: row_ptr[nb+1], col_idx[nnzb] sorted ascending, values
+ *   [nnzb][5][5] complex, row-major 5x5 blocks (the reference inserts
+ *   row-oriented blocks, GlobalOperator.cpp:188).
+ */
+#ifndef TAILOR_GB300_H
+#define TAILOR_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  TLR_OK = 0,
+  TLR_ERR_ARG = 1,          /* invalid argument (PETSC_ERR_ARG_*)          */
+  TLR_ERR_WRONGSTATE = 2,   /* stage called out of order                   */
+  TLR_ERR_SIZE = 3,         /* rule/grid size mismatch (PETSC_ERR_ARG_SIZ) */
+  TLR_ERR_STENCIL = 4,      /* stencil leaves the grid (PETSC_ERR_PLIB)    */
+  TLR_ERR_NONFINITE = 5,    /* non-finite input or result (PETSC_ERR_FP)   */
+  TLR_ERR_JACOBIAN = 6,     /* singular/negative Jacobian (ARG_OUTOFRANGE) */
+  TLR_ERR_COMPLEX = 7,      /* imaginary part too large (PETSC_ERR_SUP)    */
+  TLR_ERR_NONPOSITIVE = 8,  /* rho or T <= 0 (ARG_OUTOFRANGE)              */
+  TLR_ERR_COEFFICIENTS = 9, /* invalid curvilinear LNS coefficients        */
+  TLR_ERR_CHARACTERISTIC = 10, /* far-field decomposition failed           */
+  TLR_ERR_CUDA = 11,
+  TLR_ERR_NOMEM = 12,
+  TLR_ERR_NOT_CONVERGED = 13,
+  TLR_ERR_TIMEOUT = 14,     /* bounded device wait ran out                 */
+  TLR_ERR_SINGULAR = 15     /* zero pivot in the sparse factorisation      */
+} tlr_status;
+
+/* Numerical part of the reference Recipe (Recipe.hpp:17-61). */
+typedef struct {
+  int q_y, q_z;
+  double mach, reynolds, prandtl, gas_constant, gamma;
+  double reference_viscosity;      /* parsed but unused, as in the reference */
+  double reference_temperature, sutherland_constant;
+  double alpha_re, alpha_im;       /* streamwise wavenumber                  */
+  double omega_re, omega_im;       /* search centre; lambda_s = Im w - i Re w */
+  int nev;                         /* NumberOfEigenvalues                    */
+  double tol;                      /* EigenSolver.Tolerance                  */
+  int max_it;                      /* EigenSolver.MaximumIterations          */
+} tlr_recipe;
+
+/* One-dimensional FD-q rule (FDQRuleData, ProblemData.hpp:26-96). */
+typedef struct {
+  int node_count;
+  int q;                        /* stencil has q+1 entries                  */
+  int periodic;                 /* 0 bounded (xi), 1 periodic (eta)         */
+  double period;
+  const double *nodes;          /* [node_count]                             */
+  const int *stencil_indices;   /* [node_count][q+1] wrapped node index     */
+  const int *stencil_offsets;   /* [node_count][q+1] unwrapped displacement */
+  const double *weights;        /* [3][node_count][q+1]: d0, d1, d2         */
+} tlr_rule;
+
+/* MetricDiagnostics (Metrics.hpp:40-50). */
+typedef struct {
+  double min_jacobian, max_jacobian, max_grid_imaginary;
+  double norms[10];
+} tlr_metric_diag;
+
+/* BaseFlowDerivativeDiagnostics (BaseFlowDerivatives.hpp:67-75). */
+typedef struct {
+  double max_baseflow_imaginary;
+  double norms[25];
+} tlr_deriv_diag;
+
+/* GlobalOperatorDiagnostics (GlobalOperator.hpp:12-32). */
+typedef struct {
+  long rows, columns, block_size;
+  double mass_used_blocks, mass_allocated_blocks;
+  double spatial_used_blocks, spatial_allocated_blocks;
+  double mass_frobenius_norm, spatial_frobenius_norm;
+  float assemble_ms;            /* device time of the numeric assembly      */
+} tlr_operator_diag;
+
+/* BoundaryConditionDiagnostics (BoundaryConditions.hpp:12-34). */
+typedef struct {
+  int wall_nodes, farfield_nodes;
+  int incoming_modes, neutral_modes;
+  int min_incoming_per_node, max_incoming_per_node;
+  double max_characteristic_imaginary, max_eigenvector_condition;
+  double eigen_frobenius_norm, eigen_mass_frobenius_norm;
+} tlr_bc_diag;
+
+/* Matrices addressable through tlr_spmv / tlr_copy_out. */
+enum { TLR_MAT_M = 0, TLR_MAT_L = 1, TLR_MAT_A = 2, TLR_MAT_B = 3 };
+
+/* Arrays addressable through tlr_copy_out. */
+enum {
+  TLR_OUT_METRICS = 0,      /* [N][10] double                              */
+  TLR_OUT_DERIVATIVES = 1,  /* [N][25] double                              */
+  TLR_OUT_ROW_PTR = 2,      /* [N+1] int (pattern of L and A_bc)           */
+  TLR_OUT_COL_IDX = 3,      /* [nnzb] int                                  */
+  TLR_OUT_M_VALUES = 4,     /* [N][5][5] complex (M_Gamma, block diagonal) */
+  TLR_OUT_L_VALUES = 5,     /* [nnzb][5][5] complex                        */
+  TLR_OUT_A_VALUES = 6,     /* [nnzb][5][5] complex (A_bc)                 */
+  TLR_OUT_B_VALUES = 7      /* [N][5][5] complex (B_bc, block diagonal)    */
+};
+
+typedef struct tlr_ctx tlr_ctx;
+
+/* Create a context for an ny x nz problem (Prepare::initialize's checks on
+ * the rules: sizes, degrees, stencil indices).  device < 0 uses the
+ * current device. */
+int tlr_ctx_create(const tlr_recipe *recipe, const tlr_rule *xi,
+                   const tlr_rule *eta, int ny, int nz,
+                   double spanwise_period, int device, tlr_ctx **out);
+void tlr_ctx_destroy(tlr_ctx *ctx);
+
+/* Replace the streamwise wavenumber and search centre of a context; the
+ * derived operators must be re-assembled afterwards. */
+int tlr_set_alpha(tlr_ctx *ctx, double alpha_re, double alpha_im,
+                  double omega_re, double omega_im);
+
+/* Host arrays in natural order: grid [N][3] complex (x, y, z), baseflow
+ * [N][5] complex (rho, U, V, W, T) (Prepare.cpp:537-586). */
+int tlr_load_fields(tlr_ctx *ctx, const double *grid, const double *baseflow);
+
+int tlr_metrics(tlr_ctx *ctx, tlr_metric_diag *diag);
+int tlr_baseflow_derivatives(tlr_ctx *ctx, tlr_deriv_diag *diag);
+int tlr_assemble(tlr_ctx *ctx, tlr_operator_diag *diag);
+int tlr_apply_bc(tlr_ctx *ctx, tlr_bc_diag *diag);
+
+/* y = Mat x for Mat in {M, L, A_bc, B_bc}; x, y complex [5N].  With
+ * device_pointers = 0 both are host arrays and the call copies them. */
+int tlr_spmv(tlr_ctx *ctx, int which, const double *x, double *y,
+             int device_pointers);
+
+/* Copy one context array to host memory; bytes must match exactly. */
+int tlr_copy_out(tlr_ctx *ctx, int what, void *dst, size_t bytes);
+size_t tlr_out_bytes(tlr_ctx *ctx, int what);
+
+/* Pointwise entry points used by the golden tests.
+ * tlr_lns_points: LNSCoefficients::evaluate (LNSCoefficients.cpp:173-404)
+ *   q [np][10][5] (value, dx, dy, dz, dxx, dyy, dzz, dxy, dxz, dyz),
+ *   blocks [np][11][5][5] real (Gamma, A, B, C, D, Vxx, Vxy, Vxz, Vyy, Vyz,
+ *   Vzz), status [np] CoefficientStatus codes.
+ * tlr_transform_points: StreamwiseFourier::apply + CurvilinearTransform::
+ *   apply (StreamwiseFourier.cpp:16-44, CurvilinearTransform.cpp:62-101):
+ *   alpha [np] complex, phys [np][11][25], metrics [np][10]; fourier and
+ *   curvilinear [np][7][25] complex. */
+int tlr_lns_points(const tlr_recipe *recipe, int np, const double *q,
+                   double *blocks, int *status);
+int tlr_transform_points(int np, const double *alpha, const double *phys,
+                         const double *metrics, double *fourier,
+                         double *curvilinear, int *status);
+
+/* Shift-and-invert Krylov-Schur solve (EigenSolver.cpp:103-161). */
+typedef struct {
+  int nev;                /* 0: recipe value                                */
+  int ncv;                /* 0: max(2 nev, nev + 15) (SLEPc default)        */
+  double tol;             /* 0: recipe value                                */
+  int max_it;             /* 0: recipe value                                */
+  int precision;          /* 0: FP64 factorisation (drop-in form);
+                             1: FP32 factorisation + FP64 refinement       */
+  double sigma_re, sigma_im; /* used when use_sigma != 0                    */
+  int use_sigma;          /* 0: sigma = lambda target from omega            */
+  const double *start;    /* optional complex [5N] host start vector        */
+} tlr_solve_opts;
+
+typedef struct {
+  int requested, converged, iterations, reason;
+  double target_re, target_im;
+  double max_relative_error;
+  int factorizations, solves, refinement_steps;
+  double factor_ms, krylov_ms, total_ms;
+  double factor_flops;    /* algorithmic complex-counted flops of the LU    */
+} tlr_eig_diag;
+
+/* lambda [nev] complex, residual [nev]; modes [nev][5N] complex or NULL. */
+int tlr_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
+              double *residual, double *modes, tlr_eig_diag *diag);
+
+const char *tlr_status_string(int status);
+const char *tlr_last_error(const tlr_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,276 @@
+"""Python mirror of the reference's operator stages over the C ABI.
+
+The reference runs, in Process::run (Process.cpp:50-56), the stage objects
+Metrics, BaseFlowDerivatives, GlobalOperator, BoundaryConditions and
+EigenSolver on one ProblemData.  ``Problem`` plays ProblemData's role (it
+owns one device context); the stage classes keep the reference's method
+names (compute / assemble / apply / solve), diagnostics fields and error
+messages.  Errors raise ``TailorError`` carrying the status code and the
+reference's message text.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from .case import Case, target_lambda
+
+TLR_MAT_M, TLR_MAT_L, TLR_MAT_A, TLR_MAT_B = 0, 1, 2, 3
+(OUT_METRICS, OUT_DERIVS, OUT_ROW_PTR, OUT_COL, OUT_M, OUT_L, OUT_A,
+ OUT_B) = range(8)
+
+
+class TailorError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+        self.message = message
+
+
+def _ptr(a: np.ndarray) -> ctypes.c_void_p:
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _diag_dict(d) -> dict:
+    out = {}
+    for name, _ in d._fields_:
+        v = getattr(d, name)
+        out[name] = list(v) if isinstance(v, ctypes.Array) else v
+    return out
+
+
+def make_recipe(case: Case) -> L.Recipe:
+    ph = case.physics
+    return L.Recipe(case.qy, case.qz, ph.mach, ph.reynolds, ph.prandtl,
+                    ph.gas_constant, ph.gamma, ph.reference_viscosity,
+                    ph.reference_temperature, ph.sutherland_constant,
+                    complex(ph.alpha).real, complex(ph.alpha).imag,
+                    complex(ph.omega).real, complex(ph.omega).imag,
+                    ph.nev, ph.tol, ph.max_it)
+
+
+class Problem:
+    """Device-resident problem data (the reference's ProblemData)."""
+
+    def __init__(self, case: Case, device: int = -1, load: bool = True):
+        self.lib = L.load()
+        self.case = case
+        self._keep = []
+        recipe = make_recipe(case)
+        xi, eta = self._rule(case.xi), self._rule(case.eta)
+        ctx = ctypes.c_void_p()
+        st = self.lib.tlr_ctx_create(ctypes.byref(recipe), ctypes.byref(xi),
+                                     ctypes.byref(eta), case.ny, case.nz,
+                                     case.spanwise_period, device,
+                                     ctypes.byref(ctx))
+        if st:
+            raise TailorError(st, self.lib.tlr_last_error(None).decode())
+        self.ctx = ctx
+        if load:
+            self.load_fields(case.grid, case.baseflow)
+
+    def _rule(self, r) -> L.Rule:
+        nodes = np.ascontiguousarray(r.nodes, dtype=np.float64)
+        idx = np.ascontiguousarray(r.indices, dtype=np.int32)
+        off = np.ascontiguousarray(r.offsets, dtype=np.int32)
+        w = np.ascontiguousarray(r.weights, dtype=np.float64)
+        self._keep += [nodes, idx, off, w]
+        return L.Rule(r.n, r.q, int(r.periodic), r.period, nodes.ctypes.data,
+                      idx.ctypes.data, off.ctypes.data, w.ctypes.data)
+
+    def check(self, st: int) -> None:
+        if st:
+            raise TailorError(st, self.lib.tlr_last_error(self.ctx).decode())
+
+    def close(self) -> None:
+        if getattr(self, "ctx", None):
+            self.lib.tlr_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ----------------------------------------------------------- data
+    def load_fields(self, grid: np.ndarray, baseflow: np.ndarray) -> None:
+        g = np.ascontiguousarray(grid, dtype=np.float64)
+        b = np.ascontiguousarray(baseflow, dtype=np.float64)
+        self.check(self.lib.tlr_load_fields(self.ctx, _ptr(g), _ptr(b)))
+
+    def set_alpha(self, alpha: complex, omega: complex | None = None) -> None:
+        omega = self.case.physics.omega if omega is None else omega
+        self.check(self.lib.tlr_set_alpha(self.ctx, complex(alpha).real,
+                                          complex(alpha).imag,
+                                          complex(omega).real,
+                                          complex(omega).imag))
+
+    def copy_out(self, what: int) -> np.ndarray:
+        nbytes = self.lib.tlr_out_bytes(self.ctx, what)
+        nn = self.case.nodes
+        if what == OUT_METRICS:
+            a = np.empty((nn, 10))
+        elif what == OUT_DERIVS:
+            a = np.empty((nn, 25))
+        elif what in (OUT_ROW_PTR, OUT_COL):
+            a = np.empty(nbytes // 4, dtype=np.int32)
+        else:
+            a = np.empty((nbytes // 400, 5, 5, 2))
+        self.check(self.lib.tlr_copy_out(self.ctx, what, _ptr(a), nbytes))
+        return a
+
+    def spmv(self, which: int, x: np.ndarray) -> np.ndarray:
+        xr = np.ascontiguousarray(np.stack([x.real, x.imag], -1), dtype=np.float64)
+        y = np.empty_like(xr)
+        self.check(self.lib.tlr_spmv(self.ctx, which, _ptr(xr), _ptr(y), 0))
+        return y[..., 0] + 1j * y[..., 1]
+
+
+class Metrics:
+    """Metrics::compute (Metrics.hpp:59-87)."""
+
+    def __init__(self, problem: Problem):
+        self.p = problem
+
+    def compute(self) -> dict:
+        d = L.MetricDiag()
+        self.p.check(self.p.lib.tlr_metrics(self.p.ctx, ctypes.byref(d)))
+        return _diag_dict(d)
+
+
+class BaseFlowDerivatives:
+    """BaseFlowDerivatives::compute (BaseFlowDerivatives.hpp:83-111)."""
+
+    def __init__(self, problem: Problem):
+        self.p = problem
+
+    def compute(self) -> dict:
+        d = L.DerivDiag()
+        self.p.check(self.p.lib.tlr_baseflow_derivatives(self.p.ctx, ctypes.byref(d)))
+        return _diag_dict(d)
+
+
+class GlobalOperator:
+    """GlobalOperator::assemble (GlobalOperator.hpp:41-71)."""
+
+    def __init__(self, problem: Problem):
+        self.p = problem
+
+    def assemble(self) -> dict:
+        d = L.OperatorDiag()
+        self.p.check(self.p.lib.tlr_assemble(self.p.ctx, ctypes.byref(d)))
+        return _diag_dict(d)
+
+
+class BoundaryConditions:
+    """BoundaryConditions::apply (BoundaryConditions.hpp:46-65)."""
+
+    def __init__(self, problem: Problem):
+        self.p = problem
+
+    def apply(self) -> dict:
+        d = L.BcDiag()
+        self.p.check(self.p.lib.tlr_apply_bc(self.p.ctx, ctypes.byref(d)))
+        return _diag_dict(d)
+
+
+@dataclass
+class EigenSolution:
+    lam: np.ndarray
+    residual: np.ndarray
+    modes: np.ndarray | None
+    diag: dict
+
+    @property
+    def omega(self) -> np.ndarray:
+        return 1j * self.lam
+
+
+class EigenSolver:
+    """EigenSolver::solve (EigenSolver.hpp:48-72): shift-invert
+    Krylov-Schur on (A_bc, B_bc) with lambda target Im w - i Re w."""
+
+    def __init__(self, problem: Problem):
+        self.p = problem
+
+    def solve(self, nev: int = 0, ncv: int = 0, tol: float = 0.0,
+              max_it: int = 0, precision: int = 0, sigma: complex | None = None,
+              start: np.ndarray | None = None, modes: bool = False) -> EigenSolution:
+        ph = self.p.case.physics
+        k = nev or ph.nev
+        opts = L.SolveOpts(nev, ncv, tol, max_it, precision,
+                           0.0 if sigma is None else complex(sigma).real,
+                           0.0 if sigma is None else complex(sigma).imag,
+                           0 if sigma is None else 1, None)
+        if start is not None:
+            s = np.ascontiguousarray(np.stack([start.real, start.imag], -1),
+                                     dtype=np.float64)
+            self.p._keep.append(s)
+            opts.start = s.ctypes.data
+        lam = np.zeros((k, 2))
+        res = np.zeros(k)
+        vec = np.zeros((k, 5 * self.p.case.nodes, 2)) if modes else None
+        d = L.EigDiag()
+        st = self.p.lib.tlr_solve(self.p.ctx, ctypes.byref(opts), _ptr(lam),
+                                  _ptr(res), None if vec is None else _ptr(vec),
+                                  ctypes.byref(d))
+        self.p.check(st)
+        nconv = min(d.converged, k)
+        lam_c = lam[:nconv, 0] + 1j * lam[:nconv, 1]
+        vec_c = None if vec is None else vec[:nconv, :, 0] + 1j * vec[:nconv, :, 1]
+        return EigenSolution(lam_c, res[:nconv], vec_c, _diag_dict(d))
+
+
+def lns_points(case_or_physics, q: np.ndarray, qy: int = 10, qz: int = 6):
+    """Pointwise LNS blocks on the GPU: q [np][10][5] -> [np][11][5][5]."""
+    lib = L.load()
+    ph = getattr(case_or_physics, "physics", case_or_physics)
+    r = L.Recipe(qy, qz, ph.mach, ph.reynolds, ph.prandtl, ph.gas_constant,
+                 ph.gamma, ph.reference_viscosity, ph.reference_temperature,
+                 ph.sutherland_constant, 0, 0, 0, 0, 1, 1e-10, 1)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    npts = q.shape[0]
+    out = np.zeros((npts, 11, 5, 5))
+    st = np.zeros(npts, dtype=np.int32)
+    rc = lib.tlr_lns_points(ctypes.byref(r), npts, _ptr(q), _ptr(out), _ptr(st))
+    if rc:
+        raise TailorError(rc, "tlr_lns_points failed")
+    return st, out
+
+
+def transform_points(alpha: np.ndarray, phys: np.ndarray, metrics: np.ndarray):
+    """Fourier + curvilinear transforms on the GPU for arbitrary blocks."""
+    lib = L.load()
+    a = np.ascontiguousarray(np.stack([alpha.real, alpha.imag], -1), dtype=np.float64)
+    phys = np.ascontiguousarray(phys, dtype=np.float64)
+    met = np.ascontiguousarray(metrics, dtype=np.float64)
+    npts = a.shape[0]
+    four = np.zeros((npts, 7, 25, 2))
+    curv = np.zeros((npts, 7, 25, 2))
+    st = np.zeros(npts, dtype=np.int32)
+    rc = lib.tlr_transform_points(npts, _ptr(a), _ptr(phys), _ptr(met), _ptr(four),
+                                  _ptr(curv), _ptr(st))
+    if rc:
+        raise TailorError(rc, "tlr_transform_points failed")
+    c = lambda v: (v[..., 0] + 1j * v[..., 1]).reshape(npts, 7, 5, 5)
+    return st, c(four), c(curv)
+
+
+def run_pipeline(problem: Problem) -> dict:
+    """Process::run's stage order (Process.cpp:50-56) up to the BCs."""
+    out = {}
+    out["metrics"] = Metrics(problem).compute()
+    out["derivatives"] = BaseFlowDerivatives(problem).compute()
+    out["operator"] = GlobalOperator(problem).assemble()
+    out["bc"] = BoundaryConditions(problem).apply()
+    return out

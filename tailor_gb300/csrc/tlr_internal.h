@@ -1,0 +1,140 @@
+// tlr_internal.h -- context layout and helpers shared by the CUDA sources.
+//
+// Device layout of one problem (N = ny * nz nodes, S = (q_y+1)(q_z+1)
+// stencil blocks per block row):
+//   grid_c      [N][3][2]  complex grid as loaded (validated in place)
+//   base_c      [N][5][2]  complex base flow as loaded
+//   base        [5][N]     real base flow, structure of arrays
+//   metrics     [10][N]    real metrics (Metrics.hpp:15-26 order), SoA
+//   derivs      [25][N]    real derivatives, derivative-major SoA
+//   coef        [CF_COUNT][N] curvilinear LNS coefficients per node, SoA
+//   row_ptr/col [N+1]/[N*S] BSR pattern shared by L and A_bc
+//   L, A        [N*S][25]  double2 (re, im) row-major 5x5 blocks
+//   M, B        [N][25]    double2 block-diagonal mass matrices
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tailor_gb300.h"
+
+namespace tlr {
+
+// Coefficient record, one SoA plane per entry (CurvilinearLNSCoefficients,
+// CurvilinearTransform.hpp:170-188): K0, Kxi, Keta complex (re, im planes),
+// Vxixi, Vxieta, Vetaeta and Gamma real.
+enum : int {
+  CF_K0_RE = 0,
+  CF_K0_IM = 25,
+  CF_KXI_RE = 50,
+  CF_KXI_IM = 75,
+  CF_KETA_RE = 100,
+  CF_KETA_IM = 125,
+  CF_VXX = 150,
+  CF_VXE = 175,
+  CF_VEE = 200,
+  CF_GAMMA = 225,
+  CF_COUNT = 250
+};
+
+// Device status words (atomicMax targets), one per reference check.
+enum : int {
+  ST_STENCIL = 0,
+  ST_NONFINITE = 1,
+  ST_JACOBIAN = 2,
+  ST_COMPLEX = 3,
+  ST_SECOND = 4,
+  ST_NONPOSITIVE = 5,
+  ST_DERIV = 6,
+  ST_COEF = 7,
+  ST_CHAR = 8,
+  ST_TIMEOUT = 9,
+  ST_COUNT = 16
+};
+
+// Reduction scratch slots (doubles).
+enum : int {
+  RD_MINJ = 0,
+  RD_MAXJ = 1,
+  RD_MAXIM = 2,
+  RD_BFIM = 3,
+  RD_CHARIM = 4,
+  RD_COND = 5,
+  RD_COUNT = 8
+};
+
+struct DevRule {
+  int n = 0, q = 0, s = 0;
+  int *off = nullptr;    // [n][s]
+  int *idx = nullptr;    // [n][s]
+  double *w1 = nullptr;  // [n][s]
+  double *w2 = nullptr;  // [n][s]
+  int *centre = nullptr; // [n] slot with offset 0
+  int *order = nullptr;  // [n][s] slots sorted by wrapped index
+};
+
+struct Factor;  // sparse LU state (tlr_lu.cu)
+
+}  // namespace tlr
+
+struct tlr_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  tlr_recipe recipe{};
+  int ny = 0, nz = 0, nn = 0;
+  double span = 0.0;
+  int sx = 0, se = 0, S = 0;
+  long long nnzb = 0;
+  tlr::DevRule xi, eta;
+  std::vector<int> h_xi_off, h_eta_off, h_xi_idx, h_eta_idx;
+  std::vector<double> h_xi_w1, h_xi_w2, h_eta_w1, h_eta_w2;
+
+  double *grid_c = nullptr, *base_c = nullptr, *base = nullptr;
+  double *metrics = nullptr, *derivs = nullptr, *coef = nullptr;
+  int *row_ptr = nullptr, *col = nullptr;
+  double2 *L = nullptr, *M = nullptr, *A = nullptr, *B = nullptr;
+  int *status = nullptr;     // [ST_COUNT]
+  double *red = nullptr;     // [RD_COUNT]
+  double *partial = nullptr; // per-block partial sums for norms
+  int partial_blocks = 0;
+  int *bc_modes = nullptr;   // [nz][2]: incoming and neutral counts
+  double *bc_cond = nullptr; // [nz]: cond(R) per far-field node
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  bool fields = false, have_metrics = false, have_derivs = false;
+  bool assembled = false, have_bc = false;
+  std::string last_error;
+  tlr::Factor *factor = nullptr;
+};
+
+namespace tlr {
+
+int fail(tlr_ctx *ctx, int code, const std::string &msg);
+int cuda_fail(tlr_ctx *ctx, cudaError_t err, const char *what);
+
+#define TLR_CUDA(ctx, call)                                   \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return tlr::cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+// Stage launchers (one .cu file each).
+int run_metrics(tlr_ctx *ctx, tlr_metric_diag *diag);
+int run_derivatives(tlr_ctx *ctx, tlr_deriv_diag *diag);
+int run_pattern(tlr_ctx *ctx);
+int run_assemble(tlr_ctx *ctx, tlr_operator_diag *diag);
+int run_bc(tlr_ctx *ctx, tlr_bc_diag *diag);
+int run_spmv(tlr_ctx *ctx, int which, const double2 *x, double2 *y);
+int frobenius(tlr_ctx *ctx, const double2 *v, long long count, double *out);
+int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
+              double *residual, double *modes, tlr_eig_diag *diag);
+void free_factor(tlr_ctx *ctx);
+
+inline int blocks_for(long long n, int threads) {
+  return static_cast<int>((n + threads - 1) / threads);
+}
+
+}  // namespace tlr

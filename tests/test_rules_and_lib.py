@@ -1,0 +1,58 @@
+"""Shipped FD-q rules (polynomial exactness, like Prepare.cpp:328-437's
+moment checks) and the C ABI library surface (loads, exports every
+function declared in include/tailor_gb300.h) -- no GPU needed."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from tailor_gb300 import rules
+from tailor_gb300 import build as tb
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.mark.parametrize("name", rules.available())
+def test_rule_polynomial_exactness(name):
+    m = re.match(r"N(\d+)_q(\d+)(p?)", name)
+    n, q, per = int(m.group(1)), int(m.group(2)), m.group(3) == "p"
+    r = rules.load_rule(n if per else n + 1, q, per)
+    x = r.nodes
+    for i in range(r.n):
+        if per:
+            xs = x[i] + (r.offsets[i] * (r.period / r.n))
+        else:
+            xs = x[r.indices[i]]
+        h = xs - x[i]
+        scale = np.max(np.abs(h))
+        for k in range(0, min(q, 6) + 1):
+            p = (h / scale) ** k
+            d1 = np.dot(r.weights[1, i], p) * scale
+            d2 = np.dot(r.weights[2, i], p) * scale * scale
+            e1 = 1.0 if k == 1 else 0.0
+            e2 = 2.0 if k == 2 else 0.0
+            assert abs(d1 - e1) < 5e-9 * max(1, np.abs(r.weights[1, i]).sum() * scale)
+            assert abs(d2 - e2) < 5e-7 * max(1, np.abs(r.weights[2, i]).sum() * scale ** 2)
+        assert np.all(r.indices[i] == ((i + r.offsets[i]) % r.n if per else i + r.offsets[i]))
+
+
+def test_library_exports_header_symbols():
+    lib_path = tb.build()
+    header = (ROOT / "include" / "tailor_gb300.h").read_text()
+    declared = set(re.findall(r"^(?:int|void|size_t|const char \*)\s*\*?(tlr_\w+)\(",
+                              header, re.M))
+    assert len(declared) >= 15
+    import ctypes
+    lib = ctypes.CDLL(str(lib_path))
+    for name in sorted(declared):
+        assert hasattr(lib, name), name
+    lib.tlr_status_string.restype = ctypes.c_char_p
+    assert lib.tlr_status_string(0) == b"success"
+    assert lib.tlr_status_string(6) == b"non-positive Jacobian"
+
+
+def test_no_product_import_of_oracle():
+    for p in (ROOT / "tailor_gb300").rglob("*.py"):
+        txt = p.read_text()
+        assert "import oracle" not in txt and "from oracle" not in txt, p
