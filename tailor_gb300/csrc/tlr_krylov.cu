@@ -1,0 +1,416 @@
+// tlr_krylov.cu -- shift-and-invert Krylov-Schur eigen solve
+// (EigenSolver.cpp:103-161: EPS_GNHEP, EPSKRYLOVSCHUR, STSINVERT with a
+// single LU of A - sigma B, EPS_TARGET_MAGNITUDE, relative convergence,
+// EPSComputeError(EPS_ERROR_RELATIVE) for the reported residuals).
+//
+// The operator is OP = (A - sigma B)^-1 B.  Arnoldi runs in FP64 on the
+// device with two-pass classical Gram-Schmidt; the projected problem
+// (ncv x ncv) is reduced to complex Schur form on the host, reordered so
+// the Ritz values of largest |theta| (eigenvalues nearest sigma) lead, and
+// the basis is thick-restarted keeping half of the unconverged part, as in
+// SLEPc's default Krylov-Schur.  lambda = sigma + 1/theta.
+//
+// precision 0 factors K in complex128; precision 1 factors it in complex64
+// and refines every application of K^-1 in FP64 against the FP64 operator
+// (r = y - A w + sigma B w) until ||r|| <= 1e-13 ||y||.
+#include <cublas_v2.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <vector>
+
+#include "tlr_complex.cuh"
+#include "tlr_dense.h"
+#include "tlr_internal.h"
+#include "tlr_lu.h"
+
+namespace tlr {
+namespace {
+
+using cd = std::complex<double>;
+
+__global__ void k_to32(long long n, const double2 *__restrict__ a, float2 *__restrict__ b) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+__global__ void k_add32(long long n, const float2 *__restrict__ d, double2 *__restrict__ w) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    w[i].x += d[i].x;
+    w[i].y += d[i].y;
+  }
+}
+// r = y - (Aw - sigma Bw)   (aw = A w, bw = B w)
+__global__ void k_residual(long long n, const double2 *__restrict__ y,
+                           const double2 *__restrict__ aw, const double2 *__restrict__ bw,
+                           double sr, double si, double2 *__restrict__ r) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double2 b = bw[i];
+    r[i].x = y[i].x - (aw[i].x - (sr * b.x - si * b.y));
+    r[i].y = y[i].y - (aw[i].y - (sr * b.y + si * b.x));
+  }
+}
+// r = a - lambda b
+__global__ void k_axmy(long long n, const double2 *__restrict__ a, const double2 *__restrict__ b,
+                       double lr, double li, double2 *__restrict__ r) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double2 v = b[i];
+    r[i].x = a[i].x - (lr * v.x - li * v.y);
+    r[i].y = a[i].y - (lr * v.y + li * v.x);
+  }
+}
+
+struct Solver {
+  tlr_ctx *ctx;
+  Factor *F;
+  cublasHandle_t h = nullptr;
+  long long n;
+  double sr, si;
+  double2 *V = nullptr, *w = nullptr, *y = nullptr, *r = nullptr, *aw = nullptr,
+          *bw = nullptr, *hv = nullptr, *tmp = nullptr;
+  float2 *x32 = nullptr;
+  int solves = 0, refine = 0;
+  double refine_tol = 1e-13;
+  int max_refine = 30;
+
+  ~Solver() {
+    cudaFree(V); cudaFree(w); cudaFree(y); cudaFree(r); cudaFree(aw); cudaFree(bw);
+    cudaFree(hv); cudaFree(tmp); cudaFree(x32);
+    if (h) cublasDestroy(h);
+  }
+
+  double nrm(const double2 *v) {
+    double out = 0.0;
+    cublasDznrm2(h, (int)n, reinterpret_cast<const cuDoubleComplex *>(v), 1, &out);
+    return out;
+  }
+
+  // out = K^-1 in (FP64 vectors); in may alias nothing else
+  int apply_inverse(const double2 *in, double2 *out) {
+    cudaStream_t st = ctx->stream;
+    const int blocks = blocks_for(n, 256);
+    if (F->prec == 0) {
+      TLR_CUDA(ctx, cudaMemcpyAsync(out, in, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+      int rc = F->solve(ctx, out);
+      ++solves;
+      return rc;
+    }
+    // FP32 factor + FP64 iterative refinement
+    k_to32<<<blocks, 256, 0, st>>>(n, in, x32);
+    int rc = F->solve(ctx, x32);
+    if (rc) return rc;
+    ++solves;
+    TLR_CUDA(ctx, cudaMemsetAsync(out, 0, n * sizeof(double2), st));
+    k_add32<<<blocks, 256, 0, st>>>(n, x32, out);
+    const double ny = nrm(in);
+    for (int it = 0; it < max_refine; ++it) {
+      if ((rc = run_spmv(ctx, TLR_MAT_A, out, aw))) return rc;
+      if ((rc = run_spmv(ctx, TLR_MAT_B, out, bw))) return rc;
+      k_residual<<<blocks, 256, 0, st>>>(n, in, aw, bw, sr, si, r);
+      const double nr = nrm(r);
+      if (nr <= refine_tol * ny) break;
+      k_to32<<<blocks, 256, 0, st>>>(n, r, x32);
+      if ((rc = F->solve(ctx, x32))) return rc;
+      ++solves;
+      ++refine;
+      k_add32<<<blocks, 256, 0, st>>>(n, x32, out);
+    }
+    return TLR_OK;
+  }
+
+  // out = OP in = K^-1 B in
+  int op(const double2 *in, double2 *out) {
+    int rc = run_spmv(ctx, TLR_MAT_B, in, y);
+    if (rc) return rc;
+    return apply_inverse(y, out);
+  }
+};
+
+void fill_start(std::vector<double2> &v, unsigned long long seed) {
+  // deterministic pseudo-random start vector (xorshift64*), entries in (-1, 1)
+  unsigned long long s = seed ? seed : 0x9E3779B97F4A7C15ull;
+  auto next = [&]() {
+    s ^= s >> 12; s ^= s << 25; s ^= s >> 27;
+    return (double)((s * 2685821657736338717ull) >> 11) * (1.0 / 9007199254740992.0);
+  };
+  for (auto &e : v) e = make_double2(2.0 * next() - 1.0, 2.0 * next() - 1.0);
+}
+
+}  // namespace
+
+void free_factor(tlr_ctx *ctx) {
+  if (ctx && ctx->factor) {
+    ctx->factor->release();
+    delete ctx->factor;
+    ctx->factor = nullptr;
+  }
+}
+
+int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
+              double *residual, double *modes, tlr_eig_diag *diag) {
+  using clock = std::chrono::steady_clock;
+  const auto t0 = clock::now();
+  tlr_solve_opts o{};
+  if (opts) o = *opts;
+  const tlr_recipe &rcp = ctx->recipe;
+  const int nev = o.nev > 0 ? o.nev : rcp.nev;
+  const double tol = o.tol > 0 ? o.tol : rcp.tol;
+  const int max_it = o.max_it > 0 ? o.max_it : rcp.max_it;
+  const long long n = 5LL * ctx->nn;
+  int ncv = o.ncv > 0 ? o.ncv : std::max(2 * nev, nev + 15);
+  ncv = (int)std::min<long long>(ncv, n - 1);
+  if (nev < 1 || nev >= ncv || !lambda || !residual)
+    return fail(ctx, TLR_ERR_ARG, "invalid eigen-solver dimensions");
+  // lambda target = Im(omega) - i Re(omega)  (EigenSolver.cpp:118-120)
+  const cd target(rcp.omega_im, -rcp.omega_re);
+  const cd sigma = o.use_sigma ? cd(o.sigma_re, o.sigma_im) : target;
+  const int prec = o.precision == 1 ? 1 : 0;
+
+  // factorisation (reused when sigma and precision are unchanged)
+  Factor *F = ctx->factor;
+  if (F && (F->prec != prec || F->sigma_re != sigma.real() || F->sigma_im != sigma.imag() ||
+            !F->factored)) {
+    if (F->prec != prec) {
+      free_factor(ctx);
+      F = nullptr;
+    } else {
+      F->factored = false;
+    }
+  }
+  double factor_ms = 0.0;
+  int factorizations = 0;
+  if (!F) {
+    F = new Factor();
+    ctx->factor = F;
+    int rc = F->setup(ctx, prec, 48);
+    if (rc) {
+      free_factor(ctx);
+      return rc;
+    }
+  }
+  if (!F->factored) {
+    double anorm = 0.0;
+    int rc = frobenius(ctx, ctx->A, ctx->nnzb * 25, &anorm);
+    if (rc) return rc;
+    const double tiny = 1e-10 * anorm / std::sqrt((double)n);
+    TLR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    rc = F->factor(ctx, sigma.real(), sigma.imag(), tiny);
+    if (rc) return rc;
+    TLR_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    TLR_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    factor_ms = ms;
+    F->sigma_re = sigma.real();
+    F->sigma_im = sigma.imag();
+    factorizations = 1;
+  }
+  const auto t1 = clock::now();
+
+  Solver S;
+  S.ctx = ctx;
+  S.F = F;
+  S.n = n;
+  S.sr = sigma.real();
+  S.si = sigma.imag();
+  if (cublasCreate(&S.h) != CUBLAS_STATUS_SUCCESS)
+    return fail(ctx, TLR_ERR_CUDA, "cublasCreate failed");
+  cublasSetStream(S.h, ctx->stream);
+  const size_t vb = n * sizeof(double2);
+  TLR_CUDA(ctx, cudaMalloc(&S.V, vb * (ncv + 1)));
+  TLR_CUDA(ctx, cudaMalloc(&S.w, vb));
+  TLR_CUDA(ctx, cudaMalloc(&S.y, vb));
+  TLR_CUDA(ctx, cudaMalloc(&S.r, vb));
+  TLR_CUDA(ctx, cudaMalloc(&S.aw, vb));
+  TLR_CUDA(ctx, cudaMalloc(&S.bw, vb));
+  TLR_CUDA(ctx, cudaMalloc(&S.hv, sizeof(double2) * (ncv + 1) * (ncv + 1)));
+  TLR_CUDA(ctx, cudaMalloc(&S.tmp, vb * ncv));
+  if (prec == 1) TLR_CUDA(ctx, cudaMalloc(&S.x32, n * sizeof(float2)));
+
+  std::vector<double2> v0(n);
+  if (o.start) {
+    for (long long i = 0; i < n; ++i) v0[i] = make_double2(o.start[2 * i], o.start[2 * i + 1]);
+  } else {
+    fill_start(v0, 0x5eed0001ull);
+  }
+  TLR_CUDA(ctx, cudaMemcpyAsync(S.V, v0.data(), vb, cudaMemcpyHostToDevice, ctx->stream));
+  {
+    double nv = S.nrm(S.V);
+    if (!(nv > 0)) return fail(ctx, TLR_ERR_ARG, "start vector is zero");
+    const double inv = 1.0 / nv;
+    cublasZdscal(S.h, (int)n, &inv, reinterpret_cast<cuDoubleComplex *>(S.V), 1);
+  }
+  dense::Mat H(ncv + 1, ncv);
+  int k = 0, nconv = 0, it = 0, reason = 0;
+  std::vector<cd> theta(ncv);
+  dense::Mat Tq, Qq;
+  std::vector<cd> hcol(ncv + 1), hcol2(ncv + 1);
+  const cuDoubleComplex one = {1.0, 0.0}, zero = {0.0, 0.0}, mone = {-1.0, 0.0};
+  auto Vc = [&](int j) { return reinterpret_cast<cuDoubleComplex *>(S.V + (size_t)j * n); };
+  while (true) {
+    ++it;
+    // Arnoldi expansion k .. ncv-1
+    for (int j = k; j < ncv; ++j) {
+      int rc = S.op(S.V + (size_t)j * n, S.w);
+      if (rc) return rc;
+      for (int pass = 0; pass < 2; ++pass) {
+        cublasZgemv(S.h, CUBLAS_OP_C, (int)n, j + 1, &one, Vc(0), (int)n,
+                    reinterpret_cast<cuDoubleComplex *>(S.w), 1, &zero,
+                    reinterpret_cast<cuDoubleComplex *>(S.hv), 1);
+        cublasZgemv(S.h, CUBLAS_OP_N, (int)n, j + 1, &mone, Vc(0), (int)n,
+                    reinterpret_cast<cuDoubleComplex *>(S.hv), 1, &one,
+                    reinterpret_cast<cuDoubleComplex *>(S.w), 1);
+        TLR_CUDA(ctx, cudaMemcpyAsync(pass ? hcol2.data() : hcol.data(), S.hv,
+                                      sizeof(double2) * (j + 1), cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+      }
+      const double beta = S.nrm(S.w);
+      TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      for (int i = 0; i <= j; ++i) H(i, j) = hcol[i] + hcol2[i];
+      H(j + 1, j) = beta;
+      if (!(beta > 0)) return fail(ctx, TLR_ERR_NOT_CONVERGED, "Arnoldi breakdown");
+      const double inv = 1.0 / beta;
+      TLR_CUDA(ctx, cudaMemcpyAsync(S.V + (size_t)(j + 1) * n, S.w, vb,
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+      cublasZdscal(S.h, (int)n, &inv, Vc(j + 1), 1);
+    }
+    // projected problem: Schur form, wanted first
+    dense::Mat T(ncv, ncv), Q(ncv, ncv);
+    for (int j = 0; j < ncv; ++j) {
+      for (int i = 0; i < ncv; ++i) T(i, j) = H(i, j);
+      Q(j, j) = 1.0;
+    }
+    dense::hessenberg(T, Q);
+    if (!dense::schur(T, Q))
+      return fail(ctx, TLR_ERR_NOT_CONVERGED, "projected Schur form did not converge");
+    for (int pos = 0; pos < ncv; ++pos) {  // selection by |theta|, stable
+      int best = pos;
+      for (int q = pos + 1; q < ncv; ++q)
+        if (std::abs(T(q, q)) > std::abs(T(best, best))) best = q;
+      for (int q = best - 1; q >= pos; --q) dense::swap_adjacent(T, Q, q);
+    }
+    const double beta = std::abs(H(ncv, ncv - 1));
+    std::vector<cd> b(ncv);
+    for (int i = 0; i < ncv; ++i) b[i] = beta * Q(ncv - 1, i);
+    nconv = 0;
+    for (int i = 0; i < ncv && nconv < ncv; ++i) {
+      const auto yv = dense::tri_eigvec(T, i);
+      cd dot = 0.0;
+      double ny = 0.0;
+      for (int q = 0; q <= i; ++q) {
+        dot += b[q] * yv[q];
+        ny += std::norm(yv[q]);
+      }
+      const double res = std::abs(dot) / std::sqrt(ny);
+      if (res <= tol * std::abs(T(i, i)) && nconv == i) ++nconv;
+      else break;
+    }
+    for (int i = 0; i < ncv; ++i) theta[i] = T(i, i);
+    if (nconv >= nev || it >= max_it) {
+      reason = nconv >= nev ? 1 : -1;
+      Tq = T;
+      Qq = Q;
+      break;
+    }
+    // thick restart
+    int l = nconv + (ncv - nconv) / 2;
+    l = std::max(l, 1);
+    std::vector<double2> qh((size_t)ncv * l);
+    for (int j = 0; j < l; ++j)
+      for (int i = 0; i < ncv; ++i) qh[(size_t)j * ncv + i] = make_double2(Q(i, j).real(), Q(i, j).imag());
+    double2 *qd = nullptr;
+    TLR_CUDA(ctx, cudaMallocAsync(&qd, qh.size() * sizeof(double2), ctx->stream));
+    TLR_CUDA(ctx, cudaMemcpyAsync(qd, qh.data(), qh.size() * sizeof(double2),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    cublasZgemm(S.h, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, l, ncv, &one, Vc(0), (int)n,
+                reinterpret_cast<cuDoubleComplex *>(qd), ncv, &zero,
+                reinterpret_cast<cuDoubleComplex *>(S.tmp), (int)n);
+    TLR_CUDA(ctx, cudaMemcpyAsync(S.V, S.tmp, vb * l, cudaMemcpyDeviceToDevice, ctx->stream));
+    TLR_CUDA(ctx, cudaMemcpyAsync(S.V + (size_t)l * n, S.V + (size_t)ncv * n, vb,
+                                  cudaMemcpyDeviceToDevice, ctx->stream));
+    cudaFreeAsync(qd, ctx->stream);
+    dense::Mat Hn(ncv + 1, ncv);
+    for (int j = 0; j < l; ++j) {
+      for (int i = 0; i < l; ++i) Hn(i, j) = T(i, j);
+      Hn(l, j) = b[j];
+    }
+    H = Hn;
+    k = l;
+  }
+  const auto t2 = clock::now();
+  // Ritz vectors x_i = V Q y_i, eigenvalues, explicit residuals
+  const int nout = std::min(nev, nconv > 0 ? std::max(nconv, nev) : nev);
+  std::vector<double2> yh((size_t)ncv * nout);
+  for (int i = 0; i < nout; ++i) {
+    const auto yv = dense::tri_eigvec(Tq, i);
+    for (int q = 0; q < ncv; ++q) {
+      cd s = 0.0;
+      for (int t = 0; t <= i; ++t) s += Qq(q, t) * yv[t];
+      yh[(size_t)i * ncv + q] = make_double2(s.real(), s.imag());
+    }
+  }
+  double2 *yd = nullptr;
+  TLR_CUDA(ctx, cudaMalloc(&yd, yh.size() * sizeof(double2)));
+  TLR_CUDA(ctx, cudaMemcpyAsync(yd, yh.data(), yh.size() * sizeof(double2),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  cublasZgemm(S.h, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, nout, ncv, &one, Vc(0), (int)n,
+              reinterpret_cast<cuDoubleComplex *>(yd), ncv, &zero,
+              reinterpret_cast<cuDoubleComplex *>(S.tmp), (int)n);
+  cudaFree(yd);
+  double maxerr = 0.0;
+  std::vector<double2> hostv;
+  for (int i = 0; i < nout; ++i) {
+    double2 *x = S.tmp + (size_t)i * n;
+    const double nx = S.nrm(x);
+    const double inv = 1.0 / nx;
+    cublasZdscal(S.h, (int)n, &inv, reinterpret_cast<cuDoubleComplex *>(x), 1);
+    const cd lam = sigma + 1.0 / theta[i];
+    int rc = run_spmv(ctx, TLR_MAT_A, x, S.aw);
+    if (rc) return rc;
+    if ((rc = run_spmv(ctx, TLR_MAT_B, x, S.bw))) return rc;
+    k_axmy<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, S.aw, S.bw, lam.real(), lam.imag(),
+                                                        S.r);
+    const double res = S.nrm(S.r) / std::abs(lam);
+    lambda[2 * i] = lam.real();
+    lambda[2 * i + 1] = lam.imag();
+    residual[i] = res;
+    maxerr = std::max(maxerr, res);
+    if (modes)
+      TLR_CUDA(ctx, cudaMemcpyAsync(modes + (size_t)2 * n * i, x, vb, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+  }
+  TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const auto t3 = clock::now();
+  if (diag) {
+    tlr_eig_diag d{};
+    d.requested = nev;
+    d.converged = std::min(nconv, nev) == nev ? nout : std::min(nconv, nout);
+    d.iterations = it;
+    d.reason = reason;
+    d.target_re = target.real();
+    d.target_im = target.imag();
+    d.max_relative_error = maxerr;
+    d.factorizations = factorizations;
+    d.solves = S.solves;
+    d.refinement_steps = S.refine;
+    d.factor_ms = factor_ms;
+    d.krylov_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+    d.total_ms = std::chrono::duration<double, std::milli>(t3 - t0).count();
+    d.factor_flops = F->sym.flops;
+    *diag = d;
+  }
+  if (reason <= 0) {
+    char buf[160];
+    snprintf(buf, sizeof(buf),
+             "Krylov-Schur failed to converge (%d eigenpairs after %d iterations)", nconv, it);
+    return fail(ctx, TLR_ERR_NOT_CONVERGED, buf);
+  }
+  return TLR_OK;
+}
+
+}  // namespace tlr

@@ -1,0 +1,752 @@
+// tlr_lu.cu -- multifrontal LU of K = A_bc - sigma B_bc and its
+// triangular solves, level-batched, in FP64 (the drop-in form) or FP32
+// (the mixed form, refined in FP64 by the caller).
+//
+// Every front is a dense column-major m x m matrix in one device pool.
+// Fronts of one elimination-tree level are processed together: one launch
+// assembles all their K blocks, one launch per child slot extend-adds the
+// children's Schur complements, and each panel step of width w runs five
+// launches over all fronts that still have pivots left:
+//   k_panel        partial pivoting over the fully summed rows (one CTA/front)
+//   k_swap         the step's row interchanges on the other columns
+//   k_trsm_border  L21 = F21 U_kk^-1 for the front's border rows
+//   k_trsm_urow    U12 = L_kk^-1 F12
+//   k_gemm         trailing update F22 -= L21 U12 (the Schur complement)
+// Pivot search is restricted to fully summed rows (no delayed pivots); an
+// exactly zero pivot column is perturbed and counted, and the caller
+// refines.  The solves reuse the same level/step schedule.
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "tlr_complex.cuh"
+#include "tlr_internal.h"
+#include "tlr_lu.h"
+
+namespace tlr {
+namespace {
+
+constexpr int kTile = 64;
+
+// ------------------------------------------------------------ factorization
+
+template <class C>
+__global__ void k_asm(const AsmEntry *__restrict__ e, long long n,
+                      const double2 *__restrict__ A, const double2 *__restrict__ B,
+                      double sr, double si, C *__restrict__ pool,
+                      const DevFront *__restrict__ fr) {
+  const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n * 25) return;
+  const AsmEntry en = e[x / 25];
+  const int rc = (int)(x % 25), r = rc / 5, c = rc % 5;
+  double2 v = A[(long long)en.k * 25 + rc];
+  if (en.bnode >= 0) {
+    const double2 b = B[(long long)en.bnode * 25 + rc];
+    v.x -= sr * b.x - si * b.y;
+    v.y -= sr * b.y + si * b.x;
+  }
+  const DevFront f = fr[en.front];
+  pool[f.off + (long long)(en.col * 5 + c) * f.m + en.row * 5 + r] = from64<C>(v);
+}
+
+template <class C>
+__global__ void k_extend(const int *__restrict__ kids, const DevFront *__restrict__ fr,
+                         const int *__restrict__ cmap, C *__restrict__ pool) {
+  const int child = kids[blockIdx.y];
+  const DevFront fc = fr[child];
+  const DevFront fp = fr[fc.parent];
+  const int bc = fc.m - fc.p;
+  const long long total = (long long)bc * bc;
+  const int *map = cmap + fc.cmap_off;
+  const C *cb = pool + fc.off;
+  C *pf = pool + fp.off;
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    const int rr = (int)(x % bc), cc = (int)(x / bc);
+    const int pr = map[rr / 5] * 5 + rr % 5, pc = map[cc / 5] * 5 + cc % 5;
+    const C v = cb[(long long)(fc.p + cc) * fc.m + fc.p + rr];
+    C &d = pf[(long long)pc * fp.m + pr];
+    d = cadd(d, v);
+  }
+}
+
+template <class C>
+__global__ void __launch_bounds__(256)
+    k_panel(const int *__restrict__ fl, int s, int w, C *__restrict__ pool,
+            const DevFront *__restrict__ fr, int *__restrict__ ipiv,
+            int *__restrict__ pert, double tiny) {
+  using T = typename Real<C>::T;
+  __shared__ T sval[256];
+  __shared__ int sidx[256];
+  __shared__ int piv_sh;
+  const DevFront f = fr[fl[blockIdx.x]];
+  C *F = pool + f.off;
+  const int m = f.m, p = f.p;
+  const int k0 = s * w, ww = min(w, p - k0);
+  const int tid = threadIdx.x;
+  for (int j = 0; j < ww; ++j) {
+    const int col = k0 + j;
+    T best = -1;
+    int bi = col;
+    for (int r = col + tid; r < p; r += blockDim.x) {
+      const T a = cabs1(F[(long long)col * m + r]);
+      if (a > best) { best = a; bi = r; }
+    }
+    sval[tid] = best;
+    sidx[tid] = bi;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (tid < o) {
+        const T a = sval[tid + o];
+        const int ia = sidx[tid + o];
+        if (a > sval[tid] || (a == sval[tid] && ia < sidx[tid])) {
+          sval[tid] = a;
+          sidx[tid] = ia;
+        }
+      }
+      __syncthreads();
+    }
+    if (tid == 0) {
+      piv_sh = sidx[0];
+      ipiv[f.toff + col] = sidx[0];
+    }
+    __syncthreads();
+    const int pr = piv_sh;
+    if (pr != col) {
+      for (int c = k0 + tid; c < k0 + ww; c += blockDim.x) {
+        const C t = F[(long long)c * m + col];
+        F[(long long)c * m + col] = F[(long long)c * m + pr];
+        F[(long long)c * m + pr] = t;
+      }
+    }
+    __syncthreads();
+    C pv = F[(long long)col * m + col];
+    if (cabs1(pv) == T(0)) {
+      pv = cmake<C>((T)tiny, 0);
+      if (tid == 0) {
+        F[(long long)col * m + col] = pv;
+        atomicAdd(pert, 1);
+      }
+    }
+    const C inv = cinv(pv);
+    for (int r = col + 1 + tid; r < p; r += blockDim.x)
+      F[(long long)col * m + r] = cmul(F[(long long)col * m + r], inv);
+    __syncthreads();
+    const int nr = p - col - 1, nc = k0 + ww - col - 1;
+    for (int x = tid; x < nr * nc; x += blockDim.x) {
+      const int r = col + 1 + x % nr, c = col + 1 + x / nr;
+      F[(long long)c * m + r] =
+          cfms(F[(long long)c * m + r], F[(long long)col * m + r], F[(long long)c * m + col]);
+    }
+    __syncthreads();
+  }
+}
+
+template <class C>
+__global__ void k_swap(const int *__restrict__ fl, int s, int w, C *__restrict__ pool,
+                       const DevFront *__restrict__ fr, const int *__restrict__ ipiv) {
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int k0 = s * w, ww = min(w, f.p - k0);
+  const int c0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c0 >= f.m - ww) return;
+  const int c = c0 < k0 ? c0 : c0 + ww;
+  C *col = pool + f.off + (long long)c * f.m;
+  for (int j = 0; j < ww; ++j) {
+    const int r1 = k0 + j, r2 = ipiv[f.toff + k0 + j];
+    if (r2 != r1) {
+      const C t = col[r1];
+      col[r1] = col[r2];
+      col[r2] = t;
+    }
+  }
+}
+
+// L21 = F21 U_kk^-1 on the border rows p..m-1 of the panel columns.
+template <class C>
+__global__ void k_trsm_border(const int *__restrict__ fl, int s, int w, C *__restrict__ pool,
+                              const DevFront *__restrict__ fr) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  C *U = reinterpret_cast<C *>(sm);          // ww x ww, column-major
+  C *dinv = U + w * w;
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int k0 = s * w, ww = min(w, f.p - k0);
+  const int m = f.m;
+  C *F = pool + f.off;
+  for (int x = threadIdx.x; x < ww * ww; x += blockDim.x) {
+    const int r = x % ww, c = x / ww;
+    U[c * w + r] = F[(long long)(k0 + c) * m + k0 + r];
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < ww; c += blockDim.x) dinv[c] = cinv(U[c * w + c]);
+  __syncthreads();
+  const int r = f.p + blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= m) return;
+  C x[64];
+#pragma unroll 1
+  for (int c = 0; c < ww; ++c) {
+    C v = F[(long long)(k0 + c) * m + r];
+    for (int cp = 0; cp < c; ++cp) v = cfms(v, x[cp], U[c * w + cp]);
+    x[c] = cmul(v, dinv[c]);
+    F[(long long)(k0 + c) * m + r] = x[c];
+  }
+}
+
+// U12 = L_kk^-1 F12 for columns k0+ww..m-1 (unit lower L_kk).
+template <class C>
+__global__ void k_trsm_urow(const int *__restrict__ fl, int s, int w, C *__restrict__ pool,
+                            const DevFront *__restrict__ fr) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  C *Lk = reinterpret_cast<C *>(sm);
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int k0 = s * w, ww = min(w, f.p - k0);
+  const int m = f.m;
+  C *F = pool + f.off;
+  for (int x = threadIdx.x; x < ww * ww; x += blockDim.x) {
+    const int r = x % ww, c = x / ww;
+    Lk[c * w + r] = F[(long long)(k0 + c) * m + k0 + r];
+  }
+  __syncthreads();
+  const int c = k0 + ww + blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m) return;
+  C *col = F + (long long)c * m + k0;
+  C x[64];
+  for (int r = 0; r < ww; ++r) {
+    C v = col[r];
+    for (int rp = 0; rp < r; ++rp) v = cfms(v, Lk[rp * w + r], x[rp]);
+    x[r] = v;
+    col[r] = v;
+  }
+}
+
+// Trailing update F[k0+ww:m, k0+ww:m] -= F[k0+ww:m, k0:k0+ww] F[k0:k0+ww, k0+ww:m]
+// over a flat list of 64x64 tiles of all participating fronts.
+template <class C>
+__global__ void __launch_bounds__(256)
+    k_gemm(const int *__restrict__ fl, const int *__restrict__ prefix, int nf, int s,
+           int w, C *__restrict__ pool, const DevFront *__restrict__ fr) {
+  constexpr int KC = 16;
+  __shared__ C As[KC][kTile];
+  __shared__ C Bs[KC][kTile + 1];
+  const int t = blockIdx.x;
+  int lo = 0, hi = nf;  // find the front owning tile t
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) / 2;
+    if (prefix[mid] <= t) lo = mid; else hi = mid;
+  }
+  const DevFront f = fr[fl[lo]];
+  const int m = f.m, k0 = s * w, ww = min(w, f.p - k0);
+  const int base = k0 + ww, ext = m - base;
+  const int nt = (ext + kTile - 1) / kTile;
+  const int lt = t - prefix[lo];
+  const int R0 = base + (lt % nt) * kTile, C0 = base + (lt / nt) * kTile;
+  C *F = pool + f.off;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  C acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = czero<C>();
+  for (int kk = 0; kk < ww; kk += KC) {
+    for (int x = threadIdx.x; x < KC * kTile; x += 256) {
+      const int r = x % kTile, k = x / kTile;
+      const int gr = R0 + r, gk = k0 + kk + k;
+      As[k][r] = (gr < m && kk + k < ww) ? F[(long long)gk * m + gr] : czero<C>();
+      const int cc = x / KC, kb = x % KC;
+      const int gc = C0 + cc;
+      Bs[kb][cc] = (gc < m && kk + kb < ww) ? F[(long long)gc * m + k0 + kk + kb] : czero<C>();
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < KC; ++k) {
+      C a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[k][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[k][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = cfma(acc[i][j], a[i], b[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int gc = C0 + ty + 16 * j;
+    if (gc >= m) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int gr = R0 + tx + 16 * i;
+      if (gr >= m) continue;
+      C &d = F[(long long)gc * m + gr];
+      d = csub(d, acc[i][j]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ solves
+
+// t[i] = b[unknown of front row perm[i]] for pivot rows, 0 for border rows.
+template <class C>
+__global__ void k_sgather(const int *__restrict__ fl, const DevFront *__restrict__ fr,
+                          const int *__restrict__ nodes, const int *__restrict__ perm,
+                          const C *__restrict__ b, C *__restrict__ work) {
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= f.m) return;
+  C v = czero<C>();
+  if (i < f.p) {
+    const int q = perm[f.toff + i];
+    v = b[(long long)nodes[f.node_off + q / 5] * 5 + q % 5];
+  }
+  work[f.toff + i] = v;
+}
+
+// parent's t += child's border update, at the permuted positions.
+template <class C>
+__global__ void k_saddchild(const int *__restrict__ kids, const DevFront *__restrict__ fr,
+                            const int *__restrict__ pmap, C *__restrict__ work) {
+  const DevFront fc = fr[kids[blockIdx.y]];
+  const DevFront fp = fr[fc.parent];
+  const int bc = fc.m - fc.p;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= bc) return;
+  const int q = pmap[fc.toff + x];
+  C &d = work[fp.toff + q];
+  d = cadd(d, work[fc.toff + fc.p + x]);
+}
+
+// forward: unit-lower diagonal block of step s (one warp per front)
+template <class C>
+__global__ void k_fwd_diag(const int *__restrict__ fl, int s, int w, const C *__restrict__ pool,
+                           const DevFront *__restrict__ fr, C *__restrict__ work) {
+  const DevFront f = fr[fl[blockIdx.x]];
+  const int k0 = s * w, ww = min(w, f.p - k0);
+  const int lane = threadIdx.x;
+  const C *F = pool + f.off;
+  C *t = work + f.toff + k0;
+  const int m = f.m;
+  C mine[2];
+  mine[0] = lane < ww ? t[lane] : czero<C>();
+  mine[1] = lane + 32 < ww ? t[lane + 32] : czero<C>();
+  for (int r = 0; r < ww; ++r) {
+    const C xr = r < 32 ? mine[0] : mine[1];
+    const C xb = cmake<C>(__shfl_sync(0xffffffffu, xr.x, r & 31),
+                          __shfl_sync(0xffffffffu, xr.y, r & 31));
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int rr = lane + 32 * h;
+      if (rr > r && rr < ww) mine[h] = cfms(mine[h], F[(long long)(k0 + r) * m + k0 + rr], xb);
+    }
+  }
+  if (lane < ww) t[lane] = mine[0];
+  if (lane + 32 < ww) t[lane + 32] = mine[1];
+}
+
+// forward: rows k0+ww..m-1 -= L[:, k0:k0+ww] t[k0:k0+ww]
+template <class C>
+__global__ void k_fwd_gemv(const int *__restrict__ fl, int s, int w, const C *__restrict__ pool,
+                           const DevFront *__restrict__ fr, C *__restrict__ work) {
+  __shared__ C xs[64];
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int k0 = s * w, ww = min(w, f.p - k0);
+  C *t = work + f.toff;
+  for (int c = threadIdx.x; c < ww; c += blockDim.x) xs[c] = t[k0 + c];
+  __syncthreads();
+  const int r = k0 + ww + blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= f.m) return;
+  const C *F = pool + f.off;
+  C v = t[r];
+  for (int c = 0; c < ww; ++c) v = cfms(v, F[(long long)(k0 + c) * f.m + r], xs[c]);
+  t[r] = v;
+}
+
+// backward: t[p:m] = x at the border unknowns
+template <class C>
+__global__ void k_bgather(const int *__restrict__ fl, const DevFront *__restrict__ fr,
+                          const int *__restrict__ nodes, const C *__restrict__ x,
+                          C *__restrict__ work) {
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int i = f.p + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= f.m) return;
+  work[f.toff + i] = x[(long long)nodes[f.node_off + i / 5] * 5 + i % 5];
+}
+
+// backward: partial[front][chunk][r] = sum over a column chunk of U[k0+r, c] t[c]
+template <class C>
+__global__ void k_bwd_gemv(const int *__restrict__ fl, int s, int w, int chunk,
+                           const C *__restrict__ pool, const DevFront *__restrict__ fr,
+                           const C *__restrict__ work, double2 *__restrict__ partial,
+                           int max_chunks) {
+  __shared__ C red[8][64];
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int k0 = s * w, ww = min(w, f.p - k0);
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int cbeg = k0 + ww + blockIdx.x * chunk;
+  const int cend = min(f.m, cbeg + chunk);
+  const C *F = pool + f.off;
+  const C *t = work + f.toff;
+  C a0 = czero<C>(), a1 = czero<C>();
+  for (int c = cbeg + wp; c < cend; c += 8) {
+    const C tc = t[c];
+    const C *colp = F + (long long)c * f.m + k0;
+    if (lane < ww) a0 = cfma(a0, colp[lane], tc);
+    if (lane + 32 < ww) a1 = cfma(a1, colp[lane + 32], tc);
+  }
+  red[wp][lane] = a0;
+  red[wp][lane + 32] = a1;
+  __syncthreads();
+  if (threadIdx.x < ww) {
+    C v = czero<C>();
+    for (int q = 0; q < 8; ++q) v = cadd(v, red[q][threadIdx.x]);
+    partial[((long long)blockIdx.y * max_chunks + blockIdx.x) * 64 + threadIdx.x] = to64(v);
+  }
+}
+
+// backward: t[k0:k0+ww] = U_kk^-1 (t - sum of partials); one warp per front
+template <class C>
+__global__ void k_bwd_diag(const int *__restrict__ fl, int s, int w, int nchunks_max,
+                           int chunk, const C *__restrict__ pool,
+                           const DevFront *__restrict__ fr, C *__restrict__ work,
+                           const double2 *__restrict__ partial) {
+  const DevFront f = fr[fl[blockIdx.x]];
+  const int k0 = s * w, ww = min(w, f.p - k0);
+  const int lane = threadIdx.x;
+  const int ext = f.m - k0 - ww;
+  const int nch = ext > 0 ? (ext + chunk - 1) / chunk : 0;
+  C *t = work + f.toff + k0;
+  const C *F = pool + f.off;
+  const int m = f.m;
+  C mine[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int r = lane + 32 * h;
+    if (r < ww) {
+      double2 acc = make_double2(0, 0);
+      for (int q = 0; q < nch; ++q) {
+        const double2 pv = partial[((long long)blockIdx.x * nchunks_max + q) * 64 + r];
+        acc.x += pv.x;
+        acc.y += pv.y;
+      }
+      mine[h] = csub(t[r], from64<C>(acc));
+    } else {
+      mine[h] = czero<C>();
+    }
+  }
+  for (int r = ww - 1; r >= 0; --r) {
+    const int hr = r >> 5;
+    C xr = hr ? mine[1] : mine[0];
+    if (lane == (r & 31)) xr = cmul(xr, cinv(F[(long long)(k0 + r) * m + k0 + r]));
+    const C xb = cmake<C>(__shfl_sync(0xffffffffu, xr.x, r & 31),
+                          __shfl_sync(0xffffffffu, xr.y, r & 31));
+    if (lane == (r & 31)) {
+      if (hr) mine[1] = xb; else mine[0] = xb;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int rr = lane + 32 * h;
+      if (rr < r) mine[h] = cfms(mine[h], F[(long long)(k0 + r) * m + k0 + rr], xb);
+    }
+  }
+  if (lane < ww) t[lane] = mine[0];
+  if (lane + 32 < ww) t[lane + 32] = mine[1];
+}
+
+template <class C>
+__global__ void k_bscatter(const int *__restrict__ fl, const DevFront *__restrict__ fr,
+                           const int *__restrict__ nodes, const C *__restrict__ work,
+                           C *__restrict__ x) {
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= f.p) return;
+  x[(long long)nodes[f.node_off + i / 5] * 5 + i % 5] = work[f.toff + i];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------- host
+
+int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
+  prec = precision;
+  w = precision == 0 ? 32 : 64;
+  std::vector<int> rp(ctx->nn + 1), cl((size_t)ctx->nnzb);
+  TLR_CUDA(ctx, cudaMemcpy(rp.data(), ctx->row_ptr, rp.size() * sizeof(int),
+                           cudaMemcpyDeviceToHost));
+  TLR_CUDA(ctx, cudaMemcpy(cl.data(), ctx->col, cl.size() * sizeof(int),
+                           cudaMemcpyDeviceToHost));
+  int rc = build_symbolic(ctx->ny, ctx->nz, ctx->h_xi_idx, ctx->sx, ctx->h_eta_off,
+                          ctx->se, rp, cl, leaf, sym);
+  if (rc) {
+    char buf[96];
+    snprintf(buf, sizeof(buf), "symbolic analysis failed (code %d)", rc);
+    return fail(ctx, TLR_ERR_ARG, buf);
+  }
+  const int nf = (int)sym.fronts.size();
+  std::vector<DevFront> df(nf);
+  std::vector<int> nodes;
+  nodes.reserve(sym.work_elems / 5);
+  for (int t = 0; t < nf; ++t) {
+    const FrontInfo &f = sym.fronts[t];
+    DevFront &d = df[t];
+    d.off = f.off;
+    d.toff = f.toff;
+    d.p = f.p;
+    d.m = f.m;
+    d.parent = f.parent;
+    d.cmap_off = sym.cmap_off[t] < 0 ? 0 : sym.cmap_off[t];
+    d.node_off = (int)(f.toff / 5);
+  }
+  nodes.assign(sym.work_elems / 5, 0);
+  for (int t = 0; t < nf; ++t) {
+    const FrontInfo &f = sym.fronts[t];
+    int a = df[t].node_off;
+    for (int u : f.piv) nodes[a++] = u;
+    for (int v : f.border) nodes[a++] = v;
+  }
+  // schedules: per level, fronts sorted by p descending; per step prefix
+  std::vector<int> sched;
+  levels.clear();
+  for (size_t h = 0; h < sym.levels.size(); ++h) {
+    Level L;
+    std::vector<int> fl = sym.levels[h];
+    std::sort(fl.begin(), fl.end(),
+              [&](int a, int b) { return sym.fronts[a].p > sym.fronts[b].p; });
+    L.nfronts = (int)fl.size();
+    L.fronts_off = (int)sched.size();
+    sched.insert(sched.end(), fl.begin(), fl.end());
+    L.max_m = 0;
+    for (int t : fl) L.max_m = std::max(L.max_m, sym.fronts[t].m);
+    for (int slot = 0; slot < 2; ++slot) {
+      std::vector<int> kids;
+      for (int t : fl)
+        if ((int)sym.fronts[t].children.size() > slot) kids.push_back(sym.fronts[t].children[slot]);
+      L.kids[slot] = (int)kids.size();
+      L.kids_off[slot] = (int)sched.size();
+      int mb = 0;
+      for (int c : kids) mb = std::max(mb, sym.fronts[c].m - sym.fronts[c].p);
+      L.kids_maxb[slot] = mb;
+      sched.insert(sched.end(), kids.begin(), kids.end());
+    }
+    L.entry_begin = sym.level_entry_begin[h];
+    L.entry_end = sym.level_entry_begin[h + 1];
+    L.pool_begin = sym.fronts[fl.back()].off;
+    L.pool_end = 0;
+    for (int t : fl) {
+      L.pool_begin = std::min(L.pool_begin, sym.fronts[t].off);
+      L.pool_end = std::max(L.pool_end, sym.fronts[t].off + (long long)sym.fronts[t].m * sym.fronts[t].m);
+    }
+    const int pmax = sym.fronts[fl.front()].p;
+    const int nsteps = (pmax + w - 1) / w;
+    for (int s = 0; s < nsteps; ++s) {
+      Step st;
+      st.nf = 0;
+      for (int t : fl)
+        if (sym.fronts[t].p > s * w) ++st.nf;
+      st.max_m = 0;
+      st.max_b = 0;
+      st.max_ext = 0;
+      st.prefix_off = (int)sched.size();
+      int acc = 0;
+      for (int q = 0; q < st.nf; ++q) {
+        const FrontInfo &f = sym.fronts[fl[q]];
+        const int ww = std::min(w, f.p - s * w);
+        const int ext = f.m - s * w - ww;
+        const int nt = (ext + kTile - 1) / kTile;
+        sched.push_back(acc);
+        acc += nt * nt;
+        st.max_m = std::max(st.max_m, f.m);
+        st.max_b = std::max(st.max_b, f.m - f.p);
+        st.max_ext = std::max(st.max_ext, ext);
+      }
+      sched.push_back(acc);
+      st.tiles = acc;
+      L.steps.push_back(st);
+    }
+    levels.push_back(L);
+  }
+  max_chunks = 1;
+  for (auto &L : levels)
+    for (auto &st : L.steps) max_chunks = std::max(max_chunks, (st.max_ext + kChunk - 1) / kChunk);
+  int max_lvl_fronts = 1;
+  for (auto &L : levels) max_lvl_fronts = std::max(max_lvl_fronts, L.nfronts);
+  const size_t csize = prec == 0 ? sizeof(double2) : sizeof(float2);
+  auto alloc = [&](void **p, size_t bytes) -> int {
+    cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) {
+      *p = nullptr;
+      return fail(ctx, TLR_ERR_NOMEM, std::string("factor allocation failed: ") +
+                                          cudaGetErrorString(e));
+    }
+    return TLR_OK;
+  };
+  if ((rc = alloc(&pool, (size_t)sym.pool_elems * csize)) ||
+      (rc = alloc(&work, (size_t)sym.work_elems * csize)) ||
+      (rc = alloc((void **)&d_fronts, nf * sizeof(DevFront))) ||
+      (rc = alloc((void **)&d_entries, sym.entries.size() * sizeof(AsmEntry))) ||
+      (rc = alloc((void **)&d_cmap, sym.cmap.size() * sizeof(int))) ||
+      (rc = alloc((void **)&d_nodes, nodes.size() * sizeof(int))) ||
+      (rc = alloc((void **)&d_ipiv, sym.work_elems * sizeof(int))) ||
+      (rc = alloc((void **)&d_perm, sym.work_elems * sizeof(int))) ||
+      (rc = alloc((void **)&d_pmap, sym.work_elems * sizeof(int))) ||
+      (rc = alloc((void **)&d_sched, sched.size() * sizeof(int))) ||
+      (rc = alloc((void **)&d_partial,
+                  (size_t)max_lvl_fronts * max_chunks * 64 * sizeof(double2))) ||
+      (rc = alloc((void **)&d_pert, sizeof(int))) ||
+      (rc = alloc(&vec_a, (size_t)ctx->nn * 5 * csize)))
+    return rc;
+  TLR_CUDA(ctx, cudaMemcpy(d_fronts, df.data(), nf * sizeof(DevFront), cudaMemcpyHostToDevice));
+  TLR_CUDA(ctx, cudaMemcpy(d_entries, sym.entries.data(), sym.entries.size() * sizeof(AsmEntry),
+                           cudaMemcpyHostToDevice));
+  TLR_CUDA(ctx, cudaMemcpy(d_cmap, sym.cmap.data(), sym.cmap.size() * sizeof(int),
+                           cudaMemcpyHostToDevice));
+  TLR_CUDA(ctx, cudaMemcpy(d_nodes, nodes.data(), nodes.size() * sizeof(int),
+                           cudaMemcpyHostToDevice));
+  TLR_CUDA(ctx, cudaMemcpy(d_sched, sched.data(), sched.size() * sizeof(int),
+                           cudaMemcpyHostToDevice));
+  return TLR_OK;
+}
+
+void Factor::release() {
+  cudaFree(pool); cudaFree(work); cudaFree(d_fronts); cudaFree(d_entries);
+  cudaFree(d_cmap); cudaFree(d_nodes); cudaFree(d_ipiv); cudaFree(d_perm);
+  cudaFree(d_pmap); cudaFree(d_sched); cudaFree(d_partial); cudaFree(d_pert);
+  cudaFree(vec_a);
+  pool = work = vec_a = nullptr;
+}
+
+template <class C>
+int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
+  cudaStream_t st = ctx->stream;
+  C *P = static_cast<C *>(pool);
+  TLR_CUDA(ctx, cudaMemsetAsync(d_pert, 0, sizeof(int), st));
+  const size_t tsm = sizeof(C) * (size_t)(w * w + w);
+  TLR_CUDA(ctx, cudaFuncSetAttribute(k_trsm_border<C>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+  TLR_CUDA(ctx, cudaFuncSetAttribute(k_trsm_urow<C>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+  for (size_t h = 0; h < levels.size(); ++h) {
+    const Level &L = levels[h];
+    TLR_CUDA(ctx, cudaMemsetAsync(P + L.pool_begin, 0,
+                                  (size_t)(L.pool_end - L.pool_begin) * sizeof(C), st));
+    const long long ne = L.entry_end - L.entry_begin;
+    if (ne > 0)
+      k_asm<C><<<blocks_for(ne * 25, 256), 256, 0, st>>>(d_entries + L.entry_begin, ne,
+                                                         ctx->A, ctx->B, sr, si, P, d_fronts);
+    for (int slot = 0; slot < 2; ++slot) {
+      if (!L.kids[slot]) continue;
+      const long long mb = L.kids_maxb[slot];
+      dim3 g((unsigned)std::min<long long>(std::max<long long>(blocks_for(mb * mb, 256), 1), 4096),
+             L.kids[slot]);
+      k_extend<C><<<g, 256, 0, st>>>(d_sched + L.kids_off[slot], d_fronts, d_cmap, P);
+    }
+    const int *fl = d_sched + L.fronts_off;
+    for (int s = 0; s < (int)L.steps.size(); ++s) {
+      const Step &S = L.steps[s];
+      k_panel<C><<<S.nf, 256, 0, st>>>(fl, s, w, P, d_fronts, d_ipiv, d_pert, tiny);
+      k_swap<C><<<dim3(blocks_for(S.max_m, 128), S.nf), 128, 0, st>>>(fl, s, w, P, d_fronts,
+                                                                       d_ipiv);
+      if (S.max_b > 0)
+        k_trsm_border<C><<<dim3(blocks_for(S.max_b, 128), S.nf), 128, tsm, st>>>(fl, s, w, P,
+                                                                                 d_fronts);
+      if (S.max_ext > 0) {
+        k_trsm_urow<C><<<dim3(blocks_for(S.max_ext, 128), S.nf), 128, tsm, st>>>(fl, s, w, P,
+                                                                                 d_fronts);
+        if (S.tiles > 0)
+          k_gemm<C><<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w, P,
+                                             d_fronts);
+      }
+    }
+  }
+  TLR_CUDA(ctx, cudaGetLastError());
+  return TLR_OK;
+}
+
+int Factor::factor(tlr_ctx *ctx, double sr, double si, double tiny) {
+  int rc = prec == 0 ? factor_impl<double2>(ctx, sr, si, tiny)
+                     : factor_impl<float2>(ctx, sr, si, tiny);
+  if (rc) return rc;
+  // row permutations of every front, and the children's maps through them
+  std::vector<int> ipiv(sym.work_elems), perm(sym.work_elems), pmap(sym.work_elems, 0);
+  TLR_CUDA(ctx, cudaMemcpyAsync(ipiv.data(), d_ipiv, ipiv.size() * sizeof(int),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+  TLR_CUDA(ctx, cudaMemcpyAsync(&perturbed, d_pert, sizeof(int), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const int nf = (int)sym.fronts.size();
+  std::vector<int> inv;
+  for (int t = 0; t < nf; ++t) {
+    const FrontInfo &f = sym.fronts[t];
+    int *pr = perm.data() + f.toff;
+    for (int i = 0; i < f.m; ++i) pr[i] = i;
+    for (int c = 0; c < f.p; ++c) std::swap(pr[c], pr[ipiv[f.toff + c]]);
+  }
+  for (int t = 0; t < nf; ++t) {
+    const FrontInfo &f = sym.fronts[t];
+    if (f.parent < 0) continue;
+    const FrontInfo &pf = sym.fronts[f.parent];
+    inv.assign(pf.m, 0);
+    for (int i = 0; i < pf.m; ++i) inv[perm[pf.toff + i]] = i;
+    const int bc = f.m - f.p;
+    for (int x = 0; x < bc; ++x) {
+      const int q = sym.cmap[sym.cmap_off[t] + x / 5] * 5 + x % 5;
+      pmap[f.toff + x] = inv[q];
+    }
+  }
+  TLR_CUDA(ctx, cudaMemcpyAsync(d_perm, perm.data(), perm.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  TLR_CUDA(ctx, cudaMemcpyAsync(d_pmap, pmap.data(), pmap.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  factored = true;
+  return TLR_OK;
+}
+
+template <class C>
+int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
+  cudaStream_t st = ctx->stream;
+  const C *P = static_cast<const C *>(pool);
+  C *W = static_cast<C *>(work);
+  C *x = static_cast<C *>(xv);
+  for (size_t h = 0; h < levels.size(); ++h) {
+    const Level &L = levels[h];
+    const int *fl = d_sched + L.fronts_off;
+    k_sgather<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(
+        fl, d_fronts, d_nodes, d_perm, x, W);
+    for (int slot = 0; slot < 2; ++slot)
+      if (L.kids[slot])
+        k_saddchild<C><<<dim3(blocks_for(std::max(L.kids_maxb[slot], 1), 128), L.kids[slot]),
+                         128, 0, st>>>(d_sched + L.kids_off[slot], d_fronts, d_pmap, W);
+    for (int s = 0; s < (int)L.steps.size(); ++s) {
+      const Step &S = L.steps[s];
+      k_fwd_diag<C><<<S.nf, 32, 0, st>>>(fl, s, w, P, d_fronts, W);
+      if (S.max_ext > 0)
+        k_fwd_gemv<C><<<dim3(blocks_for(S.max_ext, 128), S.nf), 128, 0, st>>>(fl, s, w, P,
+                                                                             d_fronts, W);
+    }
+  }
+  for (int h = (int)levels.size() - 1; h >= 0; --h) {
+    const Level &L = levels[h];
+    const int *fl = d_sched + L.fronts_off;
+    k_bgather<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(fl, d_fronts,
+                                                                             d_nodes, x, W);
+    for (int s = (int)L.steps.size() - 1; s >= 0; --s) {
+      const Step &S = L.steps[s];
+      const int nch = S.max_ext > 0 ? (S.max_ext + kChunk - 1) / kChunk : 0;
+      if (nch > 0)
+        k_bwd_gemv<C><<<dim3(nch, S.nf), 256, 0, st>>>(fl, s, w, kChunk, P, d_fronts, W,
+                                                       d_partial, max_chunks);
+      k_bwd_diag<C><<<S.nf, 32, 0, st>>>(fl, s, w, max_chunks, kChunk, P, d_fronts, W,
+                                         d_partial);
+    }
+    k_bscatter<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(fl, d_fronts,
+                                                                              d_nodes, W, x);
+  }
+  TLR_CUDA(ctx, cudaGetLastError());
+  return TLR_OK;
+}
+
+int Factor::solve(tlr_ctx *ctx, void *x) {
+  return prec == 0 ? solve_impl<double2>(ctx, x) : solve_impl<float2>(ctx, x);
+}
+
+}  // namespace tlr

@@ -1,0 +1,55 @@
+// tlr_lu.h -- device multifrontal factorisation of K = A_bc - sigma B_bc.
+#pragma once
+
+#include <vector>
+
+#include "tlr_internal.h"
+#include "tlr_symbolic.h"
+
+namespace tlr {
+
+struct DevFront {
+  long long off, toff, cmap_off;
+  int p, m, parent, node_off;
+};
+
+constexpr int kChunk = 1024;  // columns per CTA in the backward GEMV
+
+struct Step {  // one panel step of one level
+  int nf, max_m, max_b, max_ext, prefix_off, tiles;
+};
+
+struct Level {
+  int nfronts = 0, fronts_off = 0, max_m = 0;
+  int kids[2] = {0, 0}, kids_off[2] = {0, 0}, kids_maxb[2] = {0, 0};
+  long long entry_begin = 0, entry_end = 0, pool_begin = 0, pool_end = 0;
+  std::vector<Step> steps;
+};
+
+struct Factor {
+  Symbolic sym;
+  int prec = 0;  // 0: complex128 fronts, 1: complex64 fronts
+  int w = 32;    // panel width
+  std::vector<Level> levels;
+  int max_chunks = 1;
+  void *pool = nullptr, *work = nullptr, *vec_a = nullptr;
+  DevFront *d_fronts = nullptr;
+  AsmEntry *d_entries = nullptr;
+  int *d_cmap = nullptr, *d_nodes = nullptr, *d_ipiv = nullptr, *d_perm = nullptr;
+  int *d_pmap = nullptr, *d_sched = nullptr, *d_pert = nullptr;
+  double2 *d_partial = nullptr;
+  int perturbed = 0;
+  bool factored = false;
+  double sigma_re = 0.0, sigma_im = 0.0;
+
+  int setup(tlr_ctx *ctx, int precision, int leaf);
+  void release();
+  int factor(tlr_ctx *ctx, double sr, double si, double tiny);
+  // In-place x <- K^-1 x on a device vector in the factor's precision.
+  int solve(tlr_ctx *ctx, void *x);
+
+  template <class C> int factor_impl(tlr_ctx *ctx, double sr, double si, double tiny);
+  template <class C> int solve_impl(tlr_ctx *ctx, void *x);
+};
+
+}  // namespace tlr

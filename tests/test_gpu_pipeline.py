@@ -106,7 +106,8 @@ def test_boundary_rows_parity(run):
         if node in far:
             Xg = np.concatenate([A[ks].transpose(1, 0, 2).reshape(5, -1), B[node]], 1)
             Xr = np.concatenate([A_ref[ks].transpose(1, 0, 2).reshape(5, -1), B_ref[node]], 1)
-            assert _rowspace_ok(Xg, Xr), node
+            assert _rowspace_ok(Xg, Xr), (node, np.round(B[node].real, 4).tolist(),
+                                          np.round(B_ref[node].real, 4).tolist())
             # incoming rows: zero B row and only the node's own columns
             nzero_b = np.where(np.abs(B[node]).sum(1) == 0)[0]
             assert len(nzero_b) == info["per_node"][node // ny]
