@@ -201,6 +201,10 @@ typedef struct {
 int tlr_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
               double *residual, double *modes, tlr_eig_diag *diag);
 
+/* The context's CUDA stream (cudaStream_t) -- all device work of the
+ * context is ordered on it; callers time or synchronise against it. */
+void *tlr_stream(tlr_ctx *ctx);
+
 const char *tlr_status_string(int status);
 const char *tlr_last_error(const tlr_ctx *ctx);
 

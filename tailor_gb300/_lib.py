@@ -107,6 +107,7 @@ SIGNATURES = {
     "tlr_lns_points": ([_P, _I, _P, _P, _P], _I),
     "tlr_transform_points": ([_I, _P, _P, _P, _P, _P, _P], _I),
     "tlr_solve": ([_P, _P, _P, _P, _P, _P], _I),
+    "tlr_stream": ([_P], ctypes.c_void_p),
     "tlr_status_string": ([_I], ctypes.c_char_p),
     "tlr_last_error": ([_P], ctypes.c_char_p),
 }

@@ -133,20 +133,42 @@ __device__ void characteristics(const double *state, const double *m10,
                              {1.0, 0.0, c * ny / rho, c * nz / rho, th}};
   for (int r = 0; r < 5; ++r)
     for (int mm = 0; mm < 5; ++mm) R[r * 5 + mm] = cols[mm][r];
-  double G[25] = {0};
-  G[0] = 1.0; G[6] = rho; G[12] = rho; G[18] = rho;
-  G[20] = -Pe * T; G[24] = rho * g2 - Pe * rho;
-  double Ginv[25];
-  if (!invert5(R, ch.Rinv) || !invert5(G, Ginv)) {
+  if (!invert5(R, ch.Rinv)) {
     ch.ok = 6;  // SingularEigenvectors
     return;
   }
+  // Gamma (LNSCoefficients.cpp:326-331) is diag(1, rho, rho, rho, g44)
+  // plus Gamma[4][0] = -Pe T; its inverse in closed form.
+  const double g44 = rho * g2 - Pe * rho;
+  if (!isfinite(g44) || fabs(g44) <= 100.0 * kEps) {
+    ch.ok = 6;
+    return;
+  }
+  double Ginv[25] = {0};
+  Ginv[0] = 1.0;
+  Ginv[6] = 1.0 / rho;
+  Ginv[12] = 1.0 / rho;
+  Ginv[18] = 1.0 / rho;
+  Ginv[24] = 1.0 / g44;
+  Ginv[20] = Pe * T / g44;
   for (int r = 0; r < 5; ++r)
     for (int q = 0; q < 5; ++q) {
       double s = 0.0;
       for (int k = 0; k < 5; ++k) s += ch.Rinv[r * 5 + k] * Ginv[k * 5 + q];
       ch.P[r * 5 + q] = s;
     }
+  // self-check: R R^-1 = I to rounding
+  double worst = 0.0;
+  for (int r = 0; r < 5; ++r)
+    for (int q = 0; q < 5; ++q) {
+      double s = 0.0;
+      for (int k = 0; k < 5; ++k) s += R[r * 5 + k] * ch.Rinv[k * 5 + q];
+      worst = fmax(worst, fabs(s - (r == q ? 1.0 : 0.0)));
+    }
+  if (!(worst <= 1e-10)) {
+    ch.ok = 6;
+    return;
+  }
   ch.cond = inf_norm5(R) * inf_norm5(ch.Rinv);
   if (!isfinite(ch.cond) || ch.cond > 1.0e12) {
     ch.ok = 7;  // IllConditionedEigenvectors

@@ -151,6 +151,8 @@ const char *tlr_status_string(int status) {
   return "unknown status";
 }
 
+void *tlr_stream(tlr_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
 const char *tlr_last_error(const tlr_ctx *ctx) {
   return ctx ? ctx->last_error.c_str() : g_error.c_str();
 }

@@ -245,10 +245,55 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     const double inv = 1.0 / nv;
     cublasZdscal(S.h, (int)n, &inv, reinterpret_cast<cuDoubleComplex *>(S.V), 1);
   }
+  double maxerr = 0.0;
+  const int nout = nev;
+  // Ritz vectors x_i = V Q y_i, lambda_i = sigma + 1/theta_i and explicit
+  // relative residuals ||A x - lambda B x|| / (|lambda| ||x||).
+  auto finalize = [&](const dense::Mat &Tq, const dense::Mat &Qq) -> int {
+    std::vector<double2> yh((size_t)ncv * nout);
+    for (int i = 0; i < nout; ++i) {
+      const auto yv = dense::tri_eigvec(Tq, i);
+      for (int q = 0; q < ncv; ++q) {
+        cd sacc = 0.0;
+        for (int t = 0; t <= i; ++t) sacc += Qq(q, t) * yv[t];
+        yh[(size_t)i * ncv + q] = make_double2(sacc.real(), sacc.imag());
+      }
+    }
+    double2 *yd = nullptr;
+    TLR_CUDA(ctx, cudaMallocAsync(&yd, yh.size() * sizeof(double2), ctx->stream));
+    TLR_CUDA(ctx, cudaMemcpyAsync(yd, yh.data(), yh.size() * sizeof(double2),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    const cuDoubleComplex one1 = {1.0, 0.0}, zero1 = {0.0, 0.0};
+    cublasZgemm(S.h, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, nout, ncv, &one1,
+                reinterpret_cast<cuDoubleComplex *>(S.V), (int)n,
+                reinterpret_cast<cuDoubleComplex *>(yd), ncv, &zero1,
+                reinterpret_cast<cuDoubleComplex *>(S.tmp), (int)n);
+    cudaFreeAsync(yd, ctx->stream);
+    maxerr = 0.0;
+    for (int i = 0; i < nout; ++i) {
+      double2 *x = S.tmp + (size_t)i * n;
+      const double nx = S.nrm(x);
+      const double inv = 1.0 / nx;
+      cublasZdscal(S.h, (int)n, &inv, reinterpret_cast<cuDoubleComplex *>(x), 1);
+      const cd lam = sigma + 1.0 / Tq(i, i);
+      int rc = run_spmv(ctx, TLR_MAT_A, x, S.aw);
+      if (rc) return rc;
+      if ((rc = run_spmv(ctx, TLR_MAT_B, x, S.bw))) return rc;
+      k_axmy<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, S.aw, S.bw, lam.real(),
+                                                          lam.imag(), S.r);
+      const double res = S.nrm(S.r) / std::abs(lam);
+      lambda[2 * i] = lam.real();
+      lambda[2 * i + 1] = lam.imag();
+      residual[i] = res;
+      maxerr = std::max(maxerr, res);
+    }
+    return TLR_OK;
+  };
+  double tol_int = tol;
+  int tighten = 0;
   dense::Mat H(ncv + 1, ncv);
   int k = 0, nconv = 0, it = 0, reason = 0;
   std::vector<cd> theta(ncv);
-  dense::Mat Tq, Qq;
   std::vector<cd> hcol(ncv + 1), hcol2(ncv + 1);
   const cuDoubleComplex one = {1.0, 0.0}, zero = {0.0, 0.0}, mone = {-1.0, 0.0};
   auto Vc = [&](int j) { return reinterpret_cast<cuDoubleComplex *>(S.V + (size_t)j * n); };
@@ -297,29 +342,48 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     const double beta = std::abs(H(ncv, ncv - 1));
     std::vector<cd> b(ncv);
     for (int i = 0; i < ncv; ++i) b[i] = beta * Q(ncv - 1, i);
-    nconv = 0;
-    for (int i = 0; i < ncv && nconv < ncv; ++i) {
-      const auto yv = dense::tri_eigvec(T, i);
-      cd dot = 0.0;
-      double ny = 0.0;
-      for (int q = 0; q <= i; ++q) {
-        dot += b[q] * yv[q];
-        ny += std::norm(yv[q]);
+    auto count_conv = [&](double tl) {
+      int c = 0;
+      for (int i = 0; i < ncv; ++i) {
+        const auto yv = dense::tri_eigvec(T, i);
+        cd dot = 0.0;
+        double ny = 0.0;
+        for (int q = 0; q <= i; ++q) {
+          dot += b[q] * yv[q];
+          ny += std::norm(yv[q]);
+        }
+        if (std::abs(dot) / std::sqrt(ny) <= tl * std::abs(T(i, i))) ++c;
+        else break;
       }
-      const double res = std::abs(dot) / std::sqrt(ny);
-      if (res <= tol * std::abs(T(i, i)) && nconv == i) ++nconv;
-      else break;
-    }
+      return c;
+    };
+    nconv = count_conv(tol_int);
     for (int i = 0; i < ncv; ++i) theta[i] = T(i, i);
-    if (nconv >= nev || it >= max_it) {
-      reason = nconv >= nev ? 1 : -1;
-      Tq = T;
-      Qq = Q;
-      break;
+    bool done = false;
+    if (nconv >= nev) {
+      int rc = finalize(T, Q);
+      if (rc) return rc;
+      if (maxerr <= tol || tighten >= 6) {
+        done = true;
+        reason = maxerr <= tol ? 1 : 2;
+      } else {
+        // Ritz estimates converged but the explicit residuals are above the
+        // tolerance: tighten the internal criterion and keep iterating.
+        tol_int *= 0.05;
+        ++tighten;
+        nconv = count_conv(tol_int);
+      }
     }
+    if (!done && it >= max_it) {
+      int rc = finalize(T, Q);
+      if (rc) return rc;
+      reason = -1;
+      done = true;
+    }
+    if (done) break;
     // thick restart
     int l = nconv + (ncv - nconv) / 2;
-    l = std::max(l, 1);
+    l = std::max(1, std::min(l, ncv - 2));
     std::vector<double2> qh((size_t)ncv * l);
     for (int j = 0; j < l; ++j)
       for (int i = 0; i < ncv; ++i) qh[(size_t)j * ncv + i] = make_double2(Q(i, j).real(), Q(i, j).imag());
@@ -343,53 +407,16 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     k = l;
   }
   const auto t2 = clock::now();
-  // Ritz vectors x_i = V Q y_i, eigenvalues, explicit residuals
-  const int nout = std::min(nev, nconv > 0 ? std::max(nconv, nev) : nev);
-  std::vector<double2> yh((size_t)ncv * nout);
-  for (int i = 0; i < nout; ++i) {
-    const auto yv = dense::tri_eigvec(Tq, i);
-    for (int q = 0; q < ncv; ++q) {
-      cd s = 0.0;
-      for (int t = 0; t <= i; ++t) s += Qq(q, t) * yv[t];
-      yh[(size_t)i * ncv + q] = make_double2(s.real(), s.imag());
-    }
-  }
-  double2 *yd = nullptr;
-  TLR_CUDA(ctx, cudaMalloc(&yd, yh.size() * sizeof(double2)));
-  TLR_CUDA(ctx, cudaMemcpyAsync(yd, yh.data(), yh.size() * sizeof(double2),
-                                cudaMemcpyHostToDevice, ctx->stream));
-  cublasZgemm(S.h, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, nout, ncv, &one, Vc(0), (int)n,
-              reinterpret_cast<cuDoubleComplex *>(yd), ncv, &zero,
-              reinterpret_cast<cuDoubleComplex *>(S.tmp), (int)n);
-  cudaFree(yd);
-  double maxerr = 0.0;
-  std::vector<double2> hostv;
-  for (int i = 0; i < nout; ++i) {
-    double2 *x = S.tmp + (size_t)i * n;
-    const double nx = S.nrm(x);
-    const double inv = 1.0 / nx;
-    cublasZdscal(S.h, (int)n, &inv, reinterpret_cast<cuDoubleComplex *>(x), 1);
-    const cd lam = sigma + 1.0 / theta[i];
-    int rc = run_spmv(ctx, TLR_MAT_A, x, S.aw);
-    if (rc) return rc;
-    if ((rc = run_spmv(ctx, TLR_MAT_B, x, S.bw))) return rc;
-    k_axmy<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, S.aw, S.bw, lam.real(), lam.imag(),
-                                                        S.r);
-    const double res = S.nrm(S.r) / std::abs(lam);
-    lambda[2 * i] = lam.real();
-    lambda[2 * i + 1] = lam.imag();
-    residual[i] = res;
-    maxerr = std::max(maxerr, res);
-    if (modes)
-      TLR_CUDA(ctx, cudaMemcpyAsync(modes + (size_t)2 * n * i, x, vb, cudaMemcpyDeviceToHost,
-                                    ctx->stream));
-  }
+  if (modes)
+    for (int i = 0; i < nout; ++i)
+      TLR_CUDA(ctx, cudaMemcpyAsync(modes + (size_t)2 * n * i, S.tmp + (size_t)i * n, vb,
+                                    cudaMemcpyDeviceToHost, ctx->stream));
   TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   const auto t3 = clock::now();
   if (diag) {
     tlr_eig_diag d{};
     d.requested = nev;
-    d.converged = std::min(nconv, nev) == nev ? nout : std::min(nconv, nout);
+    d.converged = reason >= 1 ? nout : std::min(nconv, nout);
     d.iterations = it;
     d.reason = reason;
     d.target_re = target.real();
@@ -404,10 +431,11 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     d.factor_flops = F->sym.flops;
     *diag = d;
   }
-  if (reason <= 0) {
+  if (reason != 1) {
     char buf[160];
     snprintf(buf, sizeof(buf),
-             "Krylov-Schur failed to converge (%d eigenpairs after %d iterations)", nconv, it);
+             "Krylov-Schur failed to converge (%d eigenpairs after %d iterations, max "
+             "relative residual %.3g)", nconv, it, maxerr);
     return fail(ctx, TLR_ERR_NOT_CONVERGED, buf);
   }
   return TLR_OK;

@@ -28,6 +28,10 @@ namespace {
 
 constexpr int kTile = 64;
 
+// widest panel per precision (FP64 fronts use w = 32, FP32 fronts w = 64)
+template <class C> struct MaxW { static constexpr int v = 64; };
+template <> struct MaxW<double2> { static constexpr int v = 32; };
+
 // ------------------------------------------------------------ factorization
 
 template <class C>
@@ -316,52 +320,125 @@ __global__ void k_saddchild(const int *__restrict__ kids, const DevFront *__rest
   d = cadd(d, work[fc.toff + fc.p + x]);
 }
 
-// forward: unit-lower diagonal block of step s (one warp per front)
+// forward step s, fused: every CTA loads the ww x ww diagonal block of L
+// and t[k0:k0+ww] into shared memory, solves the unit-lower system there,
+// and updates its chunk of rows k0+ww..m-1; CTA 0 writes the solved part.
 template <class C>
-__global__ void k_fwd_diag(const int *__restrict__ fl, int s, int w, const C *__restrict__ pool,
-                           const DevFront *__restrict__ fr, C *__restrict__ work) {
-  const DevFront f = fr[fl[blockIdx.x]];
-  const int k0 = s * w, ww = min(w, f.p - k0);
-  const int lane = threadIdx.x;
-  const C *F = pool + f.off;
-  C *t = work + f.toff + k0;
-  const int m = f.m;
-  C mine[2];
-  mine[0] = lane < ww ? t[lane] : czero<C>();
-  mine[1] = lane + 32 < ww ? t[lane + 32] : czero<C>();
-  for (int r = 0; r < ww; ++r) {
-    const C xr = r < 32 ? mine[0] : mine[1];
-    const C xb = cmake<C>(__shfl_sync(0xffffffffu, xr.x, r & 31),
-                          __shfl_sync(0xffffffffu, xr.y, r & 31));
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int rr = lane + 32 * h;
-      if (rr > r && rr < ww) mine[h] = cfms(mine[h], F[(long long)(k0 + r) * m + k0 + rr], xb);
-    }
-  }
-  if (lane < ww) t[lane] = mine[0];
-  if (lane + 32 < ww) t[lane + 32] = mine[1];
-}
-
-// forward: rows k0+ww..m-1 -= L[:, k0:k0+ww] t[k0:k0+ww]
-template <class C>
-__global__ void k_fwd_gemv(const int *__restrict__ fl, int s, int w, const C *__restrict__ pool,
-                           const DevFront *__restrict__ fr, C *__restrict__ work) {
-  __shared__ C xs[64];
+__global__ void __launch_bounds__(256)
+    k_fwd_step(const int *__restrict__ fl, int s, int w, const C *__restrict__ pool,
+               const DevFront *__restrict__ fr, C *__restrict__ work) {
+  constexpr int WM = MaxW<C>::v;
+  __shared__ C Ld[WM][WM + 1];
+  __shared__ C xs[WM];
   const DevFront f = fr[fl[blockIdx.y]];
   const int k0 = s * w, ww = min(w, f.p - k0);
+  const int r = k0 + ww + blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.x > 0 && k0 + ww + (int)(blockIdx.x * blockDim.x) >= f.m) return;
+  const C *F = pool + f.off;
+  const int m = f.m;
   C *t = work + f.toff;
+  for (int x = threadIdx.x; x < ww * ww; x += blockDim.x) {
+    const int rr = x % ww, cc = x / ww;
+    if (rr > cc) Ld[cc][rr] = F[(long long)(k0 + cc) * m + k0 + rr];
+  }
   for (int c = threadIdx.x; c < ww; c += blockDim.x) xs[c] = t[k0 + c];
   __syncthreads();
-  const int r = k0 + ww + blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= f.m) return;
-  const C *F = pool + f.off;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    for (int q = 0; q < ww; ++q) {
+      const C xq = xs[q];
+      __syncwarp();
+      for (int rr = q + 1 + lane; rr < ww; rr += 32) xs[rr] = cfms(xs[rr], Ld[q][rr], xq);
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int c = threadIdx.x; c < ww; c += blockDim.x) t[k0 + c] = xs[c];
+  if (r >= m) return;
   C v = t[r];
-  for (int c = 0; c < ww; ++c) v = cfms(v, F[(long long)(k0 + c) * f.m + r], xs[c]);
+  for (int c = 0; c < ww; ++c) v = cfms(v, F[(long long)(k0 + c) * m + r], xs[c]);
   t[r] = v;
 }
 
-// backward: t[p:m] = x at the border unknowns
+// backward step s, fused: CTAs reduce U[k0:k0+ww, chunk] t[chunk] into
+// per-chunk partials; the last CTA of the front (atomic ticket) sums them in
+// chunk order, solves the upper diagonal block and resets the ticket.
+template <class C>
+__global__ void __launch_bounds__(256)
+    k_bwd_step(const int *__restrict__ fl, int s, int w, int chunk,
+               const C *__restrict__ pool, const DevFront *__restrict__ fr,
+               C *__restrict__ work, double2 *__restrict__ partial, int max_chunks,
+               int *__restrict__ ticket) {
+  constexpr int WM = MaxW<C>::v;
+  __shared__ C red[8][64];
+  __shared__ C Ud[WM][WM + 1];
+  __shared__ C xs[WM];
+  __shared__ int last;
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int k0 = s * w, ww = min(w, f.p - k0);
+  const int ext = f.m - k0 - ww;
+  const int nch = ext > 0 ? (ext + chunk - 1) / chunk : 1;
+  if ((int)blockIdx.x >= nch) return;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const C *F = pool + f.off;
+  const int m = f.m;
+  C *t = work + f.toff;
+  if (ext > 0) {
+    const int cbeg = k0 + ww + blockIdx.x * chunk;
+    const int cend = min(m, cbeg + chunk);
+    C a0 = czero<C>(), a1 = czero<C>();
+    for (int c = cbeg + wp; c < cend; c += 8) {
+      const C tc = t[c];
+      const C *colp = F + (long long)c * m + k0;
+      if (lane < ww) a0 = cfma(a0, colp[lane], tc);
+      if (lane + 32 < ww) a1 = cfma(a1, colp[lane + 32], tc);
+    }
+    red[wp][lane] = a0;
+    red[wp][lane + 32] = a1;
+    __syncthreads();
+    if (threadIdx.x < ww) {
+      C v = czero<C>();
+      for (int q = 0; q < 8; ++q) v = cadd(v, red[q][threadIdx.x]);
+      partial[((long long)blockIdx.y * max_chunks + blockIdx.x) * 64 + threadIdx.x] = to64(v);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket + blockIdx.y, 1) == nch - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+  }
+  for (int x = threadIdx.x; x < ww * ww; x += blockDim.x) {
+    const int rr = x % ww, cc = x / ww;
+    if (rr <= cc) Ud[cc][rr] = F[(long long)(k0 + cc) * m + k0 + rr];
+  }
+  if (threadIdx.x < ww) {
+    double2 acc = make_double2(0, 0);
+    if (ext > 0)
+      for (int q = 0; q < nch; ++q) {
+        const double2 pv = partial[((long long)blockIdx.y * max_chunks + q) * 64 + threadIdx.x];
+        acc.x += pv.x;
+        acc.y += pv.y;
+      }
+    xs[threadIdx.x] = csub(t[k0 + threadIdx.x], from64<C>(acc));
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    for (int q = ww - 1; q >= 0; --q) {
+      if (lane == 0) xs[q] = cmul(xs[q], cinv(Ud[q][q]));
+      __syncwarp();
+      const C xq = xs[q];
+      for (int rr = lane; rr < q; rr += 32) xs[rr] = cfms(xs[rr], Ud[q][rr], xq);
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < ww) t[k0 + threadIdx.x] = xs[threadIdx.x];
+  if (threadIdx.x == 0 && ext > 0) ticket[blockIdx.y] = 0;
+}
+
+// backward: t[p:m] = x at the border unknowns (already solved ancestors)
 template <class C>
 __global__ void k_bgather(const int *__restrict__ fl, const DevFront *__restrict__ fr,
                           const int *__restrict__ nodes, const C *__restrict__ x,
@@ -370,86 +447,6 @@ __global__ void k_bgather(const int *__restrict__ fl, const DevFront *__restrict
   const int i = f.p + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= f.m) return;
   work[f.toff + i] = x[(long long)nodes[f.node_off + i / 5] * 5 + i % 5];
-}
-
-// backward: partial[front][chunk][r] = sum over a column chunk of U[k0+r, c] t[c]
-template <class C>
-__global__ void k_bwd_gemv(const int *__restrict__ fl, int s, int w, int chunk,
-                           const C *__restrict__ pool, const DevFront *__restrict__ fr,
-                           const C *__restrict__ work, double2 *__restrict__ partial,
-                           int max_chunks) {
-  __shared__ C red[8][64];
-  const DevFront f = fr[fl[blockIdx.y]];
-  const int k0 = s * w, ww = min(w, f.p - k0);
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  const int cbeg = k0 + ww + blockIdx.x * chunk;
-  const int cend = min(f.m, cbeg + chunk);
-  const C *F = pool + f.off;
-  const C *t = work + f.toff;
-  C a0 = czero<C>(), a1 = czero<C>();
-  for (int c = cbeg + wp; c < cend; c += 8) {
-    const C tc = t[c];
-    const C *colp = F + (long long)c * f.m + k0;
-    if (lane < ww) a0 = cfma(a0, colp[lane], tc);
-    if (lane + 32 < ww) a1 = cfma(a1, colp[lane + 32], tc);
-  }
-  red[wp][lane] = a0;
-  red[wp][lane + 32] = a1;
-  __syncthreads();
-  if (threadIdx.x < ww) {
-    C v = czero<C>();
-    for (int q = 0; q < 8; ++q) v = cadd(v, red[q][threadIdx.x]);
-    partial[((long long)blockIdx.y * max_chunks + blockIdx.x) * 64 + threadIdx.x] = to64(v);
-  }
-}
-
-// backward: t[k0:k0+ww] = U_kk^-1 (t - sum of partials); one warp per front
-template <class C>
-__global__ void k_bwd_diag(const int *__restrict__ fl, int s, int w, int nchunks_max,
-                           int chunk, const C *__restrict__ pool,
-                           const DevFront *__restrict__ fr, C *__restrict__ work,
-                           const double2 *__restrict__ partial) {
-  const DevFront f = fr[fl[blockIdx.x]];
-  const int k0 = s * w, ww = min(w, f.p - k0);
-  const int lane = threadIdx.x;
-  const int ext = f.m - k0 - ww;
-  const int nch = ext > 0 ? (ext + chunk - 1) / chunk : 0;
-  C *t = work + f.toff + k0;
-  const C *F = pool + f.off;
-  const int m = f.m;
-  C mine[2];
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int r = lane + 32 * h;
-    if (r < ww) {
-      double2 acc = make_double2(0, 0);
-      for (int q = 0; q < nch; ++q) {
-        const double2 pv = partial[((long long)blockIdx.x * nchunks_max + q) * 64 + r];
-        acc.x += pv.x;
-        acc.y += pv.y;
-      }
-      mine[h] = csub(t[r], from64<C>(acc));
-    } else {
-      mine[h] = czero<C>();
-    }
-  }
-  for (int r = ww - 1; r >= 0; --r) {
-    const int hr = r >> 5;
-    C xr = hr ? mine[1] : mine[0];
-    if (lane == (r & 31)) xr = cmul(xr, cinv(F[(long long)(k0 + r) * m + k0 + r]));
-    const C xb = cmake<C>(__shfl_sync(0xffffffffu, xr.x, r & 31),
-                          __shfl_sync(0xffffffffu, xr.y, r & 31));
-    if (lane == (r & 31)) {
-      if (hr) mine[1] = xb; else mine[0] = xb;
-    }
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int rr = lane + 32 * h;
-      if (rr < r) mine[h] = cfms(mine[h], F[(long long)(k0 + r) * m + k0 + rr], xb);
-    }
-  }
-  if (lane < ww) t[lane] = mine[0];
-  if (lane + 32 < ww) t[lane + 32] = mine[1];
 }
 
 template <class C>
@@ -592,8 +589,10 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
       (rc = alloc((void **)&d_partial,
                   (size_t)max_lvl_fronts * max_chunks * 64 * sizeof(double2))) ||
       (rc = alloc((void **)&d_pert, sizeof(int))) ||
+      (rc = alloc((void **)&d_ticket, max_lvl_fronts * sizeof(int))) ||
       (rc = alloc(&vec_a, (size_t)ctx->nn * 5 * csize)))
     return rc;
+  TLR_CUDA(ctx, cudaMemset(d_ticket, 0, max_lvl_fronts * sizeof(int)));
   TLR_CUDA(ctx, cudaMemcpy(d_fronts, df.data(), nf * sizeof(DevFront), cudaMemcpyHostToDevice));
   TLR_CUDA(ctx, cudaMemcpy(d_entries, sym.entries.data(), sym.entries.size() * sizeof(AsmEntry),
                            cudaMemcpyHostToDevice));
@@ -610,7 +609,9 @@ void Factor::release() {
   cudaFree(pool); cudaFree(work); cudaFree(d_fronts); cudaFree(d_entries);
   cudaFree(d_cmap); cudaFree(d_nodes); cudaFree(d_ipiv); cudaFree(d_perm);
   cudaFree(d_pmap); cudaFree(d_sched); cudaFree(d_partial); cudaFree(d_pert);
-  cudaFree(vec_a);
+  cudaFree(vec_a); cudaFree(d_ticket);
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  graph_exec = nullptr;
   pool = work = vec_a = nullptr;
 }
 
@@ -718,10 +719,8 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
                          128, 0, st>>>(d_sched + L.kids_off[slot], d_fronts, d_pmap, W);
     for (int s = 0; s < (int)L.steps.size(); ++s) {
       const Step &S = L.steps[s];
-      k_fwd_diag<C><<<S.nf, 32, 0, st>>>(fl, s, w, P, d_fronts, W);
-      if (S.max_ext > 0)
-        k_fwd_gemv<C><<<dim3(blocks_for(S.max_ext, 128), S.nf), 128, 0, st>>>(fl, s, w, P,
-                                                                             d_fronts, W);
+      k_fwd_step<C><<<dim3(std::max(blocks_for(S.max_ext, 256), 1), S.nf), 256, 0, st>>>(
+          fl, s, w, P, d_fronts, W);
     }
   }
   for (int h = (int)levels.size() - 1; h >= 0; --h) {
@@ -731,12 +730,9 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
                                                                              d_nodes, x, W);
     for (int s = (int)L.steps.size() - 1; s >= 0; --s) {
       const Step &S = L.steps[s];
-      const int nch = S.max_ext > 0 ? (S.max_ext + kChunk - 1) / kChunk : 0;
-      if (nch > 0)
-        k_bwd_gemv<C><<<dim3(nch, S.nf), 256, 0, st>>>(fl, s, w, kChunk, P, d_fronts, W,
-                                                       d_partial, max_chunks);
-      k_bwd_diag<C><<<S.nf, 32, 0, st>>>(fl, s, w, max_chunks, kChunk, P, d_fronts, W,
-                                         d_partial);
+      const int nch = S.max_ext > 0 ? (S.max_ext + kChunk - 1) / kChunk : 1;
+      k_bwd_step<C><<<dim3(nch, S.nf), 256, 0, st>>>(fl, s, w, kChunk, P, d_fronts, W,
+                                                     d_partial, max_chunks, d_ticket);
     }
     k_bscatter<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(fl, d_fronts,
                                                                               d_nodes, W, x);
@@ -746,7 +742,23 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
 }
 
 int Factor::solve(tlr_ctx *ctx, void *x) {
-  return prec == 0 ? solve_impl<double2>(ctx, x) : solve_impl<float2>(ctx, x);
+  const size_t bytes = (size_t)sym.nn * 5 * (prec == 0 ? sizeof(double2) : sizeof(float2));
+  cudaStream_t st = ctx->stream;
+  TLR_CUDA(ctx, cudaMemcpyAsync(vec_a, x, bytes, cudaMemcpyDeviceToDevice, st));
+  if (!graph_exec) {
+    TLR_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int rc = prec == 0 ? solve_impl<double2>(ctx, vec_a) : solve_impl<float2>(ctx, vec_a);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
+    const cudaError_t e2 = cudaGraphInstantiate(&graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaGraphInstantiate");
+  }
+  TLR_CUDA(ctx, cudaGraphLaunch(graph_exec, st));
+  TLR_CUDA(ctx, cudaMemcpyAsync(x, vec_a, bytes, cudaMemcpyDeviceToDevice, st));
+  return TLR_OK;
 }
 
 }  // namespace tlr

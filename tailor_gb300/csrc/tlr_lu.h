@@ -36,7 +36,8 @@ struct Factor {
   DevFront *d_fronts = nullptr;
   AsmEntry *d_entries = nullptr;
   int *d_cmap = nullptr, *d_nodes = nullptr, *d_ipiv = nullptr, *d_perm = nullptr;
-  int *d_pmap = nullptr, *d_sched = nullptr, *d_pert = nullptr;
+  int *d_pmap = nullptr, *d_sched = nullptr, *d_pert = nullptr, *d_ticket = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;  // captured solve, replayed per call
   double2 *d_partial = nullptr;
   int perturbed = 0;
   bool factored = false;
