@@ -363,13 +363,13 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     if (nconv >= nev) {
       int rc = finalize(T, Q);
       if (rc) return rc;
-      if (maxerr <= tol || tighten >= 6) {
+      if (maxerr <= tol || tighten >= 4 || tol_int <= 1e-14) {
         done = true;
         reason = maxerr <= tol ? 1 : 2;
       } else {
         // Ritz estimates converged but the explicit residuals are above the
         // tolerance: tighten the internal criterion and keep iterating.
-        tol_int *= 0.05;
+        tol_int = std::max(tol_int * 0.05, 1e-14);
         ++tighten;
         nconv = count_conv(tol_int);
       }
