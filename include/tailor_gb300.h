@@ -201,6 +201,20 @@ typedef struct {
 int tlr_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
               double *residual, double *modes, tlr_eig_diag *diag);
 
+/* Frobenius norm sqrt(sum |v|^2) of `count` complex values at the device
+ * address `values`, written to the host double `result`, computed on
+ * `stream` (NULL: the default stream) -- the norm tlr_assemble and
+ * tlr_apply_bc report for the operators.  No counterpart in the reference:
+ * it serves callers that cannot allocate device memory (code running while
+ * a CUDA graph is captured in global mode, or hosts whose allocator forbids
+ * raw cudaMalloc).  It allocates nothing: its scratch is a fixed 32 KB
+ * device array inside the library, so count is limited to 2^28 values
+ * (TLR_ERR_SIZE beyond that).  The first call on a device looks up that
+ * array and should come before any stream capture; calls that overlap on
+ * the GPU share the array and race. */
+int tlr_frobenius_noalloc(const double *values, size_t count, double *result,
+                          void *stream);
+
 /* The context's CUDA stream (cudaStream_t) -- all device work of the
  * context is ordered on it; callers time or synchronise against it. */
 void *tlr_stream(tlr_ctx *ctx);

@@ -108,6 +108,7 @@ SIGNATURES = {
     "tlr_transform_points": ([_I, _P, _P, _P, _P, _P, _P], _I),
     "tlr_solve": ([_P, _P, _P, _P, _P, _P], _I),
     "tlr_stream": ([_P], ctypes.c_void_p),
+    "tlr_frobenius_noalloc": ([_P, ctypes.c_size_t, _P, _P], _I),
     "tlr_status_string": ([_I], ctypes.c_char_p),
     "tlr_last_error": ([_P], ctypes.c_char_p),
 }

@@ -123,6 +123,9 @@ int copy_soa(tlr_ctx *ctx, const double *src, int comp, double *dst) {
 }
 
 }  // namespace
+
+void set_global_error(const std::string &msg) { g_error = msg; }
+
 }  // namespace tlr
 
 using namespace tlr;
