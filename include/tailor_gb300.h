@@ -195,6 +195,8 @@ typedef struct {
   int factorizations, solves, refinement_steps;
   double factor_ms, krylov_ms, total_ms;
   double factor_flops;    /* algorithmic complex-counted flops of the LU    */
+  double solve_ms;        /* time inside K^-1 applications (incl. refinement) */
+  double factor_bytes;    /* bytes of the stored L and U factors            */
 } tlr_eig_diag;
 
 /* lambda [nev] complex, residual [nev]; modes [nev][5N] complex or NULL. */

@@ -85,7 +85,8 @@ class EigDiag(ctypes.Structure):
                 ("factorizations", ctypes.c_int), ("solves", ctypes.c_int),
                 ("refinement_steps", ctypes.c_int),
                 ("factor_ms", ctypes.c_double), ("krylov_ms", ctypes.c_double),
-                ("total_ms", ctypes.c_double), ("factor_flops", ctypes.c_double)]
+                ("total_ms", ctypes.c_double), ("factor_flops", ctypes.c_double),
+                ("solve_ms", ctypes.c_double), ("factor_bytes", ctypes.c_double)]
 
 
 # Exported symbols and their signatures (argtypes, restype).

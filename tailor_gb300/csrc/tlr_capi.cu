@@ -273,7 +273,7 @@ int tlr_set_alpha(tlr_ctx *ctx, double alpha_re, double alpha_im, double omega_r
   ctx->recipe.omega_im = omega_im;
   ctx->assembled = false;
   ctx->have_bc = false;
-  free_factor(ctx);
+  invalidate_factor(ctx);
   return TLR_OK;
 }
 
@@ -286,7 +286,7 @@ int tlr_load_fields(tlr_ctx *ctx, const double *grid, const double *baseflow) {
   TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   ctx->fields = true;
   ctx->have_metrics = ctx->have_derivs = ctx->assembled = ctx->have_bc = false;
-  free_factor(ctx);
+  invalidate_factor(ctx);
   return TLR_OK;
 }
 
@@ -322,7 +322,7 @@ int tlr_assemble(tlr_ctx *ctx, tlr_operator_diag *diag) {
     return fail(ctx, TLR_ERR_WRONGSTATE,
                 "Base-flow derivatives are required before matrix assembly");
   ctx->assembled = ctx->have_bc = false;
-  free_factor(ctx);
+  invalidate_factor(ctx);
   const int rc = run_assemble(ctx, diag);
   if (rc == TLR_OK) ctx->assembled = true;
   return rc;
@@ -334,7 +334,7 @@ int tlr_apply_bc(tlr_ctx *ctx, tlr_bc_diag *diag) {
     return fail(ctx, TLR_ERR_WRONGSTATE,
                 "Global operators must be assembled before boundary conditions");
   ctx->have_bc = false;
-  free_factor(ctx);
+  invalidate_factor(ctx);
   const int rc = run_bc(ctx, diag);
   if (rc == TLR_OK) ctx->have_bc = true;
   return rc;

@@ -132,6 +132,8 @@ int frobenius(tlr_ctx *ctx, const double2 *v, long long count, double *out);
 int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
               double *residual, double *modes, tlr_eig_diag *diag);
 void free_factor(tlr_ctx *ctx);
+// Keep the symbolic analysis and device buffers, drop the numeric factor.
+void invalidate_factor(tlr_ctx *ctx);
 
 inline int blocks_for(long long n, int threads) {
   return static_cast<int>((n + threads - 1) / threads);

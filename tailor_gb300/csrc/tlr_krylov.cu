@@ -90,8 +90,19 @@ struct Solver {
     return out;
   }
 
+  double solve_ms = 0.0;
+
   // out = K^-1 in (FP64 vectors); in may alias nothing else
   int apply_inverse(const double2 *in, double2 *out) {
+    TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = apply_inverse_impl(in, out);
+    TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    solve_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+  }
+
+  int apply_inverse_impl(const double2 *in, double2 *out) {
     cudaStream_t st = ctx->stream;
     const int blocks = blocks_for(n, 256);
     if (F->prec == 0) {
@@ -142,6 +153,10 @@ void fill_start(std::vector<double2> &v, unsigned long long seed) {
 }
 
 }  // namespace
+
+void invalidate_factor(tlr_ctx *ctx) {
+  if (ctx && ctx->factor) ctx->factor->factored = false;
+}
 
 void free_factor(tlr_ctx *ctx) {
   if (ctx && ctx->factor) {
@@ -429,6 +444,8 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     d.krylov_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
     d.total_ms = std::chrono::duration<double, std::milli>(t3 - t0).count();
     d.factor_flops = F->sym.flops;
+    d.solve_ms = S.solve_ms;
+    d.factor_bytes = (double)F->sym.factor_elems * (prec == 0 ? 16.0 : 8.0);
     *diag = d;
   }
   if (reason != 1) {

@@ -288,6 +288,92 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// FP32 trailing update: 128x64 tiles, 256 threads, 8x4 complex register
+// tile per thread (rows tx + 16 i, columns ty + 16 j), K staged 16 at a time
+// through double-buffered shared memory.  Per k step a thread issues 12
+// 8-byte shared loads for 32 complex FMAs (128 FFMA), so the FFMA pipe, not
+// shared memory, is the limit.
+constexpr int kTM32 = 128, kTN32 = 64;
+
+__global__ void __launch_bounds__(256)
+    k_gemm32(const int *__restrict__ fl, const int *__restrict__ prefix, int nf, int s,
+             int w, float2 *__restrict__ pool, const DevFront *__restrict__ fr) {
+  constexpr int KC = 8;
+  __shared__ float2 As[2][KC][kTM32];
+  __shared__ float2 Bs[2][KC][kTN32 + 1];
+  const int t = blockIdx.x;
+  int lo = 0, hi = nf;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) / 2;
+    if (prefix[mid] <= t) lo = mid; else hi = mid;
+  }
+  const DevFront f = fr[fl[lo]];
+  const int m = f.m, k0 = s * w, ww = min(w, f.p - k0);
+  const int base = k0 + ww, ext = m - base;
+  const int ntm = (ext + kTM32 - 1) / kTM32;
+  const int lt = t - prefix[lo];
+  const int R0 = base + (lt % ntm) * kTM32, C0 = base + (lt / ntm) * kTN32;
+  float2 *F = pool + f.off;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  float2 acc[8][4];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.f, 0.f);
+  auto load = [&](int buf, int kk) {
+    for (int x = threadIdx.x; x < KC * kTM32; x += 256) {
+      const int r = x % kTM32, k = x / kTM32;
+      const int gr = R0 + r;
+      As[buf][k][r] = (gr < m && kk + k < ww) ? F[(long long)(k0 + kk + k) * m + gr]
+                                              : make_float2(0.f, 0.f);
+    }
+    for (int x = threadIdx.x; x < KC * kTN32; x += 256) {
+      const int cc = x / KC, kb = x % KC;
+      const int gc = C0 + cc;
+      Bs[buf][kb][cc] = (gc < m && kk + kb < ww) ? F[(long long)gc * m + k0 + kk + kb]
+                                                 : make_float2(0.f, 0.f);
+    }
+  };
+  int buf = 0;
+  load(0, 0);
+  __syncthreads();
+  for (int kk = 0; kk < ww; kk += KC) {
+    if (kk + KC < ww) load(buf ^ 1, kk + KC);
+#pragma unroll
+    for (int k = 0; k < KC; ++k) {
+      float2 a[8], b[4];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) a[i] = As[buf][k][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[buf][k][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          acc[i][j].x = fmaf(a[i].x, b[j].x, acc[i][j].x);
+          acc[i][j].x = fmaf(-a[i].y, b[j].y, acc[i][j].x);
+          acc[i][j].y = fmaf(a[i].x, b[j].y, acc[i][j].y);
+          acc[i][j].y = fmaf(a[i].y, b[j].x, acc[i][j].y);
+        }
+    }
+    __syncthreads();
+    buf ^= 1;
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int gc = C0 + ty + 16 * j;
+    if (gc >= m) continue;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int gr = R0 + tx + 16 * i;
+      if (gr >= m) continue;
+      float2 &d = F[(long long)gc * m + gr];
+      d.x -= acc[i][j].x;
+      d.y -= acc[i][j].y;
+    }
+  }
+}
+
 // ------------------------------------------------------------------ solves
 
 // t[i] = b[unknown of front row perm[i]] for pivot rows, 0 for border rows.
@@ -333,7 +419,7 @@ __global__ void __launch_bounds__(256)
   const DevFront f = fr[fl[blockIdx.y]];
   const int k0 = s * w, ww = min(w, f.p - k0);
   const int r = k0 + ww + blockIdx.x * blockDim.x + threadIdx.x;
-  if (blockIdx.x > 0 && k0 + ww + (int)(blockIdx.x * blockDim.x) >= f.m) return;
+  if (blockIdx.x > 0 && k0 + ww + (int)(blockIdx.x * blockDim.x) >= f.p) return;
   const C *F = pool + f.off;
   const int m = f.m;
   C *t = work + f.toff;
@@ -355,10 +441,108 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   if (blockIdx.x == 0)
     for (int c = threadIdx.x; c < ww; c += blockDim.x) t[k0 + c] = xs[c];
-  if (r >= m) return;
+  if (r >= f.p) return;
   C v = t[r];
+#pragma unroll 8
   for (int c = 0; c < ww; ++c) v = cfms(v, F[(long long)(k0 + c) * m + r], xs[c]);
   t[r] = v;
+}
+
+// forward border coupling of one level, pass 1: partial[front][chunk][r] =
+// sum over a 512-column chunk of L21[r, c] t[c] (L21 = rows p..m-1).
+template <class C>
+__global__ void __launch_bounds__(128)
+    k_fwd_border(const int *__restrict__ fl, const C *__restrict__ pool,
+                 const DevFront *__restrict__ fr, const C *__restrict__ work,
+                 double2 *__restrict__ partial, int nck, int bmax) {
+  __shared__ C ts[512];
+  const DevFront f = fr[fl[blockIdx.z]];
+  const int b = f.m - f.p;
+  const int c0 = blockIdx.y * 512;
+  if (c0 >= f.p || (int)(blockIdx.x * blockDim.x) >= b) return;
+  const int c1 = min(f.p, c0 + 512);
+  const C *t = work + f.toff;
+  for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) ts[c - c0] = t[c];
+  __syncthreads();
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= b) return;
+  const C *F = pool + f.off + f.p + r;
+  C a0 = czero<C>(), a1 = czero<C>();
+  int c = c0;
+  for (; c + 1 < c1; c += 2) {
+    a0 = cfma(a0, F[(long long)c * f.m], ts[c - c0]);
+    a1 = cfma(a1, F[(long long)(c + 1) * f.m], ts[c + 1 - c0]);
+  }
+  if (c < c1) a0 = cfma(a0, F[(long long)c * f.m], ts[c - c0]);
+  partial[((long long)blockIdx.z * nck + blockIdx.y) * bmax + r] = to64(cadd(a0, a1));
+}
+
+// pass 2: t[p + r] -= sum of the chunks, in chunk order.
+template <class C>
+__global__ void k_fwd_border_reduce(const int *__restrict__ fl, const DevFront *__restrict__ fr,
+                                    C *__restrict__ work, const double2 *__restrict__ partial,
+                                    int nck, int bmax) {
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int b = f.m - f.p;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= b) return;
+  const int nc = (f.p + 511) / 512;
+  double2 acc = make_double2(0, 0);
+  for (int q = 0; q < nc; ++q) {
+    const double2 v = partial[((long long)blockIdx.y * nck + q) * bmax + r];
+    acc.x += v.x;
+    acc.y += v.y;
+  }
+  C *t = work + f.toff + f.p + r;
+  *t = csub(*t, from64<C>(acc));
+}
+
+// backward border coupling of one level, pass 1: partial[front][chunk][i]
+// = sum over a 512-column chunk of the border of U12[i, c] t[c], pivot rows i.
+template <class C>
+__global__ void __launch_bounds__(128)
+    k_bwd_border(const int *__restrict__ fl, const C *__restrict__ pool,
+                 const DevFront *__restrict__ fr, const C *__restrict__ work,
+                 double2 *__restrict__ partial, int nck, int pmax) {
+  __shared__ C ts[512];
+  const DevFront f = fr[fl[blockIdx.z]];
+  const int b = f.m - f.p;
+  const int c0 = blockIdx.y * 512;
+  if (c0 >= b || (int)(blockIdx.x * blockDim.x) >= f.p) return;
+  const int c1 = min(b, c0 + 512);
+  const C *t = work + f.toff + f.p;
+  for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) ts[c - c0] = t[c];
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= f.p) return;
+  const C *F = pool + f.off + (long long)f.p * f.m + i;
+  C a0 = czero<C>(), a1 = czero<C>();
+  int c = c0;
+  for (; c + 1 < c1; c += 2) {
+    a0 = cfma(a0, F[(long long)c * f.m], ts[c - c0]);
+    a1 = cfma(a1, F[(long long)(c + 1) * f.m], ts[c + 1 - c0]);
+  }
+  if (c < c1) a0 = cfma(a0, F[(long long)c * f.m], ts[c - c0]);
+  partial[((long long)blockIdx.z * nck + blockIdx.y) * pmax + i] = to64(cadd(a0, a1));
+}
+
+// pass 2: t[i] -= sum of the chunks for the pivot rows.
+template <class C>
+__global__ void k_bwd_border_reduce(const int *__restrict__ fl, const DevFront *__restrict__ fr,
+                                    C *__restrict__ work, const double2 *__restrict__ partial,
+                                    int nck, int pmax) {
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= f.p) return;
+  const int nc = (f.m - f.p + 511) / 512;
+  double2 acc = make_double2(0, 0);
+  for (int q = 0; q < nc; ++q) {
+    const double2 v = partial[((long long)blockIdx.y * nck + q) * pmax + i];
+    acc.x += v.x;
+    acc.y += v.y;
+  }
+  C *t = work + f.toff + i;
+  *t = csub(*t, from64<C>(acc));
 }
 
 // backward step s, fused: CTAs reduce U[k0:k0+ww, chunk] t[chunk] into
@@ -377,7 +561,7 @@ __global__ void __launch_bounds__(256)
   __shared__ int last;
   const DevFront f = fr[fl[blockIdx.y]];
   const int k0 = s * w, ww = min(w, f.p - k0);
-  const int ext = f.m - k0 - ww;
+  const int ext = f.p - k0 - ww;  // columns of the pivot block right of the panel
   const int nch = ext > 0 ? (ext + chunk - 1) / chunk : 1;
   if ((int)blockIdx.x >= nch) return;
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
@@ -386,7 +570,7 @@ __global__ void __launch_bounds__(256)
   C *t = work + f.toff;
   if (ext > 0) {
     const int cbeg = k0 + ww + blockIdx.x * chunk;
-    const int cend = min(m, cbeg + chunk);
+    const int cend = min(f.p, cbeg + chunk);
     C a0 = czero<C>(), a1 = czero<C>();
     for (int c = cbeg + wp; c < cend; c += 8) {
       const C tc = t[c];
@@ -548,9 +732,9 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
         const FrontInfo &f = sym.fronts[fl[q]];
         const int ww = std::min(w, f.p - s * w);
         const int ext = f.m - s * w - ww;
-        const int nt = (ext + kTile - 1) / kTile;
+        const int tm = prec == 0 ? kTile : kTM32, tn = prec == 0 ? kTile : kTN32;
         sched.push_back(acc);
-        acc += nt * nt;
+        acc += ((ext + tm - 1) / tm) * ((ext + tn - 1) / tn);
         st.max_m = std::max(st.max_m, f.m);
         st.max_b = std::max(st.max_b, f.m - f.p);
         st.max_ext = std::max(st.max_ext, ext);
@@ -562,10 +746,33 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
     levels.push_back(L);
   }
   max_chunks = 1;
-  for (auto &L : levels)
-    for (auto &st : L.steps) max_chunks = std::max(max_chunks, (st.max_ext + kChunk - 1) / kChunk);
+  long long partial_elems = 0;
+  for (auto &L : levels) {
+    L.pmax = 0;
+    L.bmax = 0;
+    for (int q = 0; q < L.nfronts; ++q) {
+      const FrontInfo &f = sym.fronts[sched[L.fronts_off + q]];
+      L.pmax = std::max(L.pmax, f.p);
+      L.bmax = std::max(L.bmax, f.m - f.p);
+    }
+    L.nck_f = std::max(1, (L.pmax + 511) / 512);
+    L.nck_b = std::max(1, (L.bmax + 511) / 512);
+    for (auto &st : L.steps) {
+      // per-step backward chunks cover only the pivot block right of the panel
+      int ext_p = 0;
+      for (int q = 0; q < st.nf; ++q) {
+        const FrontInfo &f = sym.fronts[sched[L.fronts_off + q]];
+        ext_p = std::max(ext_p, f.p - (int)(&st - L.steps.data()) * w - std::min(w, f.p - (int)(&st - L.steps.data()) * w));
+      }
+      st.max_ext_p = ext_p;
+      max_chunks = std::max(max_chunks, (ext_p + kChunk - 1) / kChunk);
+    }
+    partial_elems = std::max(partial_elems, (long long)L.nfronts * L.nck_f * std::max(L.bmax, 1));
+    partial_elems = std::max(partial_elems, (long long)L.nfronts * L.nck_b * std::max(L.pmax, 1));
+  }
   int max_lvl_fronts = 1;
   for (auto &L : levels) max_lvl_fronts = std::max(max_lvl_fronts, L.nfronts);
+  partial_elems = std::max(partial_elems, (long long)max_lvl_fronts * max_chunks * 64);
   const size_t csize = prec == 0 ? sizeof(double2) : sizeof(float2);
   auto alloc = [&](void **p, size_t bytes) -> int {
     cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
@@ -586,8 +793,7 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
       (rc = alloc((void **)&d_perm, sym.work_elems * sizeof(int))) ||
       (rc = alloc((void **)&d_pmap, sym.work_elems * sizeof(int))) ||
       (rc = alloc((void **)&d_sched, sched.size() * sizeof(int))) ||
-      (rc = alloc((void **)&d_partial,
-                  (size_t)max_lvl_fronts * max_chunks * 64 * sizeof(double2))) ||
+      (rc = alloc((void **)&d_partial, (size_t)partial_elems * sizeof(double2))) ||
       (rc = alloc((void **)&d_pert, sizeof(int))) ||
       (rc = alloc((void **)&d_ticket, max_lvl_fronts * sizeof(int))) ||
       (rc = alloc(&vec_a, (size_t)ctx->nn * 5 * csize)))
@@ -652,9 +858,14 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
       if (S.max_ext > 0) {
         k_trsm_urow<C><<<dim3(blocks_for(S.max_ext, 128), S.nf), 128, tsm, st>>>(fl, s, w, P,
                                                                                  d_fronts);
-        if (S.tiles > 0)
-          k_gemm<C><<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w, P,
-                                             d_fronts);
+        if (S.tiles > 0) {
+          if constexpr (sizeof(C) == sizeof(float2))
+            k_gemm32<<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w,
+                                              reinterpret_cast<float2 *>(P), d_fronts);
+          else
+            k_gemm<C><<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w, P,
+                                               d_fronts);
+        }
       }
     }
   }
@@ -719,8 +930,14 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
                          128, 0, st>>>(d_sched + L.kids_off[slot], d_fronts, d_pmap, W);
     for (int s = 0; s < (int)L.steps.size(); ++s) {
       const Step &S = L.steps[s];
-      k_fwd_step<C><<<dim3(std::max(blocks_for(S.max_ext, 256), 1), S.nf), 256, 0, st>>>(
+      k_fwd_step<C><<<dim3(std::max(blocks_for(S.max_ext_p, 256), 1), S.nf), 256, 0, st>>>(
           fl, s, w, P, d_fronts, W);
+    }
+    if (L.bmax > 0) {
+      k_fwd_border<C><<<dim3(blocks_for(L.bmax, 128), L.nck_f, L.nfronts), 128, 0, st>>>(
+          fl, P, d_fronts, W, d_partial, L.nck_f, L.bmax);
+      k_fwd_border_reduce<C><<<dim3(blocks_for(L.bmax, 128), L.nfronts), 128, 0, st>>>(
+          fl, d_fronts, W, d_partial, L.nck_f, L.bmax);
     }
   }
   for (int h = (int)levels.size() - 1; h >= 0; --h) {
@@ -728,9 +945,15 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
     const int *fl = d_sched + L.fronts_off;
     k_bgather<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(fl, d_fronts,
                                                                              d_nodes, x, W);
+    if (L.bmax > 0) {
+      k_bwd_border<C><<<dim3(blocks_for(L.pmax, 128), L.nck_b, L.nfronts), 128, 0, st>>>(
+          fl, P, d_fronts, W, d_partial, L.nck_b, L.pmax);
+      k_bwd_border_reduce<C><<<dim3(blocks_for(L.pmax, 128), L.nfronts), 128, 0, st>>>(
+          fl, d_fronts, W, d_partial, L.nck_b, L.pmax);
+    }
     for (int s = (int)L.steps.size() - 1; s >= 0; --s) {
       const Step &S = L.steps[s];
-      const int nch = S.max_ext > 0 ? (S.max_ext + kChunk - 1) / kChunk : 1;
+      const int nch = S.max_ext_p > 0 ? (S.max_ext_p + kChunk - 1) / kChunk : 1;
       k_bwd_step<C><<<dim3(nch, S.nf), 256, 0, st>>>(fl, s, w, kChunk, P, d_fronts, W,
                                                      d_partial, max_chunks, d_ticket);
     }

@@ -13,14 +13,16 @@ struct DevFront {
   int p, m, parent, node_off;
 };
 
-constexpr int kChunk = 1024;  // columns per CTA in the backward GEMV
+constexpr int kChunk = 256;   // columns per CTA in the backward step GEMV
 
 struct Step {  // one panel step of one level
   int nf, max_m, max_b, max_ext, prefix_off, tiles;
+  int max_ext_p = 0;  // pivot-block columns right of the panel
 };
 
 struct Level {
   int nfronts = 0, fronts_off = 0, max_m = 0;
+  int pmax = 0, bmax = 0, nck_f = 1, nck_b = 1;  // border GEMV chunking
   int kids[2] = {0, 0}, kids_off[2] = {0, 0}, kids_maxb[2] = {0, 0};
   long long entry_begin = 0, entry_end = 0, pool_begin = 0, pool_end = 0;
   std::vector<Step> steps;

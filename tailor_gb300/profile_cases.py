@@ -48,7 +48,8 @@ def main() -> None:
         if a.stage == "solve":
             sol = api.EigenSolver(p).solve(precision=a.precision)
             out["solve"] = {k: sol.diag[k] for k in ("factor_ms", "krylov_ms", "solves",
-                                                     "iterations", "max_relative_error")}
+                                                     "iterations", "max_relative_error",
+                                                     "solve_ms", "factor_bytes", "factor_flops")}
     print(json.dumps(out))
 
 
