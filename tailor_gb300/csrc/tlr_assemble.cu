@@ -251,6 +251,184 @@ __global__ void __launch_bounds__(kWriterThreads)
   }
 }
 
+// Writer specialised on the stencil sizes (SX xi slots, SE eta slots).
+// Per group of kSub nodes:
+//   pass A  every line-block entry: (w1 K_re, w1 K_im)          (lane-dense)
+//           every cross block: scale s = -(w1_eta w1_xi) and its 6 nonzeros
+//   pass B  the 6 viscous positions of each non-centre line block:
+//           re = (w1 K_re + (-w2) V) + s Vxieta                   (lane-dense)
+//   pass C  the centre block from scratch: ((K0 + xi) + eta) + cross
+//   store   one warp per 5x5 block: the block's line/cross/zero source is
+//           decided once per warp, lanes 0..24 store 400 contiguous bytes.
+// Dropping the products with structural zeros of V is exact: for finite y,
+// x + 0*y equals x (up to the sign of a zero result).
+template <int SX, int SE>
+struct WriterSharedT {
+  static constexpr int S = SX * SE, NL = SX + SE - 1;
+  double cf[kSub][CF_COUNT];
+  double2 line[kSub][NL][25];
+  double cross[kSub][S][6];
+  double scl[kSub][S];
+  double w1x[kSub][SX], w2x[kSub][SX];
+  double w1e[kSub][SE], w2e[kSub][SE];
+  int order[kSub][SE];
+  int rank[kSub][SE];  // rank[u][slot] = sorted position of eta slot
+  int cx[kSub], ce[kSub];
+};
+
+template <int SX, int SE>
+__global__ void __launch_bounds__(kWriterThreads)
+    k_write_rows_t(int ny, int nz, DevRule xi, DevRule eta, const double *__restrict__ coef,
+                   double2 *__restrict__ L, double2 *__restrict__ Mv) {
+  using SH = WriterSharedT<SX, SE>;
+  constexpr int S = SH::S, NL = SH::NL;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SH &sh = *reinterpret_cast<SH *>(smem_raw);
+  const int nn = ny * nz;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int groups = (nn + kSub - 1) / kSub;
+  for (int g = blockIdx.x; g < groups; g += gridDim.x) {
+    const int n0 = g * kSub;
+    const int cnt = min(kSub, nn - n0);
+    for (int x = tid; x < CF_COUNT * kSub; x += kWriterThreads) {
+      const int f = x / kSub, u = x % kSub;
+      sh.cf[u][f] = u < cnt ? coef[(size_t)f * nn + n0 + u] : 0.0;
+    }
+    for (int x = tid; x < kSub * (SX + SE + 1); x += kWriterThreads) {
+      const int u = x / (SX + SE + 1), r = x % (SX + SE + 1);
+      const int n = min(n0 + u, nn - 1);
+      const int i = n % ny, j = n / ny;
+      if (r < SX) {
+        sh.w1x[u][r] = xi.w1[i * SX + r];
+        sh.w2x[u][r] = xi.w2[i * SX + r];
+      } else if (r < SX + SE) {
+        const int q = r - SX;
+        sh.w1e[u][q] = eta.w1[j * SE + q];
+        sh.w2e[u][q] = eta.w2[j * SE + q];
+        sh.order[u][q] = eta.order[j * SE + q];
+        sh.rank[u][eta.order[j * SE + q]] = q;
+      } else {
+        sh.cx[u] = xi.centre[i];
+        sh.ce[u] = eta.centre[j];
+      }
+    }
+    __syncthreads();
+    // pass A: w1 K for every line entry; cross scales and nonzeros
+    for (int x = tid; x < kSub * NL * 25; x += kWriterThreads) {
+      const int u = x / (NL * 25), rem = x % (NL * 25);
+      const int lb = rem / 25, rc = rem % 25;
+      const double *cf = sh.cf[u];
+      double w1, kr, ki;
+      if (lb < SX) {
+        w1 = sh.w1x[u][lb];
+        kr = cf[CF_KXI_RE + rc];
+        ki = cf[CF_KXI_IM + rc];
+      } else {
+        int q = lb - SX;
+        if (q >= sh.ce[u]) ++q;
+        w1 = sh.w1e[u][q];
+        kr = cf[CF_KETA_RE + rc];
+        ki = cf[CF_KETA_IM + rc];
+      }
+      sh.line[u][lb][rc] = make_double2(w1 * kr, w1 * ki);
+    }
+    for (int x = tid; x < kSub * S; x += kWriterThreads) {
+      const int u = x / S, k = x % S;
+      const int q = sh.order[u][k / SX], t = k % SX;
+      const double sc = -sh.w1e[u][q] * sh.w1x[u][t];
+      sh.scl[u][k] = sc;
+#pragma unroll
+      for (int p = 0; p < 6; ++p) sh.cross[u][k][p] = sc * sh.cf[u][CF_VXE + c_vpos[p]];
+    }
+    __syncthreads();
+    // pass B: viscous positions of the non-centre line blocks
+    for (int x = tid; x < kSub * NL * 6; x += kWriterThreads) {
+      const int u = x / (NL * 6), rem = x % (NL * 6);
+      const int lb = rem / 6, pidx = rem % 6, rc = c_vpos[pidx];
+      const int cx = sh.cx[u], ce = sh.ce[u];
+      const double *cf = sh.cf[u];
+      double w2, v, sc;
+      if (lb < SX) {
+        if (lb == cx) continue;
+        w2 = -sh.w2x[u][lb];
+        v = cf[CF_VXX + rc];
+        sc = sh.scl[u][sh.rank[u][ce] * SX + lb];  // block (eta slot ce, xi slot lb)
+      } else {
+        int q = lb - SX;
+        if (q >= ce) ++q;
+        w2 = -sh.w2e[u][q];
+        v = cf[CF_VEE + rc];
+        sc = sh.scl[u][sh.rank[u][q] * SX + cx];  // block (eta slot q, xi slot cx)
+      }
+      double2 &e = sh.line[u][lb][rc];
+      e.x = (e.x + w2 * v) + sc * cf[CF_VXE + rc];
+    }
+    // pass C: the centre block
+    for (int x = tid; x < kSub * 25; x += kWriterThreads) {
+      const int u = x / 25, rc = x % 25;
+      const int cx = sh.cx[u], ce = sh.ce[u];
+      const double *cf = sh.cf[u];
+      const double w1x = sh.w1x[u][cx], w2x = -sh.w2x[u][cx];
+      const double w1e = sh.w1e[u][ce], w2e = -sh.w2e[u][ce];
+      const double sc = -w1e * w1x;
+      const double bre = w1x * cf[CF_KXI_RE + rc] + w2x * cf[CF_VXX + rc];
+      const double ere = w1e * cf[CF_KETA_RE + rc] + w2e * cf[CF_VEE + rc];
+      const double re = ((cf[CF_K0_RE + rc] + bre) + ere) + sc * cf[CF_VXE + rc];
+      const double im = (cf[CF_K0_IM + rc] + w1x * cf[CF_KXI_IM + rc]) + w1e * cf[CF_KETA_IM + rc];
+      sh.line[u][cx][rc] = make_double2(re, im);
+    }
+    __syncthreads();
+    // store: one warp per block
+    for (int b = warp; b < cnt * S; b += kWriterThreads / 32) {
+      const int u = b / S, k = b % S;
+      const int r = k / SX, t = k % SX;
+      const int q = sh.order[u][r];
+      const int cx = sh.cx[u], ce = sh.ce[u];
+      const int lb = q == ce ? t : (t == cx ? SX + (q < ce ? q : q - 1) : -1);
+      if (lane < 25) {
+        double2 v;
+        if (lb >= 0) {
+          v = sh.line[u][lb][lane];
+        } else {
+          const int vi = c_vidx[lane];
+          v = make_double2(vi >= 0 ? sh.cross[u][k][vi] : 0.0, 0.0);
+        }
+        __stcs(L + ((long long)(n0 + u) * S + k) * 25 + lane, v);
+      }
+    }
+    for (int u = warp; u < cnt; u += kWriterThreads / 32)
+      if (lane < 25)
+        __stcs(Mv + (long long)(n0 + u) * 25 + lane, make_double2(sh.cf[u][CF_GAMMA + lane], 0.0));
+    __syncthreads();
+  }
+}
+
+template <int SX, int SE>
+int launch_writer_t(tlr_ctx *ctx) {
+  const size_t smem = sizeof(WriterSharedT<SX, SE>);
+  TLR_CUDA(ctx, cudaFuncSetAttribute(k_write_rows_t<SX, SE>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int sms = 0, per_sm = 0;
+  TLR_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  TLR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_write_rows_t<SX, SE>,
+                                                              kWriterThreads, smem));
+  const int groups = (ctx->nn + kSub - 1) / kSub;
+  const int grid = std::max(1, std::min(groups, sms * std::max(per_sm, 1)));
+  k_write_rows_t<SX, SE><<<grid, kWriterThreads, smem, ctx->stream>>>(
+      ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->coef, ctx->L, ctx->M);
+  TLR_CUDA(ctx, cudaGetLastError());
+  return TLR_OK;
+}
+
+// Specialised writer for the common stencils; -1 when none applies.
+int launch_writer(tlr_ctx *ctx) {
+  if (ctx->sx == 11 && ctx->se == 7) return launch_writer_t<11, 7>(ctx);
+  if (ctx->sx == 11 && ctx->se == 5) return launch_writer_t<11, 5>(ctx);
+  if (ctx->sx == 5 && ctx->se == 5) return launch_writer_t<5, 5>(ctx);
+  if (ctx->sx == 5 && ctx->se == 7) return launch_writer_t<5, 7>(ctx);
+  return -1;
+}
+
 }  // namespace
 
 int run_pattern(tlr_ctx *ctx) {
@@ -307,9 +485,13 @@ int run_assemble(tlr_ctx *ctx, tlr_operator_diag *diag) {
   const int groups = (ctx->nn + kSub - 1) / kSub;
   const int grid = std::max(1, std::min(groups, sms * std::max(per_sm, 1)));
   TLR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-  k_write_rows<<<grid, kWriterThreads, smem, ctx->stream>>>(
-      ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->coef, ctx->L, ctx->M);
-  TLR_CUDA(ctx, cudaGetLastError());
+  const int wr = launch_writer(ctx);
+  if (wr > 0) return wr;
+  if (wr < 0) {
+    k_write_rows<<<grid, kWriterThreads, smem, ctx->stream>>>(
+        ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->coef, ctx->L, ctx->M);
+    TLR_CUDA(ctx, cudaGetLastError());
+  }
   TLR_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
   TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (diag) {

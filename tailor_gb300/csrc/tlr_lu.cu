@@ -442,9 +442,14 @@ __global__ void __launch_bounds__(256)
   if (blockIdx.x == 0)
     for (int c = threadIdx.x; c < ww; c += blockDim.x) t[k0 + c] = xs[c];
   if (r >= f.p) return;
+  C lv[WM];
+#pragma unroll
+  for (int c = 0; c < WM; ++c)
+    if (c < ww) lv[c] = F[(long long)(k0 + c) * m + r];
   C v = t[r];
-#pragma unroll 8
-  for (int c = 0; c < ww; ++c) v = cfms(v, F[(long long)(k0 + c) * m + r], xs[c]);
+#pragma unroll
+  for (int c = 0; c < WM; ++c)
+    if (c < ww) v = cfms(v, lv[c], xs[c]);
   t[r] = v;
 }
 
@@ -569,10 +574,13 @@ __global__ void __launch_bounds__(256)
   const int m = f.m;
   C *t = work + f.toff;
   if (ext > 0) {
-    const int cbeg = k0 + ww + blockIdx.x * chunk;
-    const int cend = min(f.p, cbeg + chunk);
+    // each warp owns chunk/8 consecutive columns; all its loads are
+    // independent, so they are issued back to back
+    const int cbeg = k0 + ww + blockIdx.x * chunk + wp * (chunk / 8);
+    const int cend = min(f.p, cbeg + chunk / 8);
     C a0 = czero<C>(), a1 = czero<C>();
-    for (int c = cbeg + wp; c < cend; c += 8) {
+#pragma unroll 4
+    for (int c = cbeg; c < cend; ++c) {
       const C tc = t[c];
       const C *colp = F + (long long)c * m + k0;
       if (lane < ww) a0 = cfma(a0, colp[lane], tc);
@@ -930,7 +938,7 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
                          128, 0, st>>>(d_sched + L.kids_off[slot], d_fronts, d_pmap, W);
     for (int s = 0; s < (int)L.steps.size(); ++s) {
       const Step &S = L.steps[s];
-      k_fwd_step<C><<<dim3(std::max(blocks_for(S.max_ext_p, 256), 1), S.nf), 256, 0, st>>>(
+      k_fwd_step<C><<<dim3(std::max(blocks_for(S.max_ext_p, 64), 1), S.nf), 64, 0, st>>>(
           fl, s, w, P, d_fronts, W);
     }
     if (L.bmax > 0) {

@@ -13,7 +13,7 @@ struct DevFront {
   int p, m, parent, node_off;
 };
 
-constexpr int kChunk = 256;   // columns per CTA in the backward step GEMV
+constexpr int kChunk = 64;    // columns per CTA in the backward step GEMV (8 per warp)
 
 struct Step {  // one panel step of one level
   int nf, max_m, max_b, max_ext, prefix_off, tiles;
