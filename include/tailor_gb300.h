@@ -142,6 +142,12 @@ void tlr_ctx_destroy(tlr_ctx *ctx);
 int tlr_set_alpha(tlr_ctx *ctx, double alpha_re, double alpha_im,
                   double omega_re, double omega_im);
 
+/* Replace every numerical recipe value (physics, wavenumber, target,
+ * solver settings) of a context; q_y / q_z must not change.  The grid,
+ * rules, symbolic analysis and buffers are kept; the derived operators
+ * must be re-assembled (sweeps over alpha, Re, Mach reuse one context). */
+int tlr_set_physics(tlr_ctx *ctx, const tlr_recipe *recipe);
+
 /* Host arrays in natural order: grid [N][3] complex (x, y, z), baseflow
  * [N][5] complex (rho, U, V, W, T) (Prepare.cpp:537-586). */
 int tlr_load_fields(tlr_ctx *ctx, const double *grid, const double *baseflow);
@@ -202,6 +208,28 @@ typedef struct {
 /* lambda [nev] complex, residual [nev]; modes [nev][5N] complex or NULL. */
 int tlr_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
               double *residual, double *modes, tlr_eig_diag *diag);
+
+/* Learned shift / start-vector proposal: a multilayer perceptron with
+ * `depth` SiLU hidden layers of `width` units, trained and evaluated on the
+ * GPU by hand-written kernels.  No reference counterpart (the reference
+ * starts SLEPc from a random vector at the configured target).  Parameters
+ * are FP32, flat per layer: W [out][in] row-major, then b [out].  All
+ * arrays are host arrays, row-major [rows][features]. */
+typedef struct tlr_mlp tlr_mlp;
+int tlr_mlp_create(int n_in, int width, int depth, int n_out,
+                   unsigned long long seed, tlr_mlp **out);
+void tlr_mlp_destroy(tlr_mlp *m);
+long long tlr_mlp_num_params(const tlr_mlp *m);
+/* set != 0 copies params into the network, else out of it */
+int tlr_mlp_params(tlr_mlp *m, float *params, int set);
+/* mean-squared-error loss and its parameter gradient on one batch */
+int tlr_mlp_gradients(tlr_mlp *m, const float *x, const float *y, int n,
+                      float *grads, float *loss);
+/* Adam over `epochs` passes in minibatches; loss_history[epochs] optional */
+int tlr_mlp_train(tlr_mlp *m, const float *x, const float *y, int n,
+                  int epochs, int batch, float lr, float *loss_history);
+/* inference; bf16 != 0 rounds weights and activations to bfloat16 */
+int tlr_mlp_forward(tlr_mlp *m, const float *x, int n, float *y, int bf16);
 
 /* Frobenius norm sqrt(sum |v|^2) of `count` complex values at the device
  * address `values`, written to the host double `result`, computed on

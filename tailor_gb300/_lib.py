@@ -97,6 +97,7 @@ SIGNATURES = {
     "tlr_ctx_destroy": ([_P], None),
     "tlr_set_alpha": ([_P, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                        ctypes.c_double], _I),
+    "tlr_set_physics": ([_P, _P], _I),
     "tlr_load_fields": ([_P, _P, _P], _I),
     "tlr_metrics": ([_P, _P], _I),
     "tlr_baseflow_derivatives": ([_P, _P], _I),
@@ -110,6 +111,13 @@ SIGNATURES = {
     "tlr_solve": ([_P, _P, _P, _P, _P, _P], _I),
     "tlr_stream": ([_P], ctypes.c_void_p),
     "tlr_frobenius_noalloc": ([_P, ctypes.c_size_t, _P, _P], _I),
+    "tlr_mlp_create": ([_I, _I, _I, _I, ctypes.c_ulonglong, _P], _I),
+    "tlr_mlp_destroy": ([_P], None),
+    "tlr_mlp_num_params": ([_P], ctypes.c_longlong),
+    "tlr_mlp_params": ([_P, _P, _I], _I),
+    "tlr_mlp_gradients": ([_P, _P, _P, _I, _P, _P], _I),
+    "tlr_mlp_train": ([_P, _P, _P, _I, _I, _I, ctypes.c_float, _P], _I),
+    "tlr_mlp_forward": ([_P, _P, _I, _P, _I], _I),
     "tlr_status_string": ([_I], ctypes.c_char_p),
     "tlr_last_error": ([_P], ctypes.c_char_p),
 }

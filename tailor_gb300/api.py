@@ -115,6 +115,12 @@ class Problem:
                                           complex(omega).real,
                                           complex(omega).imag))
 
+    def set_physics(self, physics) -> None:
+        """New Re / Mach / alpha / target on the same grid (re-assemble after)."""
+        self.case.physics = physics
+        r = make_recipe(self.case)
+        self.check(self.lib.tlr_set_physics(self.ctx, ctypes.byref(r)))
+
     def copy_out(self, what: int) -> np.ndarray:
         nbytes = self.lib.tlr_out_bytes(self.ctx, what)
         nn = self.case.nodes

@@ -277,6 +277,17 @@ int tlr_set_alpha(tlr_ctx *ctx, double alpha_re, double alpha_im, double omega_r
   return TLR_OK;
 }
 
+int tlr_set_physics(tlr_ctx *ctx, const tlr_recipe *recipe) {
+  if (!ctx || !recipe) return fail(ctx, TLR_ERR_ARG, "null recipe");
+  if (recipe->q_y != ctx->recipe.q_y || recipe->q_z != ctx->recipe.q_z)
+    return fail(ctx, TLR_ERR_SIZE, "FD-q degrees cannot change within a context");
+  ctx->recipe = *recipe;
+  ctx->assembled = false;
+  ctx->have_bc = false;
+  invalidate_factor(ctx);
+  return TLR_OK;
+}
+
 int tlr_load_fields(tlr_ctx *ctx, const double *grid, const double *baseflow) {
   if (!ctx || !grid || !baseflow) return fail(ctx, TLR_ERR_ARG, "null field array");
   TLR_CUDA(ctx, cudaMemcpyAsync(ctx->grid_c, grid, sizeof(double) * 6 * ctx->nn,

@@ -14,7 +14,10 @@
 //   k_gemm         trailing update F22 -= L21 U12 (the Schur complement)
 // Pivot search is restricted to fully summed rows (no delayed pivots); an
 // exactly zero pivot column is perturbed and counted, and the caller
-// refines.  The solves reuse the same level/step schedule.
+// refines.  After the last level every pivot block's kSW x kSW diagonal
+// blocks are inverted explicitly (k_tri_inv), so each solve step is a
+// parallel GEMV plus one small dense product instead of a serial
+// substitution; the solves walk the same levels.
 #include <algorithm>
 #include <cstdio>
 #include <vector>
@@ -74,73 +77,112 @@ __global__ void k_extend(const int *__restrict__ kids, const DevFront *__restric
   }
 }
 
+// Panel factorisation of step s for one front per CTA: columns k0..k0+ww,
+// partial pivoting over the fully summed rows k0..p-1.  The panel is
+// processed in sub-panels of kSB columns: pivoting, scaling and rank-1
+// updates stay inside the sub-panel, then the rest of the panel is updated
+// once per sub-panel (a unit-lower solve for its U rows and a rank-kSB
+// update below), so each panel element crosses L2 ww/kSB times instead of
+// ww times.
+constexpr int kSB = 8;
+
 template <class C>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
     k_panel(const int *__restrict__ fl, int s, int w, C *__restrict__ pool,
             const DevFront *__restrict__ fr, int *__restrict__ ipiv,
             int *__restrict__ pert, double tiny) {
   using T = typename Real<C>::T;
-  __shared__ T sval[256];
-  __shared__ int sidx[256];
+  __shared__ T sval[512];
+  __shared__ int sidx[512];
   __shared__ int piv_sh;
+  __shared__ C lsub[kSB][kSB];
   const DevFront f = fr[fl[blockIdx.x]];
   C *F = pool + f.off;
   const int m = f.m, p = f.p;
   const int k0 = s * w, ww = min(w, p - k0);
-  const int tid = threadIdx.x;
-  for (int j = 0; j < ww; ++j) {
-    const int col = k0 + j;
-    T best = -1;
-    int bi = col;
-    for (int r = col + tid; r < p; r += blockDim.x) {
-      const T a = cabs1(F[(long long)col * m + r]);
-      if (a > best) { best = a; bi = r; }
-    }
-    sval[tid] = best;
-    sidx[tid] = bi;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-      if (tid < o) {
-        const T a = sval[tid + o];
-        const int ia = sidx[tid + o];
-        if (a > sval[tid] || (a == sval[tid] && ia < sidx[tid])) {
-          sval[tid] = a;
-          sidx[tid] = ia;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int jb = 0; jb < ww; jb += kSB) {
+    const int nb = min(kSB, ww - jb);
+    const int c0 = k0 + jb, c1 = c0 + nb;  // sub-panel columns [c0, c1)
+    for (int col = c0; col < c1; ++col) {
+      T best = -1;
+      int bi = col;
+      for (int r = col + tid; r < p; r += nt) {
+        const T a = cabs1(F[(long long)col * m + r]);
+        if (a > best) { best = a; bi = r; }
+      }
+      sval[tid] = best;
+      sidx[tid] = bi;
+      __syncthreads();
+      for (int o = nt / 2; o > 0; o >>= 1) {
+        if (tid < o) {
+          const T a = sval[tid + o];
+          const int ia = sidx[tid + o];
+          if (a > sval[tid] || (a == sval[tid] && ia < sidx[tid])) {
+            sval[tid] = a;
+            sidx[tid] = ia;
+          }
         }
+        __syncthreads();
+      }
+      if (tid == 0) {
+        piv_sh = sidx[0];
+        ipiv[f.toff + col] = sidx[0];
+      }
+      __syncthreads();
+      const int pr = piv_sh;
+      if (pr != col)
+        for (int c = k0 + tid; c < k0 + ww; c += nt) {
+          const C t = F[(long long)c * m + col];
+          F[(long long)c * m + col] = F[(long long)c * m + pr];
+          F[(long long)c * m + pr] = t;
+        }
+      __syncthreads();
+      C pv = F[(long long)col * m + col];
+      if (cabs1(pv) == T(0)) {
+        pv = cmake<C>((T)tiny, 0);
+        if (tid == 0) {
+          F[(long long)col * m + col] = pv;
+          atomicAdd(pert, 1);
+        }
+      }
+      const C inv = cinv(pv);
+      for (int r = col + 1 + tid; r < p; r += nt)
+        F[(long long)col * m + r] = cmul(F[(long long)col * m + r], inv);
+      __syncthreads();
+      const int nr = p - col - 1, nc = c1 - col - 1;
+      for (int x = tid; x < nr * nc; x += nt) {
+        const int r = col + 1 + x % nr, c = col + 1 + x / nr;
+        F[(long long)c * m + r] =
+            cfms(F[(long long)c * m + r], F[(long long)col * m + r], F[(long long)c * m + col]);
       }
       __syncthreads();
     }
-    if (tid == 0) {
-      piv_sh = sidx[0];
-      ipiv[f.toff + col] = sidx[0];
-    }
+    if (c1 >= k0 + ww) break;
+    // U rows of the sub-panel for the remaining panel columns: unit-lower solve
+    for (int x = tid; x < nb * nb; x += nt) lsub[x / nb][x % nb] = F[(long long)(c0 + x % nb) * m + c0 + x / nb];
     __syncthreads();
-    const int pr = piv_sh;
-    if (pr != col) {
-      for (int c = k0 + tid; c < k0 + ww; c += blockDim.x) {
-        const C t = F[(long long)c * m + col];
-        F[(long long)c * m + col] = F[(long long)c * m + pr];
-        F[(long long)c * m + pr] = t;
+    for (int c = c1 + tid; c < k0 + ww; c += nt) {
+      C xr[kSB];
+#pragma unroll
+      for (int r = 0; r < kSB; ++r) {
+        if (r >= nb) break;
+        C v = F[(long long)c * m + c0 + r];
+        for (int rp = 0; rp < r; ++rp) v = cfms(v, lsub[r][rp], xr[rp]);
+        xr[r] = v;
+        F[(long long)c * m + c0 + r] = v;
       }
     }
     __syncthreads();
-    C pv = F[(long long)col * m + col];
-    if (cabs1(pv) == T(0)) {
-      pv = cmake<C>((T)tiny, 0);
-      if (tid == 0) {
-        F[(long long)col * m + col] = pv;
-        atomicAdd(pert, 1);
-      }
-    }
-    const C inv = cinv(pv);
-    for (int r = col + 1 + tid; r < p; r += blockDim.x)
-      F[(long long)col * m + r] = cmul(F[(long long)col * m + r], inv);
-    __syncthreads();
-    const int nr = p - col - 1, nc = k0 + ww - col - 1;
-    for (int x = tid; x < nr * nc; x += blockDim.x) {
-      const int r = col + 1 + x % nr, c = col + 1 + x / nr;
-      F[(long long)c * m + r] =
-          cfms(F[(long long)c * m + r], F[(long long)col * m + r], F[(long long)c * m + col]);
+    // rank-nb update of the rest of the panel below the sub-panel
+    const int nr = p - c1, nc = k0 + ww - c1;
+    for (int x = tid; x < nr * nc; x += nt) {
+      const int r = c1 + x % nr, c = c1 + x / nr;
+      C v = F[(long long)c * m + r];
+#pragma unroll
+      for (int t = 0; t < kSB; ++t)
+        if (t < nb) v = cfms(v, F[(long long)(c0 + t) * m + r], F[(long long)c * m + c0 + t]);
+      F[(long long)c * m + r] = v;
     }
     __syncthreads();
   }
@@ -406,51 +448,223 @@ __global__ void k_saddchild(const int *__restrict__ kids, const DevFront *__rest
   d = cadd(d, work[fc.toff + fc.p + x]);
 }
 
-// forward step s, fused: every CTA loads the ww x ww diagonal block of L
-// and t[k0:k0+ww] into shared memory, solves the unit-lower system there,
-// and updates its chunk of rows k0+ww..m-1; CTA 0 writes the solved part.
+// ---- block-inverse triangular solves ------------------------------------
+// After factorisation every front's pivot block is cut into diagonal
+// blocks of kSW rows; their explicit inverses inv(L_bb) (unit lower) and
+// inv(U_bb) are stored, so a solve step is a parallel GEMV instead of a
+// serial substitution.  One launch per block step: CTAs update their row
+// (forward) or column (backward) chunk, and the last CTA of the front
+// (atomic ticket, no waiting) applies the next block's inverse.
+
+// inverses of diagonal block fb.y of front fb.x: blockIdx.y = 0 gives
+// inv(L_bb) (unit lower), 1 gives inv(U_bb).  Thread r owns row r of the
+// inverse for a chunk of kIC columns in registers; step q publishes the
+// final row q through shared memory and the other rows take its multiple
+// (column-oriented substitution).  Stored column-major, leading dim nb.
+constexpr int kIC = 32;
+
+template <class C>
+__global__ void __launch_bounds__(kSW)
+    k_tri_inv(const int2 *__restrict__ blocks, const C *__restrict__ pool,
+              const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
+              C *__restrict__ Linv, C *__restrict__ Uinv) {
+  __shared__ C rowq[kIC];
+  const int2 fb = blocks[blockIdx.x];
+  const DevFront f = fr[fb.x];
+  const int b0 = fb.y * kSW, nb = min(kSW, f.p - b0);
+  const C *F = pool + f.off + (long long)b0 * f.m + b0;  // F[c * m + r] = K_bb(r, c)
+  const int m = f.m, r = threadIdx.x;
+  const bool lower = blockIdx.y == 0;
+  C *out = (lower ? Linv : Uinv) + inv_off[fb.x] + (long long)fb.y * kSW * kSW;
+  for (int c0 = 0; c0 < nb; c0 += kIC) {
+    C x[kIC];
+#pragma unroll
+    for (int j = 0; j < kIC; ++j) x[j] = r == c0 + j ? cmake<C>(1, 0) : czero<C>();
+    if (lower) {
+      for (int q = c0; q < nb; ++q) {
+        if (r == q)
+#pragma unroll
+          for (int j = 0; j < kIC; ++j) rowq[j] = x[j];
+        __syncthreads();
+        if (r > q && r < nb) {
+          const C l = F[(long long)q * m + r];
+#pragma unroll
+          for (int j = 0; j < kIC; ++j) x[j] = cfms(x[j], l, rowq[j]);
+        }
+        __syncthreads();
+      }
+    } else {
+      for (int q = min(nb - 1, c0 + kIC - 1); q >= 0; --q) {
+        if (r == q) {
+          const C d = cinv(F[(long long)q * m + q]);
+#pragma unroll
+          for (int j = 0; j < kIC; ++j) {
+            x[j] = cmul(x[j], d);
+            rowq[j] = x[j];
+          }
+        }
+        __syncthreads();
+        if (r < q) {
+          const C u = F[(long long)q * m + r];
+#pragma unroll
+          for (int j = 0; j < kIC; ++j) x[j] = cfms(x[j], u, rowq[j]);
+        }
+        __syncthreads();
+      }
+    }
+    if (r < nb)
+#pragma unroll
+      for (int j = 0; j < kIC; ++j)
+        if (c0 + j < nb) out[(long long)(c0 + j) * nb + r] = x[j];
+  }
+}
+
+// t[0:nb] <- Minv xs[0:nb] by one CTA of 256 threads (Minv column-major,
+// leading dim nb <= kSW; xs already in shared memory).
+template <class C>
+__device__ void apply_inverse_block(const C *__restrict__ Minv, C *t, int nb, const C *xs,
+                                    C (*red)[kSW]) {
+  const int r = threadIdx.x & (kSW - 1), half = threadIdx.x / kSW;
+  C v = czero<C>();
+  if (r < nb) {
+    const int q0 = half * (nb / 2), q1 = half ? nb : nb / 2;
+#pragma unroll 8
+    for (int q = q0; q < q1; ++q) v = cfma(v, Minv[(long long)q * nb + r], xs[q]);
+  }
+  red[half][r] = v;
+  __syncthreads();
+  if (threadIdx.x < nb) t[threadIdx.x] = cadd(red[0][threadIdx.x], red[1][threadIdx.x]);
+}
+
+// forward, first diagonal block of every front of the level
 template <class C>
 __global__ void __launch_bounds__(256)
-    k_fwd_step(const int *__restrict__ fl, int s, int w, const C *__restrict__ pool,
-               const DevFront *__restrict__ fr, C *__restrict__ work) {
-  constexpr int WM = MaxW<C>::v;
-  __shared__ C Ld[WM][WM + 1];
-  __shared__ C xs[WM];
-  const DevFront f = fr[fl[blockIdx.y]];
-  const int k0 = s * w, ww = min(w, f.p - k0);
-  const int r = k0 + ww + blockIdx.x * blockDim.x + threadIdx.x;
-  if (blockIdx.x > 0 && k0 + ww + (int)(blockIdx.x * blockDim.x) >= f.p) return;
-  const C *F = pool + f.off;
-  const int m = f.m;
+    k_fwd_first(const int *__restrict__ fl, const DevFront *__restrict__ fr,
+                const long long *__restrict__ inv_off, const C *__restrict__ Linv,
+                C *__restrict__ work) {
+  __shared__ C xs[kSW];
+  __shared__ C red[2][kSW];
+  const int fid = fl[blockIdx.x];
+  const DevFront f = fr[fid];
+  const int nb = min(kSW, f.p);
   C *t = work + f.toff;
-  for (int x = threadIdx.x; x < ww * ww; x += blockDim.x) {
-    const int rr = x % ww, cc = x / ww;
-    if (rr > cc) Ld[cc][rr] = F[(long long)(k0 + cc) * m + k0 + rr];
-  }
-  for (int c = threadIdx.x; c < ww; c += blockDim.x) xs[c] = t[k0 + c];
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) xs[q] = t[q];
   __syncthreads();
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    for (int q = 0; q < ww; ++q) {
-      const C xq = xs[q];
-      __syncwarp();
-      for (int rr = q + 1 + lane; rr < ww; rr += 32) xs[rr] = cfms(xs[rr], Ld[q][rr], xq);
-      __syncwarp();
+  apply_inverse_block(Linv + inv_off[fid], t, nb, xs, red);
+}
+
+// forward block step b of every front with p > (b+1) kSW: the pivot rows
+// below the block take t[r] -= L[r, b0:b1] y_b (CTA = 32 rows, 8 warps of
+// kSW/8 columns); the front's last CTA (atomic ticket) then forms
+// y_{b+1} = inv(L_{b+1}) t[b1:b2].
+template <class C>
+__global__ void __launch_bounds__(256)
+    k_fwd_blk(const int *__restrict__ fl, int b, const C *__restrict__ pool,
+              const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
+              const C *__restrict__ Linv, C *__restrict__ work, int *__restrict__ ticket) {
+  __shared__ C ys[kSW];
+  __shared__ C red8[8][32];
+  __shared__ C red[2][kSW];
+  __shared__ int last;
+  const int fid = fl[blockIdx.y];
+  const DevFront f = fr[fid];
+  const int b0 = b * kSW, b1 = min(f.p, b0 + kSW), nb = b1 - b0;
+  const int rows = f.p - b1;
+  if (rows <= 0) return;
+  const int nch = (rows + 31) / 32;
+  if ((int)blockIdx.x >= nch) return;
+  C *t = work + f.toff;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) ys[q] = t[b0 + q];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int r = b1 + blockIdx.x * 32 + lane;
+  const C *F = pool + f.off;
+  C acc = czero<C>();
+  if (r < f.p) {
+    const int q0 = wp * (kSW / 8), q1 = min(nb, q0 + kSW / 8);
+#pragma unroll 8
+    for (int q = q0; q < q1; ++q) acc = cfma(acc, F[(long long)(b0 + q) * f.m + r], ys[q]);
+  }
+  red8[wp][lane] = acc;
+  __syncthreads();
+  if (wp == 0 && r < f.p) {
+    C v = t[r];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v = csub(v, red8[k][lane]);
+    t[r] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket + blockIdx.y, 1) == nch - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x == 0) ticket[blockIdx.y] = 0;
+  const int n2 = min(kSW, f.p - b1);
+  for (int q = threadIdx.x; q < n2; q += blockDim.x) ys[q] = __ldcg(t + b1 + q);
+  __syncthreads();
+  apply_inverse_block(Linv + inv_off[fid] + (long long)(b + 1) * kSW * kSW, t + b1, n2, ys,
+                      red);
+}
+
+// backward block step b of every front with p > b kSW:
+// x_b = inv(U_b) (t[b0:b1] - U[b0:b1, b1:p] x[b1:p]).  CTAs reduce column
+// chunks of kBC into FP64 partials (2 halves x kSW rows per CTA); the
+// front's last CTA sums them and applies the inverse.
+constexpr int kBC = 64;
+
+template <class C>
+__global__ void __launch_bounds__(256)
+    k_bwd_blk(const int *__restrict__ fl, int b, const C *__restrict__ pool,
+              const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
+              const C *__restrict__ Uinv, C *__restrict__ work, double2 *__restrict__ partial,
+              int max_chunks, int *__restrict__ ticket) {
+  __shared__ C xs[kSW];
+  __shared__ C red[2][kSW];
+  __shared__ int last;
+  const int fid = fl[blockIdx.y];
+  const DevFront f = fr[fid];
+  const int b0 = b * kSW, b1 = min(f.p, b0 + kSW), nb = b1 - b0;
+  if (nb <= 0) return;
+  const int cols = f.p - b1;
+  const int nch = cols > 0 ? (cols + kBC - 1) / kBC : 1;
+  if ((int)blockIdx.x >= nch) return;
+  C *t = work + f.toff;
+  if (cols > 0) {
+    const C *F = pool + f.off;
+    const int r = threadIdx.x & (kSW - 1), half = threadIdx.x / kSW;
+    const int c0 = b1 + blockIdx.x * kBC + half * (kBC / 2), c1 = min(f.p, c0 + kBC / 2);
+    C acc = czero<C>();
+    if (r < nb) {
+#pragma unroll 8
+      for (int c = c0; c < c1; ++c) acc = cfma(acc, F[(long long)c * f.m + b0 + r], t[c]);
     }
+    red[half][r] = acc;
+    __syncthreads();
+    if (threadIdx.x < nb)
+      partial[((long long)blockIdx.y * max_chunks + blockIdx.x) * kSW + threadIdx.x] =
+          to64(cadd(red[0][threadIdx.x], red[1][threadIdx.x]));
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket + blockIdx.y, 1) == nch - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x == 0) ticket[blockIdx.y] = 0;
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+      double2 s = make_double2(0, 0);
+      for (int k = 0; k < nch; ++k) {
+        const double2 v = __ldcg(partial + ((long long)blockIdx.y * max_chunks + k) * kSW + q);
+        s.x += v.x;
+        s.y += v.y;
+      }
+      xs[q] = csub(t[b0 + q], from64<C>(s));
+    }
+  } else {
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) xs[q] = t[b0 + q];
   }
   __syncthreads();
-  if (blockIdx.x == 0)
-    for (int c = threadIdx.x; c < ww; c += blockDim.x) t[k0 + c] = xs[c];
-  if (r >= f.p) return;
-  C lv[WM];
-#pragma unroll
-  for (int c = 0; c < WM; ++c)
-    if (c < ww) lv[c] = F[(long long)(k0 + c) * m + r];
-  C v = t[r];
-#pragma unroll
-  for (int c = 0; c < WM; ++c)
-    if (c < ww) v = cfms(v, lv[c], xs[c]);
-  t[r] = v;
+  apply_inverse_block(Uinv + inv_off[fid] + (long long)b * kSW * kSW, t + b0, nb, xs, red);
 }
 
 // forward border coupling of one level, pass 1: partial[front][chunk][r] =
@@ -548,86 +762,6 @@ __global__ void k_bwd_border_reduce(const int *__restrict__ fl, const DevFront *
   }
   C *t = work + f.toff + i;
   *t = csub(*t, from64<C>(acc));
-}
-
-// backward step s, fused: CTAs reduce U[k0:k0+ww, chunk] t[chunk] into
-// per-chunk partials; the last CTA of the front (atomic ticket) sums them in
-// chunk order, solves the upper diagonal block and resets the ticket.
-template <class C>
-__global__ void __launch_bounds__(256)
-    k_bwd_step(const int *__restrict__ fl, int s, int w, int chunk,
-               const C *__restrict__ pool, const DevFront *__restrict__ fr,
-               C *__restrict__ work, double2 *__restrict__ partial, int max_chunks,
-               int *__restrict__ ticket) {
-  constexpr int WM = MaxW<C>::v;
-  __shared__ C red[8][64];
-  __shared__ C Ud[WM][WM + 1];
-  __shared__ C xs[WM];
-  __shared__ int last;
-  const DevFront f = fr[fl[blockIdx.y]];
-  const int k0 = s * w, ww = min(w, f.p - k0);
-  const int ext = f.p - k0 - ww;  // columns of the pivot block right of the panel
-  const int nch = ext > 0 ? (ext + chunk - 1) / chunk : 1;
-  if ((int)blockIdx.x >= nch) return;
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  const C *F = pool + f.off;
-  const int m = f.m;
-  C *t = work + f.toff;
-  if (ext > 0) {
-    // each warp owns chunk/8 consecutive columns; all its loads are
-    // independent, so they are issued back to back
-    const int cbeg = k0 + ww + blockIdx.x * chunk + wp * (chunk / 8);
-    const int cend = min(f.p, cbeg + chunk / 8);
-    C a0 = czero<C>(), a1 = czero<C>();
-#pragma unroll 4
-    for (int c = cbeg; c < cend; ++c) {
-      const C tc = t[c];
-      const C *colp = F + (long long)c * m + k0;
-      if (lane < ww) a0 = cfma(a0, colp[lane], tc);
-      if (lane + 32 < ww) a1 = cfma(a1, colp[lane + 32], tc);
-    }
-    red[wp][lane] = a0;
-    red[wp][lane + 32] = a1;
-    __syncthreads();
-    if (threadIdx.x < ww) {
-      C v = czero<C>();
-      for (int q = 0; q < 8; ++q) v = cadd(v, red[q][threadIdx.x]);
-      partial[((long long)blockIdx.y * max_chunks + blockIdx.x) * 64 + threadIdx.x] = to64(v);
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(ticket + blockIdx.y, 1) == nch - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-  }
-  for (int x = threadIdx.x; x < ww * ww; x += blockDim.x) {
-    const int rr = x % ww, cc = x / ww;
-    if (rr <= cc) Ud[cc][rr] = F[(long long)(k0 + cc) * m + k0 + rr];
-  }
-  if (threadIdx.x < ww) {
-    double2 acc = make_double2(0, 0);
-    if (ext > 0)
-      for (int q = 0; q < nch; ++q) {
-        const double2 pv = partial[((long long)blockIdx.y * max_chunks + q) * 64 + threadIdx.x];
-        acc.x += pv.x;
-        acc.y += pv.y;
-      }
-    xs[threadIdx.x] = csub(t[k0 + threadIdx.x], from64<C>(acc));
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    for (int q = ww - 1; q >= 0; --q) {
-      if (lane == 0) xs[q] = cmul(xs[q], cinv(Ud[q][q]));
-      __syncwarp();
-      const C xq = xs[q];
-      for (int rr = lane; rr < q; rr += 32) xs[rr] = cfms(xs[rr], Ud[q][rr], xq);
-      __syncwarp();
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < ww) t[k0 + threadIdx.x] = xs[threadIdx.x];
-  if (threadIdx.x == 0 && ext > 0) ticket[blockIdx.y] = 0;
 }
 
 // backward: t[p:m] = x at the border unknowns (already solved ancestors)
@@ -765,22 +899,34 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
     }
     L.nck_f = std::max(1, (L.pmax + 511) / 512);
     L.nck_b = std::max(1, (L.bmax + 511) / 512);
-    for (auto &st : L.steps) {
-      // per-step backward chunks cover only the pivot block right of the panel
-      int ext_p = 0;
-      for (int q = 0; q < st.nf; ++q) {
-        const FrontInfo &f = sym.fronts[sched[L.fronts_off + q]];
-        ext_p = std::max(ext_p, f.p - (int)(&st - L.steps.data()) * w - std::min(w, f.p - (int)(&st - L.steps.data()) * w));
-      }
-      st.max_ext_p = ext_p;
-      max_chunks = std::max(max_chunks, (ext_p + kChunk - 1) / kChunk);
+    L.blk_nf.clear();
+    for (int b = 0; b * kSW < L.pmax; ++b) {
+      int n = 0;
+      for (int q = 0; q < L.nfronts; ++q)
+        if (sym.fronts[sched[L.fronts_off + q]].p > b * kSW) ++n;
+      L.blk_nf.push_back(n);
     }
+    max_chunks = std::max(max_chunks, (std::max(L.pmax - kSW, 1) + kBC - 1) / kBC);
     partial_elems = std::max(partial_elems, (long long)L.nfronts * L.nck_f * std::max(L.bmax, 1));
     partial_elems = std::max(partial_elems, (long long)L.nfronts * L.nck_b * std::max(L.pmax, 1));
   }
   int max_lvl_fronts = 1;
   for (auto &L : levels) max_lvl_fronts = std::max(max_lvl_fronts, L.nfronts);
-  partial_elems = std::max(partial_elems, (long long)max_lvl_fronts * max_chunks * 64);
+  partial_elems = std::max(partial_elems, (long long)max_lvl_fronts * max_chunks * kSW);
+  // diagonal-block inverses: full blocks kSW x kSW, the last one nb x nb
+  std::vector<long long> inv_off(nf);
+  std::vector<int2> inv_blocks;
+  inv_elems = 0;
+  for (int t = 0; t < nf; ++t) {
+    const int p = sym.fronts[t].p;
+    inv_off[t] = inv_elems;
+    for (int b = 0; b * kSW < p; ++b) {
+      const int nb = std::min(kSW, p - b * kSW);
+      inv_blocks.push_back(make_int2(t, b));
+      inv_elems += (long long)nb * nb;
+    }
+  }
+  n_inv_blocks = (int)inv_blocks.size();
   const size_t csize = prec == 0 ? sizeof(double2) : sizeof(float2);
   auto alloc = [&](void **p, size_t bytes) -> int {
     cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
@@ -804,8 +950,16 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
       (rc = alloc((void **)&d_partial, (size_t)partial_elems * sizeof(double2))) ||
       (rc = alloc((void **)&d_pert, sizeof(int))) ||
       (rc = alloc((void **)&d_ticket, max_lvl_fronts * sizeof(int))) ||
+      (rc = alloc(&linv, (size_t)inv_elems * csize)) ||
+      (rc = alloc(&uinv, (size_t)inv_elems * csize)) ||
+      (rc = alloc((void **)&d_inv_off, nf * sizeof(long long))) ||
+      (rc = alloc((void **)&d_inv_blocks, inv_blocks.size() * sizeof(int2))) ||
       (rc = alloc(&vec_a, (size_t)ctx->nn * 5 * csize)))
     return rc;
+  TLR_CUDA(ctx, cudaMemcpy(d_inv_off, inv_off.data(), nf * sizeof(long long),
+                           cudaMemcpyHostToDevice));
+  TLR_CUDA(ctx, cudaMemcpy(d_inv_blocks, inv_blocks.data(), inv_blocks.size() * sizeof(int2),
+                           cudaMemcpyHostToDevice));
   TLR_CUDA(ctx, cudaMemset(d_ticket, 0, max_lvl_fronts * sizeof(int)));
   TLR_CUDA(ctx, cudaMemcpy(d_fronts, df.data(), nf * sizeof(DevFront), cudaMemcpyHostToDevice));
   TLR_CUDA(ctx, cudaMemcpy(d_entries, sym.entries.data(), sym.entries.size() * sizeof(AsmEntry),
@@ -823,7 +977,11 @@ void Factor::release() {
   cudaFree(pool); cudaFree(work); cudaFree(d_fronts); cudaFree(d_entries);
   cudaFree(d_cmap); cudaFree(d_nodes); cudaFree(d_ipiv); cudaFree(d_perm);
   cudaFree(d_pmap); cudaFree(d_sched); cudaFree(d_partial); cudaFree(d_pert);
-  cudaFree(vec_a); cudaFree(d_ticket);
+  cudaFree(vec_a); cudaFree(d_ticket); cudaFree(linv); cudaFree(uinv);
+  cudaFree(d_inv_off); cudaFree(d_inv_blocks);
+  linv = uinv = nullptr;
+  d_inv_off = nullptr;
+  d_inv_blocks = nullptr;
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   graph_exec = nullptr;
   pool = work = vec_a = nullptr;
@@ -857,7 +1015,7 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
     const int *fl = d_sched + L.fronts_off;
     for (int s = 0; s < (int)L.steps.size(); ++s) {
       const Step &S = L.steps[s];
-      k_panel<C><<<S.nf, 256, 0, st>>>(fl, s, w, P, d_fronts, d_ipiv, d_pert, tiny);
+      k_panel<C><<<S.nf, 512, 0, st>>>(fl, s, w, P, d_fronts, d_ipiv, d_pert, tiny);
       k_swap<C><<<dim3(blocks_for(S.max_m, 128), S.nf), 128, 0, st>>>(fl, s, w, P, d_fronts,
                                                                        d_ipiv);
       if (S.max_b > 0)
@@ -877,6 +1035,10 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
       }
     }
   }
+  if (n_inv_blocks > 0)
+    k_tri_inv<C><<<dim3(n_inv_blocks, 2), kSW, 0, st>>>(d_inv_blocks, P, d_fronts, d_inv_off,
+                                                       static_cast<C *>(linv),
+                                                       static_cast<C *>(uinv));
   TLR_CUDA(ctx, cudaGetLastError());
   return TLR_OK;
 }
@@ -936,10 +1098,13 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
       if (L.kids[slot])
         k_saddchild<C><<<dim3(blocks_for(std::max(L.kids_maxb[slot], 1), 128), L.kids[slot]),
                          128, 0, st>>>(d_sched + L.kids_off[slot], d_fronts, d_pmap, W);
-    for (int s = 0; s < (int)L.steps.size(); ++s) {
-      const Step &S = L.steps[s];
-      k_fwd_step<C><<<dim3(std::max(blocks_for(S.max_ext_p, 64), 1), S.nf), 64, 0, st>>>(
-          fl, s, w, P, d_fronts, W);
+    const C *Li = static_cast<const C *>(linv);
+    const C *Ui = static_cast<const C *>(uinv);
+    k_fwd_first<C><<<L.nfronts, 256, 0, st>>>(fl, d_fronts, d_inv_off, Li, W);
+    for (int b = 0; b + 1 < (int)L.blk_nf.size(); ++b) {
+      const int rows = L.pmax - (b + 1) * kSW;
+      k_fwd_blk<C><<<dim3(blocks_for(rows, 32), L.blk_nf[b + 1]), 256, 0, st>>>(
+          fl, b, P, d_fronts, d_inv_off, Li, W, d_ticket);
     }
     if (L.bmax > 0) {
       k_fwd_border<C><<<dim3(blocks_for(L.bmax, 128), L.nck_f, L.nfronts), 128, 0, st>>>(
@@ -959,11 +1124,11 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
       k_bwd_border_reduce<C><<<dim3(blocks_for(L.pmax, 128), L.nfronts), 128, 0, st>>>(
           fl, d_fronts, W, d_partial, L.nck_b, L.pmax);
     }
-    for (int s = (int)L.steps.size() - 1; s >= 0; --s) {
-      const Step &S = L.steps[s];
-      const int nch = S.max_ext_p > 0 ? (S.max_ext_p + kChunk - 1) / kChunk : 1;
-      k_bwd_step<C><<<dim3(nch, S.nf), 256, 0, st>>>(fl, s, w, kChunk, P, d_fronts, W,
-                                                     d_partial, max_chunks, d_ticket);
+    for (int b = (int)L.blk_nf.size() - 1; b >= 0; --b) {
+      const int cols = L.pmax - (b + 1) * kSW;
+      k_bwd_blk<C><<<dim3(std::max(blocks_for(std::max(cols, 0), kBC), 1), L.blk_nf[b]), 256, 0,
+                     st>>>(fl, b, P, d_fronts, d_inv_off, static_cast<const C *>(uinv), W,
+                           d_partial, max_chunks, d_ticket);
     }
     k_bscatter<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(fl, d_fronts,
                                                                               d_nodes, W, x);

@@ -13,11 +13,10 @@ struct DevFront {
   int p, m, parent, node_off;
 };
 
-constexpr int kChunk = 64;    // columns per CTA in the backward step GEMV (8 per warp)
+constexpr int kSW = 128;  // rows of a diagonal block of the solves (explicit inverses)
 
 struct Step {  // one panel step of one level
   int nf, max_m, max_b, max_ext, prefix_off, tiles;
-  int max_ext_p = 0;  // pivot-block columns right of the panel
 };
 
 struct Level {
@@ -26,6 +25,7 @@ struct Level {
   int kids[2] = {0, 0}, kids_off[2] = {0, 0}, kids_maxb[2] = {0, 0};
   long long entry_begin = 0, entry_end = 0, pool_begin = 0, pool_end = 0;
   std::vector<Step> steps;
+  std::vector<int> blk_nf;  // blk_nf[b]: fronts of the level with p > b kSW
 };
 
 struct Factor {
@@ -39,6 +39,12 @@ struct Factor {
   AsmEntry *d_entries = nullptr;
   int *d_cmap = nullptr, *d_nodes = nullptr, *d_ipiv = nullptr, *d_perm = nullptr;
   int *d_pmap = nullptr, *d_sched = nullptr, *d_pert = nullptr, *d_ticket = nullptr;
+  // explicit inverses of the kSW x kSW diagonal blocks of every pivot block
+  void *linv = nullptr, *uinv = nullptr;
+  long long *d_inv_off = nullptr;
+  int2 *d_inv_blocks = nullptr;
+  int n_inv_blocks = 0;
+  long long inv_elems = 0;
   cudaGraphExec_t graph_exec = nullptr;  // captured solve, replayed per call
   double2 *d_partial = nullptr;
   int perturbed = 0;
