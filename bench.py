@@ -203,6 +203,7 @@ def main():
     clocks = ClockSampler()
     clocks.start()
     barrier()
+    launches0 = prob.lib.tlr_kernel_launches()
     ev.record(ev.a, stream)
     good_total, sols = 0, []
     for _ in range(args.steps):
@@ -211,6 +212,7 @@ def main():
         sols.append(sol)
     ev.record(ev.b, stream)
     ms = ev.elapsed_ms()
+    launches = prob.lib.tlr_kernel_launches() - launches0
     barrier()
     clk = clocks.stop()
     if dist:
@@ -257,8 +259,18 @@ def main():
                "sample": "one 60x32 eigen solve (C2 physics, nev 16): C oracle assembly, "
                          "zggev boundary rows, SuperLU+ARPACK, %.1f s" % times[0]}
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-    bf16 = peaks.get("bf16_tflops", 1900.0)
-    ftf = last["factor_flops"] / (last["factor_ms"] * 1e-3) / 1e12 if last["factor_ms"] > 0 else 0.0
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    # dominant kernel: the triangular solves (one CUDA graph per K^-1
+    # application), timed live with CUDA events around every graph replay.
+    csize = 8 if args.precision == 1 else 16
+    tri_bytes = last["factor_bytes"] + 2 * 5 * case.nodes * csize
+    tri_avg_ms = last["trisolve_ms"] / max(last["trisolves"], 1)
+    achieved = tri_bytes / (tri_avg_ms * 1e-3) / 1e9 if tri_avg_ms > 0 else 0.0
+    traffic = None
+    tf = ROOT / "profiles" / "trisolve_traffic.json"
+    if tf.exists():
+        t = json.loads(tf.read_text()).get("c64" if args.precision == 1 else "c128", {})
+        traffic = t.get("bytes_per_solve_c2")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -272,14 +284,20 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": gbytes + bbytes,
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": None,
+        "gpu_launches": launches,
         "clocks": clk,
-        "roofline": {"bound": "tensor", "achieved": ftf, "peak": bf16, "unit": "TFLOP/s",
-                     "frac": ftf / bf16, "traffic": None,
-                     "kernel": "multifrontal factorisation (k_gemm dominant)",
-                     "note": "CUDA-core FP32/FP64 complex GEMM; peak is the measured bf16 tensor rate"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "kernel": "triangular solves (solve graph: k_blk_update, k_border_gemv, "
+                               "k_bwd_start, gathers)",
+                     "algorithmic_bytes": tri_bytes, "avg_ms": tri_avg_ms,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        "factor": {"flops": last["factor_flops"], "ms": last["factor_ms"],
+                   "tflops": last["factor_flops"] / (last["factor_ms"] * 1e-3) / 1e12
+                   if last["factor_ms"] > 0 else 0.0},
         "solve": {k: last[k] for k in ("iterations", "solves", "refinement_steps", "factor_ms",
-                                       "krylov_ms", "total_ms", "max_relative_error")},
+                                       "krylov_ms", "total_ms", "max_relative_error",
+                                       "trisolve_ms", "trisolves")},
         "cpu_baseline": cpu,
         "plain_fp64": plain,
     }

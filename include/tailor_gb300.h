@@ -203,6 +203,9 @@ typedef struct {
   double factor_flops;    /* algorithmic complex-counted flops of the LU    */
   double solve_ms;        /* time inside K^-1 applications (incl. refinement) */
   double factor_bytes;    /* bytes of the stored L and U factors            */
+  double trisolve_ms;     /* device time of the triangular solves (CUDA
+                             events around each solve graph)               */
+  int trisolves;          /* triangular solves timed in trisolve_ms         */
 } tlr_eig_diag;
 
 /* lambda [nev] complex, residual [nev]; modes [nev][5N] complex or NULL. */
@@ -248,6 +251,12 @@ int tlr_frobenius_noalloc(const double *values, size_t count, double *result,
 /* The context's CUDA stream (cudaStream_t) -- all device work of the
  * context is ordered on it; callers time or synchronise against it. */
 void *tlr_stream(tlr_ctx *ctx);
+
+/* Kernels of this library launched by the process so far (every kernel
+ * node of a replayed CUDA graph counts once per replay; cuBLAS kernels are
+ * not counted).  No counterpart in the reference: it lets a caller check
+ * which device work a region ran. */
+long long tlr_kernel_launches(void);
 
 const char *tlr_status_string(int status);
 const char *tlr_last_error(const tlr_ctx *ctx);

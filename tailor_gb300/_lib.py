@@ -86,7 +86,8 @@ class EigDiag(ctypes.Structure):
                 ("refinement_steps", ctypes.c_int),
                 ("factor_ms", ctypes.c_double), ("krylov_ms", ctypes.c_double),
                 ("total_ms", ctypes.c_double), ("factor_flops", ctypes.c_double),
-                ("solve_ms", ctypes.c_double), ("factor_bytes", ctypes.c_double)]
+                ("solve_ms", ctypes.c_double), ("factor_bytes", ctypes.c_double),
+                ("trisolve_ms", ctypes.c_double), ("trisolves", ctypes.c_int)]
 
 
 # Exported symbols and their signatures (argtypes, restype).
@@ -110,6 +111,7 @@ SIGNATURES = {
     "tlr_transform_points": ([_I, _P, _P, _P, _P, _P, _P], _I),
     "tlr_solve": ([_P, _P, _P, _P, _P, _P], _I),
     "tlr_stream": ([_P], ctypes.c_void_p),
+    "tlr_kernel_launches": ([], ctypes.c_longlong),
     "tlr_frobenius_noalloc": ([_P, ctypes.c_size_t, _P, _P], _I),
     "tlr_mlp_create": ([_I, _I, _I, _I, ctypes.c_ulonglong, _P], _I),
     "tlr_mlp_destroy": ([_P], None),

@@ -414,8 +414,8 @@ int launch_writer_t(tlr_ctx *ctx) {
                                                               kWriterThreads, smem));
   const int groups = (ctx->nn + kSub - 1) / kSub;
   const int grid = std::max(1, std::min(groups, sms * std::max(per_sm, 1)));
-  k_write_rows_t<SX, SE><<<grid, kWriterThreads, smem, ctx->stream>>>(
-      ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->coef, ctx->L, ctx->M);
+  { k_write_rows_t<SX, SE><<<grid, kWriterThreads, smem, ctx->stream>>>(
+      ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->coef, ctx->L, ctx->M); count_launches(); }
   TLR_CUDA(ctx, cudaGetLastError());
   return TLR_OK;
 }
@@ -434,8 +434,8 @@ int launch_writer(tlr_ctx *ctx) {
 int run_pattern(tlr_ctx *ctx) {
   const long long total = (long long)ctx->nn * ctx->S;
   const long long threads = total > ctx->nn + 1 ? total : ctx->nn + 1;
-  k_pattern<<<blocks_for(threads, 256), 256, 0, ctx->stream>>>(
-      ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->row_ptr, ctx->col);
+  { k_pattern<<<blocks_for(threads, 256), 256, 0, ctx->stream>>>(
+      ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->row_ptr, ctx->col); count_launches(); }
   TLR_CUDA(ctx, cudaGetLastError());
   return TLR_OK;
 }
@@ -459,8 +459,8 @@ int run_assemble(tlr_ctx *ctx, tlr_operator_diag *diag) {
   p.a2_im = ar * ai + ai * ar;
   p.alpha_finite = std::isfinite(ar) && std::isfinite(ai);
   TLR_CUDA(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int) * ST_COUNT, ctx->stream));
-  k_coefficients<<<blocks_for(ctx->nn, 128), 128, 0, ctx->stream>>>(
-      p, ctx->base_c, ctx->derivs, ctx->metrics, ctx->coef, ctx->status);
+  { k_coefficients<<<blocks_for(ctx->nn, 128), 128, 0, ctx->stream>>>(
+      p, ctx->base_c, ctx->derivs, ctx->metrics, ctx->coef, ctx->status); count_launches(); }
   TLR_CUDA(ctx, cudaGetLastError());
   int st[ST_COUNT];
   TLR_CUDA(ctx, cudaMemcpyAsync(st, ctx->status, sizeof(st), cudaMemcpyDeviceToHost,
@@ -488,8 +488,8 @@ int run_assemble(tlr_ctx *ctx, tlr_operator_diag *diag) {
   const int wr = launch_writer(ctx);
   if (wr > 0) return wr;
   if (wr < 0) {
-    k_write_rows<<<grid, kWriterThreads, smem, ctx->stream>>>(
-        ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->coef, ctx->L, ctx->M);
+    { k_write_rows<<<grid, kWriterThreads, smem, ctx->stream>>>(
+        ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->coef, ctx->L, ctx->M); count_launches(); }
     TLR_CUDA(ctx, cudaGetLastError());
   }
   TLR_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
@@ -524,8 +524,8 @@ int time_writer(tlr_ctx *ctx, float *ms) {
   const int groups = (ctx->nn + kSub - 1) / kSub;
   const int grid = std::max(1, std::min(groups, sms * std::max(per_sm, 1)));
   TLR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-  k_write_rows<<<grid, kWriterThreads, smem, ctx->stream>>>(
-      ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->coef, ctx->L, ctx->M);
+  { k_write_rows<<<grid, kWriterThreads, smem, ctx->stream>>>(
+      ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->coef, ctx->L, ctx->M); count_launches(); }
   TLR_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
   TLR_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
   cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1);

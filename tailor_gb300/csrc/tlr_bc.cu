@@ -254,17 +254,17 @@ __global__ void k_farfield(int ny, int nz, int S, double M, double gamma,
 int run_bc(tlr_ctx *ctx, tlr_bc_diag *diag) {
   const long long nA = ctx->nnzb * 25, nB = (long long)ctx->nn * 25;
   TLR_CUDA(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int) * ST_COUNT, ctx->stream));
-  k_negate_copy<<<std::min<long long>(blocks_for(nA, 256), 152 * 16), 256, 0,
-                  ctx->stream>>>(nA, ctx->L, ctx->A);
+  { k_negate_copy<<<std::min<long long>(blocks_for(nA, 256), 152 * 16), 256, 0,
+                  ctx->stream>>>(nA, ctx->L, ctx->A); count_launches(); }
   TLR_CUDA(ctx, cudaMemcpyAsync(ctx->B, ctx->M, sizeof(double2) * nB,
                                 cudaMemcpyDeviceToDevice, ctx->stream));
   const long long wall = (long long)ctx->nz * ctx->S * 20;
-  k_wall<<<blocks_for(wall, 256), 256, 0, ctx->stream>>>(ctx->ny, ctx->nz, ctx->S,
-                                                         ctx->col, ctx->A, ctx->B);
-  k_farfield<<<ctx->nz, 64, 0, ctx->stream>>>(
+  { k_wall<<<blocks_for(wall, 256), 256, 0, ctx->stream>>>(ctx->ny, ctx->nz, ctx->S,
+                                                         ctx->col, ctx->A, ctx->B); count_launches(); }
+  { k_farfield<<<ctx->nz, 64, 0, ctx->stream>>>(
       ctx->ny, ctx->nz, ctx->S, ctx->recipe.mach, ctx->recipe.gamma, ctx->base,
       ctx->metrics, ctx->col, ctx->A, ctx->B, ctx->bc_modes, ctx->bc_cond,
-      ctx->status);
+      ctx->status); count_launches(); }
   TLR_CUDA(ctx, cudaGetLastError());
   int st[ST_COUNT];
   std::vector<int> modes(ctx->nz * 2);

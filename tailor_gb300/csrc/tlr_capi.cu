@@ -156,6 +156,8 @@ const char *tlr_status_string(int status) {
 
 void *tlr_stream(tlr_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
+long long tlr_kernel_launches(void) { return tlr::launch_total(); }
+
 const char *tlr_last_error(const tlr_ctx *ctx) {
   return ctx ? ctx->last_error.c_str() : g_error.c_str();
 }

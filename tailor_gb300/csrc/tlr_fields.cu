@@ -287,10 +287,10 @@ __global__ void k_sq_final(int nblocks, int ncomp, const double *partial,
 
 int norms(tlr_ctx *ctx, const double *planes, int ncomp, double *host_out) {
   const int blocks = ctx->partial_blocks;
-  k_sq_partial<<<blocks, 256, 0, ctx->stream>>>(ctx->nn, ncomp, planes,
-                                                ctx->partial);
-  k_sq_final<<<1, 32, 0, ctx->stream>>>(blocks, ncomp, ctx->partial,
-                                        ctx->partial + blocks * 32);
+  { k_sq_partial<<<blocks, 256, 0, ctx->stream>>>(ctx->nn, ncomp, planes,
+                                                ctx->partial); count_launches(); }
+  { k_sq_final<<<1, 32, 0, ctx->stream>>>(blocks, ncomp, ctx->partial,
+                                        ctx->partial + blocks * 32); count_launches(); }
   TLR_CUDA(ctx, cudaMemcpyAsync(host_out, ctx->partial + blocks * 32,
                                 sizeof(double) * ncomp, cudaMemcpyDeviceToHost,
                                 ctx->stream));
@@ -324,9 +324,9 @@ int run_metrics(tlr_ctx *ctx, tlr_metric_diag *diag) {
   if (rc) return rc;
   TLR_CUDA(ctx, cudaMemsetAsync(ctx->metrics, 0, sizeof(double) * 10 * nn,
                                 ctx->stream));
-  k_metrics_first<<<blocks_for(nn, 128), 128, 0, ctx->stream>>>(
+  { k_metrics_first<<<blocks_for(nn, 128), 128, 0, ctx->stream>>>(
       ctx->ny, ctx->nz, ctx->span, ctx->xi, ctx->eta, ctx->grid_c,
-      ctx->metrics, ctx->status, ctx->red);
+      ctx->metrics, ctx->status, ctx->red); count_launches(); }
   int st[ST_COUNT];
   double red[RD_COUNT];
   if ((rc = read_status(ctx, st, red))) return rc;
@@ -355,8 +355,8 @@ int run_metrics(tlr_ctx *ctx, tlr_metric_diag *diag) {
              "is %.16g", d.max_grid_imaginary);
     return fail(ctx, TLR_ERR_COMPLEX, buf);
   }
-  k_metrics_second<<<blocks_for(nn, 128), 128, 0, ctx->stream>>>(
-      ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->metrics, ctx->status);
+  { k_metrics_second<<<blocks_for(nn, 128), 128, 0, ctx->stream>>>(
+      ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->metrics, ctx->status); count_launches(); }
   if ((rc = read_status(ctx, st, red))) return rc;
   if (st[ST_SECOND])
     return fail(ctx, TLR_ERR_NONFINITE,
@@ -372,11 +372,11 @@ int run_derivatives(tlr_ctx *ctx, tlr_deriv_diag *diag) {
   if (rc) return rc;
   TLR_CUDA(ctx, cudaMemsetAsync(ctx->derivs, 0, sizeof(double) * 25 * nn,
                                 ctx->stream));
-  k_baseflow_prep<<<blocks_for(nn, 128), 128, 0, ctx->stream>>>(
-      nn, ctx->base_c, ctx->base, ctx->status, ctx->red);
-  k_derivatives<<<blocks_for(nn, 128), 128, 0, ctx->stream>>>(
+  { k_baseflow_prep<<<blocks_for(nn, 128), 128, 0, ctx->stream>>>(
+      nn, ctx->base_c, ctx->base, ctx->status, ctx->red); count_launches(); }
+  { k_derivatives<<<blocks_for(nn, 128), 128, 0, ctx->stream>>>(
       ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->base, ctx->metrics,
-      ctx->derivs, ctx->status);
+      ctx->derivs, ctx->status); count_launches(); }
   int st[ST_COUNT];
   double red[RD_COUNT];
   if ((rc = read_status(ctx, st, red))) return rc;

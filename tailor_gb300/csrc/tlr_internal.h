@@ -135,6 +135,16 @@ void free_factor(tlr_ctx *ctx);
 // Keep the symbolic analysis and device buffers, drop the numeric factor.
 void invalidate_factor(tlr_ctx *ctx);
 
+// Count of this library's kernel launches (tlr_kernel_launches).  Launches
+// recorded while a stream is captured are not counted; a replayed graph
+// adds its kernel nodes.
+void count_launches(long long n = 1);
+long long launch_total();
+struct CaptureScope {  // suppresses counting on this thread during capture
+  CaptureScope();
+  ~CaptureScope();
+};
+
 inline int blocks_for(long long n, int threads) {
   return static_cast<int>((n + threads - 1) / threads);
 }

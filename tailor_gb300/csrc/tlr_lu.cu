@@ -448,13 +448,20 @@ __global__ void k_saddchild(const int *__restrict__ kids, const DevFront *__rest
   d = cadd(d, work[fc.toff + fc.p + x]);
 }
 
-// ---- block-inverse triangular solves ------------------------------------
-// After factorisation every front's pivot block is cut into diagonal
-// blocks of kSW rows; their explicit inverses inv(L_bb) (unit lower) and
-// inv(U_bb) are stored, so a solve step is a parallel GEMV instead of a
-// serial substitution.  One launch per block step: CTAs update their row
-// (forward) or column (backward) chunk, and the last CTA of the front
-// (atomic ticket, no waiting) applies the next block's inverse.
+// ---- block-scaled triangular solves ---------------------------------------
+// After factorisation each front's pivot block is cut into diagonal blocks
+// of kSW rows.  With Dl = blockdiag(L_bb) and Du = blockdiag(U_bb), the
+// factors are rewritten in place as L' = L Dl^-1 (every block column right-
+// multiplied by inv(L_bb), border rows included) and U' = Du^-1 U (every
+// block row left-multiplied by inv(U_bb), border columns included), and
+// D_b = inv(U_bb) inv(L_bb) is stored.  L' and U' have identity diagonal
+// blocks, so
+//   forward:  z_b = t_b, then t_r -= L'(r, b) z_b for the rows below;
+//   backward: t = D z - U'12 x_border, then for b from the last block
+//             x_b = t_b and t_r -= U'(r, b) x_b for the rows above.
+// Every solve step is one fully parallel launch (rows split over CTAs, no
+// reductions across CTAs, no serial part); only the border product of the
+// backward pass reduces across column chunks.
 
 // inverses of diagonal block fb.y of front fb.x: blockIdx.y = 0 gives
 // inv(L_bb) (unit lower), 1 gives inv(U_bb).  Thread r owns row r of the
@@ -519,249 +526,219 @@ __global__ void __launch_bounds__(kSW)
   }
 }
 
-// t[0:nb] <- Minv xs[0:nb] by one CTA of 256 threads (Minv column-major,
-// leading dim nb <= kSW; xs already in shared memory).
+// L'(rows, c) = L(rows, c) inv(L_cc) in place: CTA = 32 rows of block
+// column c (all nb columns, staged in shared memory before any write);
+// thread (row, g) forms columns g, g+8, ... of its row.
+// tiles: {front, block c, first row, -}.
+constexpr int kRT = 32;
+
 template <class C>
-__device__ void apply_inverse_block(const C *__restrict__ Minv, C *t, int nb, const C *xs,
-                                    C (*red)[kSW]) {
+__global__ void __launch_bounds__(256)
+    k_scale_l(const int4 *__restrict__ tiles, C *__restrict__ pool,
+              const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
+              const C *__restrict__ Linv) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *As = reinterpret_cast<C *>(smem_raw);  // [kSW][kRT], As[q * kRT + r]
+  const int4 tl = tiles[blockIdx.x];
+  const DevFront f = fr[tl.x];
+  const int c0 = tl.y * kSW, nb = min(kSW, f.p - c0);
+  const int r0 = tl.z, nr = min(kRT, f.m - r0);
+  C *F = pool + f.off;
+  for (int x = threadIdx.x; x < nb * kRT; x += blockDim.x) {
+    const int q = x / kRT, r = x % kRT;
+    As[x] = r < nr ? F[(long long)(c0 + q) * f.m + r0 + r] : czero<C>();
+  }
+  __syncthreads();
+  const C *Li = Linv + inv_off[tl.x] + (long long)tl.y * kSW * kSW;  // (q, j) at j nb + q
+  const int r = threadIdx.x & (kRT - 1), g = threadIdx.x / kRT;
+  C acc[kSW / 8];
+#pragma unroll
+  for (int k = 0; k < kSW / 8; ++k) acc[k] = czero<C>();
+  for (int q = 0; q < nb; ++q) {
+    const C a = As[q * kRT + r];
+#pragma unroll
+    for (int k = 0; k < kSW / 8; ++k) {
+      const int j = g + 8 * k;
+      if (j <= q) acc[k] = cfma(acc[k], a, Li[(long long)j * nb + q]);
+    }
+  }
+  if (r < nr)
+#pragma unroll
+    for (int k = 0; k < kSW / 8; ++k) {
+      const int j = g + 8 * k;
+      if (j < nb) F[(long long)(c0 + j) * f.m + r0 + r] = acc[k];
+    }
+}
+
+// Left product by inv(U_bb), in place over a tile of 32 columns (staged in
+// shared memory before any write); thread (row i, half h) forms columns
+// h, h+2, ... of row i.  tiles: {front, block b, first column, kind}:
+//   kind 0: U'(b rows, cols) = inv(U_bb) U(b rows, cols) inside the front;
+//   kind 1: D_b(:, cols) = inv(U_bb) inv(L_bb)(:, cols) into dmat.
+template <class C>
+__global__ void __launch_bounds__(256)
+    k_scale_u(const int4 *__restrict__ tiles, C *__restrict__ pool,
+              const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
+              const C *__restrict__ Linv, const C *__restrict__ Uinv, C *__restrict__ dmat) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *As = reinterpret_cast<C *>(smem_raw);  // [kSW][kRT], As[q * kRT + cc]
+  const int4 tl = tiles[blockIdx.x];
+  const DevFront f = fr[tl.x];
+  const int b0 = tl.y * kSW, nb = min(kSW, f.p - b0);
+  const long long io = inv_off[tl.x] + (long long)tl.y * kSW * kSW;
+  const C *src;
+  C *dst;
+  long long ld, ncol;
+  if (tl.w == 0) {
+    dst = pool + f.off + b0;
+    src = dst;
+    ld = f.m;
+    ncol = f.m;
+  } else {
+    src = Linv + io;
+    dst = dmat + io;
+    ld = nb;
+    ncol = nb;
+  }
+  const int col0 = tl.z, nc = (int)min((long long)kRT, ncol - col0);
+  for (int x = threadIdx.x; x < nb * kRT; x += blockDim.x) {
+    const int cc = x / nb, q = x % nb;
+    As[q * kRT + cc] = cc < nc ? src[(long long)(col0 + cc) * ld + q] : czero<C>();
+  }
+  __syncthreads();
+  const C *Ui = Uinv + io;  // (i, q) at q nb + i, upper triangular
+  const int i = threadIdx.x & (kSW - 1), h = threadIdx.x / kSW;
+  C acc[kRT / 2];
+#pragma unroll
+  for (int k = 0; k < kRT / 2; ++k) acc[k] = czero<C>();
+  if (i < nb) {
+    for (int q = i & ~31; q < nb; ++q) {
+      const C u = q >= i ? Ui[(long long)q * nb + i] : czero<C>();
+#pragma unroll
+      for (int k = 0; k < kRT / 2; ++k) acc[k] = cfma(acc[k], u, As[q * kRT + h + 2 * k]);
+    }
+#pragma unroll
+    for (int k = 0; k < kRT / 2; ++k) {
+      const int cc = h + 2 * k;
+      if (cc < nc) dst[(long long)(col0 + cc) * ld + i] = acc[k];
+    }
+  }
+}
+
+// One solve step of every front of the level that owns block b: rows
+// [lo, hi) take t[r] -= F(r, b0:b1) t[b0:b1] (forward: lo = b1, hi = m;
+// backward: lo = 0, hi = b0).  CTA = 32 rows x 8 warps of kSW/8 columns.
+template <class C>
+__global__ void __launch_bounds__(256)
+    k_blk_update(const int *__restrict__ fl, int b, int backward, const C *__restrict__ pool,
+                 const DevFront *__restrict__ fr, C *__restrict__ work) {
+  __shared__ C vs[kSW];
+  __shared__ C red[8][32];
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int b0 = b * kSW, b1 = min(f.p, b0 + kSW), nb = b1 - b0;
+  const int lo = backward ? 0 : b1, hi = backward ? b0 : f.m;
+  const int r0 = lo + blockIdx.x * 32;
+  if (nb <= 0 || r0 >= hi) return;
+  C *t = work + f.toff;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int r = r0 + lane;
+  const C *F = pool + f.off + (long long)b0 * f.m;
+  // the matrix loads go out before the vector is staged (independent)
+  constexpr int kQ = kSW / 8;
+  const int q0 = wp * kQ;
+  C fv[kQ];
+#pragma unroll
+  for (int k = 0; k < kQ; ++k)
+    fv[k] = (r < hi && q0 + k < nb) ? F[(long long)(q0 + k) * f.m + r] : czero<C>();
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) vs[q] = t[b0 + q];
+  __syncthreads();
+  C acc = czero<C>();
+#pragma unroll
+  for (int k = 0; k < kQ; ++k)
+    if (q0 + k < nb) acc = cfma(acc, fv[k], vs[q0 + k]);
+  red[wp][lane] = acc;
+  __syncthreads();
+  if (wp == 0 && r < hi) {
+    C v = t[r];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v = csub(v, red[k][lane]);
+    t[r] = v;
+  }
+}
+
+// Backward border product, pass 1: partial[front][chunk][i] = sum over a
+// kBC-column chunk of the border of U'(i, c) t[c], pivot rows i.  CTA = 32
+// rows x 8 warps of kBC/8 columns.
+constexpr int kBC = 256;
+
+template <class C>
+__global__ void __launch_bounds__(256)
+    k_border_gemv(const int *__restrict__ fl, const C *__restrict__ pool,
+                  const DevFront *__restrict__ fr, const C *__restrict__ work,
+                  double2 *__restrict__ partial, int nck, int pmax) {
+  __shared__ C red[8][32];
+  const int fq = blockIdx.z;
+  const DevFront f = fr[fl[fq]];
+  const int r0 = blockIdx.x * 32;
+  const int c0 = f.p + blockIdx.y * kBC;
+  if (r0 >= f.p) return;
+  const C *t = work + f.toff;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int r = r0 + lane;
+  C acc = czero<C>();
+  if (r < f.p) {
+    const int ca = c0 + wp * (kBC / 8), cb = min(f.m, ca + kBC / 8);
+#pragma unroll 8
+    for (int c = ca; c < cb; ++c) acc = cfma(acc, pool[f.off + (long long)c * f.m + r], t[c]);
+  }
+  red[wp][lane] = acc;
+  __syncthreads();
+  if (wp == 0 && r < f.p) {
+    C v = czero<C>();
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v = cadd(v, red[k][lane]);
+    partial[((long long)fq * nck + blockIdx.y) * pmax + r] = to64(v);
+  }
+}
+
+// Start of a front's backward pass, block b: t_b = D_b z_b minus the
+// border chunks of pass 1 (summed in chunk order).  256 threads = 2 halves
+// of the q range for each of kSW rows.
+template <class C>
+__global__ void __launch_bounds__(256)
+    k_bwd_start(const int *__restrict__ fl, const DevFront *__restrict__ fr,
+                const long long *__restrict__ inv_off, const C *__restrict__ dmat,
+                C *__restrict__ work, const double2 *__restrict__ partial, int nck, int pmax) {
+  __shared__ C zs[kSW];
+  __shared__ C red[2][kSW];
+  const int fq = blockIdx.y, fid = fl[fq];
+  const DevFront f = fr[fid];
+  const int b0 = blockIdx.x * kSW, nb = min(kSW, f.p - b0);
+  if (nb <= 0) return;
+  C *t = work + f.toff + b0;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) zs[q] = t[q];
+  __syncthreads();
+  const C *Dm = dmat + inv_off[fid] + (long long)blockIdx.x * kSW * kSW;
   const int r = threadIdx.x & (kSW - 1), half = threadIdx.x / kSW;
   C v = czero<C>();
   if (r < nb) {
     const int q0 = half * (nb / 2), q1 = half ? nb : nb / 2;
 #pragma unroll 8
-    for (int q = q0; q < q1; ++q) v = cfma(v, Minv[(long long)q * nb + r], xs[q]);
+    for (int q = q0; q < q1; ++q) v = cfma(v, Dm[(long long)q * nb + r], zs[q]);
   }
   red[half][r] = v;
   __syncthreads();
-  if (threadIdx.x < nb) t[threadIdx.x] = cadd(red[0][threadIdx.x], red[1][threadIdx.x]);
-}
-
-// forward, first diagonal block of every front of the level
-template <class C>
-__global__ void __launch_bounds__(256)
-    k_fwd_first(const int *__restrict__ fl, const DevFront *__restrict__ fr,
-                const long long *__restrict__ inv_off, const C *__restrict__ Linv,
-                C *__restrict__ work) {
-  __shared__ C xs[kSW];
-  __shared__ C red[2][kSW];
-  const int fid = fl[blockIdx.x];
-  const DevFront f = fr[fid];
-  const int nb = min(kSW, f.p);
-  C *t = work + f.toff;
-  for (int q = threadIdx.x; q < nb; q += blockDim.x) xs[q] = t[q];
-  __syncthreads();
-  apply_inverse_block(Linv + inv_off[fid], t, nb, xs, red);
-}
-
-// forward block step b of every front with p > (b+1) kSW: the pivot rows
-// below the block take t[r] -= L[r, b0:b1] y_b (CTA = 32 rows, 8 warps of
-// kSW/8 columns); the front's last CTA (atomic ticket) then forms
-// y_{b+1} = inv(L_{b+1}) t[b1:b2].
-template <class C>
-__global__ void __launch_bounds__(256)
-    k_fwd_blk(const int *__restrict__ fl, int b, const C *__restrict__ pool,
-              const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
-              const C *__restrict__ Linv, C *__restrict__ work, int *__restrict__ ticket) {
-  __shared__ C ys[kSW];
-  __shared__ C red8[8][32];
-  __shared__ C red[2][kSW];
-  __shared__ int last;
-  const int fid = fl[blockIdx.y];
-  const DevFront f = fr[fid];
-  const int b0 = b * kSW, b1 = min(f.p, b0 + kSW), nb = b1 - b0;
-  const int rows = f.p - b1;
-  if (rows <= 0) return;
-  const int nch = (rows + 31) / 32;
-  if ((int)blockIdx.x >= nch) return;
-  C *t = work + f.toff;
-  for (int q = threadIdx.x; q < nb; q += blockDim.x) ys[q] = t[b0 + q];
-  __syncthreads();
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  const int r = b1 + blockIdx.x * 32 + lane;
-  const C *F = pool + f.off;
-  C acc = czero<C>();
-  if (r < f.p) {
-    const int q0 = wp * (kSW / 8), q1 = min(nb, q0 + kSW / 8);
-#pragma unroll 8
-    for (int q = q0; q < q1; ++q) acc = cfma(acc, F[(long long)(b0 + q) * f.m + r], ys[q]);
-  }
-  red8[wp][lane] = acc;
-  __syncthreads();
-  if (wp == 0 && r < f.p) {
-    C v = t[r];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) v = csub(v, red8[k][lane]);
-    t[r] = v;
-  }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(ticket + blockIdx.y, 1) == nch - 1;
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  if (threadIdx.x == 0) ticket[blockIdx.y] = 0;
-  const int n2 = min(kSW, f.p - b1);
-  for (int q = threadIdx.x; q < n2; q += blockDim.x) ys[q] = __ldcg(t + b1 + q);
-  __syncthreads();
-  apply_inverse_block(Linv + inv_off[fid] + (long long)(b + 1) * kSW * kSW, t + b1, n2, ys,
-                      red);
-}
-
-// backward block step b of every front with p > b kSW:
-// x_b = inv(U_b) (t[b0:b1] - U[b0:b1, b1:p] x[b1:p]).  CTAs reduce column
-// chunks of kBC into FP64 partials (2 halves x kSW rows per CTA); the
-// front's last CTA sums them and applies the inverse.
-constexpr int kBC = 64;
-
-template <class C>
-__global__ void __launch_bounds__(256)
-    k_bwd_blk(const int *__restrict__ fl, int b, const C *__restrict__ pool,
-              const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
-              const C *__restrict__ Uinv, C *__restrict__ work, double2 *__restrict__ partial,
-              int max_chunks, int *__restrict__ ticket) {
-  __shared__ C xs[kSW];
-  __shared__ C red[2][kSW];
-  __shared__ int last;
-  const int fid = fl[blockIdx.y];
-  const DevFront f = fr[fid];
-  const int b0 = b * kSW, b1 = min(f.p, b0 + kSW), nb = b1 - b0;
-  if (nb <= 0) return;
-  const int cols = f.p - b1;
-  const int nch = cols > 0 ? (cols + kBC - 1) / kBC : 1;
-  if ((int)blockIdx.x >= nch) return;
-  C *t = work + f.toff;
-  if (cols > 0) {
-    const C *F = pool + f.off;
-    const int r = threadIdx.x & (kSW - 1), half = threadIdx.x / kSW;
-    const int c0 = b1 + blockIdx.x * kBC + half * (kBC / 2), c1 = min(f.p, c0 + kBC / 2);
-    C acc = czero<C>();
-    if (r < nb) {
-#pragma unroll 8
-      for (int c = c0; c < c1; ++c) acc = cfma(acc, F[(long long)c * f.m + b0 + r], t[c]);
+  if (threadIdx.x < nb) {
+    C w = cadd(red[0][threadIdx.x], red[1][threadIdx.x]);
+    const int nchf = f.m > f.p ? (f.m - f.p + kBC - 1) / kBC : 0;
+    double2 s = make_double2(0, 0);
+    for (int k = 0; k < nchf; ++k) {
+      const double2 pv = partial[((long long)fq * nck + k) * pmax + b0 + threadIdx.x];
+      s.x += pv.x;
+      s.y += pv.y;
     }
-    red[half][r] = acc;
-    __syncthreads();
-    if (threadIdx.x < nb)
-      partial[((long long)blockIdx.y * max_chunks + blockIdx.x) * kSW + threadIdx.x] =
-          to64(cadd(red[0][threadIdx.x], red[1][threadIdx.x]));
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(ticket + blockIdx.y, 1) == nch - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    if (threadIdx.x == 0) ticket[blockIdx.y] = 0;
-    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
-      double2 s = make_double2(0, 0);
-      for (int k = 0; k < nch; ++k) {
-        const double2 v = __ldcg(partial + ((long long)blockIdx.y * max_chunks + k) * kSW + q);
-        s.x += v.x;
-        s.y += v.y;
-      }
-      xs[q] = csub(t[b0 + q], from64<C>(s));
-    }
-  } else {
-    for (int q = threadIdx.x; q < nb; q += blockDim.x) xs[q] = t[b0 + q];
+    t[threadIdx.x] = csub(w, from64<C>(s));
   }
-  __syncthreads();
-  apply_inverse_block(Uinv + inv_off[fid] + (long long)b * kSW * kSW, t + b0, nb, xs, red);
-}
-
-// forward border coupling of one level, pass 1: partial[front][chunk][r] =
-// sum over a 512-column chunk of L21[r, c] t[c] (L21 = rows p..m-1).
-template <class C>
-__global__ void __launch_bounds__(128)
-    k_fwd_border(const int *__restrict__ fl, const C *__restrict__ pool,
-                 const DevFront *__restrict__ fr, const C *__restrict__ work,
-                 double2 *__restrict__ partial, int nck, int bmax) {
-  __shared__ C ts[512];
-  const DevFront f = fr[fl[blockIdx.z]];
-  const int b = f.m - f.p;
-  const int c0 = blockIdx.y * 512;
-  if (c0 >= f.p || (int)(blockIdx.x * blockDim.x) >= b) return;
-  const int c1 = min(f.p, c0 + 512);
-  const C *t = work + f.toff;
-  for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) ts[c - c0] = t[c];
-  __syncthreads();
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= b) return;
-  const C *F = pool + f.off + f.p + r;
-  C a0 = czero<C>(), a1 = czero<C>();
-  int c = c0;
-  for (; c + 1 < c1; c += 2) {
-    a0 = cfma(a0, F[(long long)c * f.m], ts[c - c0]);
-    a1 = cfma(a1, F[(long long)(c + 1) * f.m], ts[c + 1 - c0]);
-  }
-  if (c < c1) a0 = cfma(a0, F[(long long)c * f.m], ts[c - c0]);
-  partial[((long long)blockIdx.z * nck + blockIdx.y) * bmax + r] = to64(cadd(a0, a1));
-}
-
-// pass 2: t[p + r] -= sum of the chunks, in chunk order.
-template <class C>
-__global__ void k_fwd_border_reduce(const int *__restrict__ fl, const DevFront *__restrict__ fr,
-                                    C *__restrict__ work, const double2 *__restrict__ partial,
-                                    int nck, int bmax) {
-  const DevFront f = fr[fl[blockIdx.y]];
-  const int b = f.m - f.p;
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= b) return;
-  const int nc = (f.p + 511) / 512;
-  double2 acc = make_double2(0, 0);
-  for (int q = 0; q < nc; ++q) {
-    const double2 v = partial[((long long)blockIdx.y * nck + q) * bmax + r];
-    acc.x += v.x;
-    acc.y += v.y;
-  }
-  C *t = work + f.toff + f.p + r;
-  *t = csub(*t, from64<C>(acc));
-}
-
-// backward border coupling of one level, pass 1: partial[front][chunk][i]
-// = sum over a 512-column chunk of the border of U12[i, c] t[c], pivot rows i.
-template <class C>
-__global__ void __launch_bounds__(128)
-    k_bwd_border(const int *__restrict__ fl, const C *__restrict__ pool,
-                 const DevFront *__restrict__ fr, const C *__restrict__ work,
-                 double2 *__restrict__ partial, int nck, int pmax) {
-  __shared__ C ts[512];
-  const DevFront f = fr[fl[blockIdx.z]];
-  const int b = f.m - f.p;
-  const int c0 = blockIdx.y * 512;
-  if (c0 >= b || (int)(blockIdx.x * blockDim.x) >= f.p) return;
-  const int c1 = min(b, c0 + 512);
-  const C *t = work + f.toff + f.p;
-  for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) ts[c - c0] = t[c];
-  __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= f.p) return;
-  const C *F = pool + f.off + (long long)f.p * f.m + i;
-  C a0 = czero<C>(), a1 = czero<C>();
-  int c = c0;
-  for (; c + 1 < c1; c += 2) {
-    a0 = cfma(a0, F[(long long)c * f.m], ts[c - c0]);
-    a1 = cfma(a1, F[(long long)(c + 1) * f.m], ts[c + 1 - c0]);
-  }
-  if (c < c1) a0 = cfma(a0, F[(long long)c * f.m], ts[c - c0]);
-  partial[((long long)blockIdx.z * nck + blockIdx.y) * pmax + i] = to64(cadd(a0, a1));
-}
-
-// pass 2: t[i] -= sum of the chunks for the pivot rows.
-template <class C>
-__global__ void k_bwd_border_reduce(const int *__restrict__ fl, const DevFront *__restrict__ fr,
-                                    C *__restrict__ work, const double2 *__restrict__ partial,
-                                    int nck, int pmax) {
-  const DevFront f = fr[fl[blockIdx.y]];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= f.p) return;
-  const int nc = (f.m - f.p + 511) / 512;
-  double2 acc = make_double2(0, 0);
-  for (int q = 0; q < nc; ++q) {
-    const double2 v = partial[((long long)blockIdx.y * nck + q) * pmax + i];
-    acc.x += v.x;
-    acc.y += v.y;
-  }
-  C *t = work + f.toff + i;
-  *t = csub(*t, from64<C>(acc));
 }
 
 // backward: t[p:m] = x at the border unknowns (already solved ancestors)
@@ -887,7 +864,6 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
     }
     levels.push_back(L);
   }
-  max_chunks = 1;
   long long partial_elems = 0;
   for (auto &L : levels) {
     L.pmax = 0;
@@ -897,35 +873,43 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
       L.pmax = std::max(L.pmax, f.p);
       L.bmax = std::max(L.bmax, f.m - f.p);
     }
-    L.nck_f = std::max(1, (L.pmax + 511) / 512);
-    L.nck_b = std::max(1, (L.bmax + 511) / 512);
+    L.nck_b = std::max(1, (L.bmax + kBC - 1) / kBC);
     L.blk_nf.clear();
+    L.fwd_rows.clear();
     for (int b = 0; b * kSW < L.pmax; ++b) {
-      int n = 0;
-      for (int q = 0; q < L.nfronts; ++q)
-        if (sym.fronts[sched[L.fronts_off + q]].p > b * kSW) ++n;
+      int n = 0, rows = 0;
+      for (int q = 0; q < L.nfronts; ++q) {
+        const FrontInfo &f = sym.fronts[sched[L.fronts_off + q]];
+        if (f.p > b * kSW) {
+          ++n;
+          rows = std::max(rows, f.m - std::min(f.p, (b + 1) * kSW));
+        }
+      }
       L.blk_nf.push_back(n);
+      L.fwd_rows.push_back(rows);
     }
-    max_chunks = std::max(max_chunks, (std::max(L.pmax - kSW, 1) + kBC - 1) / kBC);
-    partial_elems = std::max(partial_elems, (long long)L.nfronts * L.nck_f * std::max(L.bmax, 1));
     partial_elems = std::max(partial_elems, (long long)L.nfronts * L.nck_b * std::max(L.pmax, 1));
   }
-  int max_lvl_fronts = 1;
-  for (auto &L : levels) max_lvl_fronts = std::max(max_lvl_fronts, L.nfronts);
-  partial_elems = std::max(partial_elems, (long long)max_lvl_fronts * max_chunks * kSW);
-  // diagonal-block inverses: full blocks kSW x kSW, the last one nb x nb
+  // diagonal blocks (full blocks kSW x kSW, the last one nb x nb) and the
+  // tiles of the factor rewrite L' = L Dl^-1, U' = Du^-1 U, D = Du^-1 Dl^-1
   std::vector<long long> inv_off(nf);
   std::vector<int2> inv_blocks;
+  std::vector<int4> ltiles, utiles;
   inv_elems = 0;
   for (int t = 0; t < nf; ++t) {
-    const int p = sym.fronts[t].p;
+    const int p = sym.fronts[t].p, m = sym.fronts[t].m;
     inv_off[t] = inv_elems;
     for (int b = 0; b * kSW < p; ++b) {
-      const int nb = std::min(kSW, p - b * kSW);
+      const int b1 = std::min(p, (b + 1) * kSW), nb = b1 - b * kSW;
       inv_blocks.push_back(make_int2(t, b));
       inv_elems += (long long)nb * nb;
+      for (int r = b1; r < m; r += kRT) ltiles.push_back(make_int4(t, b, r, 0));
+      for (int c = b1; c < m; c += kRT) utiles.push_back(make_int4(t, b, c, 0));
+      for (int c = 0; c < nb; c += kRT) utiles.push_back(make_int4(t, b, c, 1));
     }
   }
+  n_ltiles = (long long)ltiles.size();
+  n_utiles = (long long)utiles.size();
   n_inv_blocks = (int)inv_blocks.size();
   const size_t csize = prec == 0 ? sizeof(double2) : sizeof(float2);
   auto alloc = [&](void **p, size_t bytes) -> int {
@@ -949,18 +933,23 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
       (rc = alloc((void **)&d_sched, sched.size() * sizeof(int))) ||
       (rc = alloc((void **)&d_partial, (size_t)partial_elems * sizeof(double2))) ||
       (rc = alloc((void **)&d_pert, sizeof(int))) ||
-      (rc = alloc((void **)&d_ticket, max_lvl_fronts * sizeof(int))) ||
       (rc = alloc(&linv, (size_t)inv_elems * csize)) ||
       (rc = alloc(&uinv, (size_t)inv_elems * csize)) ||
+      (rc = alloc(&dmat, (size_t)inv_elems * csize)) ||
+      (rc = alloc((void **)&d_ltiles, ltiles.size() * sizeof(int4))) ||
+      (rc = alloc((void **)&d_utiles, utiles.size() * sizeof(int4))) ||
       (rc = alloc((void **)&d_inv_off, nf * sizeof(long long))) ||
       (rc = alloc((void **)&d_inv_blocks, inv_blocks.size() * sizeof(int2))) ||
       (rc = alloc(&vec_a, (size_t)ctx->nn * 5 * csize)))
     return rc;
   TLR_CUDA(ctx, cudaMemcpy(d_inv_off, inv_off.data(), nf * sizeof(long long),
                            cudaMemcpyHostToDevice));
+  TLR_CUDA(ctx, cudaMemcpy(d_ltiles, ltiles.data(), ltiles.size() * sizeof(int4),
+                           cudaMemcpyHostToDevice));
+  TLR_CUDA(ctx, cudaMemcpy(d_utiles, utiles.data(), utiles.size() * sizeof(int4),
+                           cudaMemcpyHostToDevice));
   TLR_CUDA(ctx, cudaMemcpy(d_inv_blocks, inv_blocks.data(), inv_blocks.size() * sizeof(int2),
                            cudaMemcpyHostToDevice));
-  TLR_CUDA(ctx, cudaMemset(d_ticket, 0, max_lvl_fronts * sizeof(int)));
   TLR_CUDA(ctx, cudaMemcpy(d_fronts, df.data(), nf * sizeof(DevFront), cudaMemcpyHostToDevice));
   TLR_CUDA(ctx, cudaMemcpy(d_entries, sym.entries.data(), sym.entries.size() * sizeof(AsmEntry),
                            cudaMemcpyHostToDevice));
@@ -973,13 +962,29 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
   return TLR_OK;
 }
 
+double Factor::take_solve_time(int *count) {
+  double ms = 0.0;
+  if (ev_used > 0) cudaEventSynchronize(ev_pool[ev_used - 1]);
+  for (size_t i = 0; i + 1 < ev_used; i += 2) {
+    float e = 0.f;
+    if (cudaEventElapsedTime(&e, ev_pool[i], ev_pool[i + 1]) == cudaSuccess) ms += e;
+  }
+  if (count) *count = (int)(ev_used / 2);
+  ev_used = 0;
+  return ms;
+}
+
 void Factor::release() {
+  for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
+  ev_pool.clear();
+  ev_used = 0;
   cudaFree(pool); cudaFree(work); cudaFree(d_fronts); cudaFree(d_entries);
   cudaFree(d_cmap); cudaFree(d_nodes); cudaFree(d_ipiv); cudaFree(d_perm);
   cudaFree(d_pmap); cudaFree(d_sched); cudaFree(d_partial); cudaFree(d_pert);
-  cudaFree(vec_a); cudaFree(d_ticket); cudaFree(linv); cudaFree(uinv);
-  cudaFree(d_inv_off); cudaFree(d_inv_blocks);
-  linv = uinv = nullptr;
+  cudaFree(vec_a); cudaFree(linv); cudaFree(uinv); cudaFree(dmat);
+  cudaFree(d_inv_off); cudaFree(d_inv_blocks); cudaFree(d_ltiles); cudaFree(d_utiles);
+  linv = uinv = dmat = nullptr;
+  d_ltiles = d_utiles = nullptr;
   d_inv_off = nullptr;
   d_inv_blocks = nullptr;
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
@@ -1003,42 +1008,54 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
                                   (size_t)(L.pool_end - L.pool_begin) * sizeof(C), st));
     const long long ne = L.entry_end - L.entry_begin;
     if (ne > 0)
-      k_asm<C><<<blocks_for(ne * 25, 256), 256, 0, st>>>(d_entries + L.entry_begin, ne,
-                                                         ctx->A, ctx->B, sr, si, P, d_fronts);
+      { k_asm<C><<<blocks_for(ne * 25, 256), 256, 0, st>>>(d_entries + L.entry_begin, ne,
+                                                         ctx->A, ctx->B, sr, si, P, d_fronts); count_launches(); }
     for (int slot = 0; slot < 2; ++slot) {
       if (!L.kids[slot]) continue;
       const long long mb = L.kids_maxb[slot];
       dim3 g((unsigned)std::min<long long>(std::max<long long>(blocks_for(mb * mb, 256), 1), 4096),
              L.kids[slot]);
-      k_extend<C><<<g, 256, 0, st>>>(d_sched + L.kids_off[slot], d_fronts, d_cmap, P);
+      { k_extend<C><<<g, 256, 0, st>>>(d_sched + L.kids_off[slot], d_fronts, d_cmap, P); count_launches(); }
     }
     const int *fl = d_sched + L.fronts_off;
     for (int s = 0; s < (int)L.steps.size(); ++s) {
       const Step &S = L.steps[s];
-      k_panel<C><<<S.nf, 512, 0, st>>>(fl, s, w, P, d_fronts, d_ipiv, d_pert, tiny);
-      k_swap<C><<<dim3(blocks_for(S.max_m, 128), S.nf), 128, 0, st>>>(fl, s, w, P, d_fronts,
-                                                                       d_ipiv);
+      { k_panel<C><<<S.nf, 512, 0, st>>>(fl, s, w, P, d_fronts, d_ipiv, d_pert, tiny); count_launches(); }
+      { k_swap<C><<<dim3(blocks_for(S.max_m, 128), S.nf), 128, 0, st>>>(fl, s, w, P, d_fronts,
+                                                                       d_ipiv); count_launches(); }
       if (S.max_b > 0)
-        k_trsm_border<C><<<dim3(blocks_for(S.max_b, 128), S.nf), 128, tsm, st>>>(fl, s, w, P,
-                                                                                 d_fronts);
+        { k_trsm_border<C><<<dim3(blocks_for(S.max_b, 128), S.nf), 128, tsm, st>>>(fl, s, w, P,
+                                                                                 d_fronts); count_launches(); }
       if (S.max_ext > 0) {
-        k_trsm_urow<C><<<dim3(blocks_for(S.max_ext, 128), S.nf), 128, tsm, st>>>(fl, s, w, P,
-                                                                                 d_fronts);
+        { k_trsm_urow<C><<<dim3(blocks_for(S.max_ext, 128), S.nf), 128, tsm, st>>>(fl, s, w, P,
+                                                                                 d_fronts); count_launches(); }
         if (S.tiles > 0) {
           if constexpr (sizeof(C) == sizeof(float2))
-            k_gemm32<<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w,
-                                              reinterpret_cast<float2 *>(P), d_fronts);
+            { k_gemm32<<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w,
+                                              reinterpret_cast<float2 *>(P), d_fronts); count_launches(); }
           else
-            k_gemm<C><<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w, P,
-                                               d_fronts);
+            { k_gemm<C><<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w, P,
+                                               d_fronts); count_launches(); }
         }
       }
     }
   }
-  if (n_inv_blocks > 0)
-    k_tri_inv<C><<<dim3(n_inv_blocks, 2), kSW, 0, st>>>(d_inv_blocks, P, d_fronts, d_inv_off,
-                                                       static_cast<C *>(linv),
-                                                       static_cast<C *>(uinv));
+  if (n_inv_blocks > 0) {
+    C *Li = static_cast<C *>(linv), *Ui = static_cast<C *>(uinv);
+    { k_tri_inv<C><<<dim3(n_inv_blocks, 2), kSW, 0, st>>>(d_inv_blocks, P, d_fronts, d_inv_off,
+                                                         Li, Ui); count_launches(); }
+    const size_t ssm = sizeof(C) * kSW * kRT;
+    TLR_CUDA(ctx, cudaFuncSetAttribute(k_scale_u<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)ssm));
+    TLR_CUDA(ctx, cudaFuncSetAttribute(k_scale_l<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)ssm));
+    if (n_utiles > 0)
+      { k_scale_u<C><<<(unsigned)n_utiles, 256, ssm, st>>>(d_utiles, P, d_fronts, d_inv_off, Li,
+                                                           Ui, static_cast<C *>(dmat)); count_launches(); }
+    if (n_ltiles > 0)
+      { k_scale_l<C><<<(unsigned)n_ltiles, 256, ssm, st>>>(d_ltiles, P, d_fronts, d_inv_off,
+                                                           Li); count_launches(); }
+  }
   TLR_CUDA(ctx, cudaGetLastError());
   return TLR_OK;
 }
@@ -1092,46 +1109,35 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
   for (size_t h = 0; h < levels.size(); ++h) {
     const Level &L = levels[h];
     const int *fl = d_sched + L.fronts_off;
-    k_sgather<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(
-        fl, d_fronts, d_nodes, d_perm, x, W);
+    { k_sgather<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(
+        fl, d_fronts, d_nodes, d_perm, x, W); count_launches(); }
     for (int slot = 0; slot < 2; ++slot)
       if (L.kids[slot])
-        k_saddchild<C><<<dim3(blocks_for(std::max(L.kids_maxb[slot], 1), 128), L.kids[slot]),
-                         128, 0, st>>>(d_sched + L.kids_off[slot], d_fronts, d_pmap, W);
-    const C *Li = static_cast<const C *>(linv);
-    const C *Ui = static_cast<const C *>(uinv);
-    k_fwd_first<C><<<L.nfronts, 256, 0, st>>>(fl, d_fronts, d_inv_off, Li, W);
-    for (int b = 0; b + 1 < (int)L.blk_nf.size(); ++b) {
-      const int rows = L.pmax - (b + 1) * kSW;
-      k_fwd_blk<C><<<dim3(blocks_for(rows, 32), L.blk_nf[b + 1]), 256, 0, st>>>(
-          fl, b, P, d_fronts, d_inv_off, Li, W, d_ticket);
-    }
-    if (L.bmax > 0) {
-      k_fwd_border<C><<<dim3(blocks_for(L.bmax, 128), L.nck_f, L.nfronts), 128, 0, st>>>(
-          fl, P, d_fronts, W, d_partial, L.nck_f, L.bmax);
-      k_fwd_border_reduce<C><<<dim3(blocks_for(L.bmax, 128), L.nfronts), 128, 0, st>>>(
-          fl, d_fronts, W, d_partial, L.nck_f, L.bmax);
+        { k_saddchild<C><<<dim3(blocks_for(std::max(L.kids_maxb[slot], 1), 128), L.kids[slot]),
+                         128, 0, st>>>(d_sched + L.kids_off[slot], d_fronts, d_pmap, W); count_launches(); }
+    for (int b = 0; b < (int)L.blk_nf.size(); ++b) {
+      const int rows = L.fwd_rows[b];
+      if (rows > 0)
+        { k_blk_update<C><<<dim3(blocks_for(rows, 32), L.blk_nf[b]), 256, 0, st>>>(
+            fl, b, 0, P, d_fronts, W); count_launches(); }
     }
   }
   for (int h = (int)levels.size() - 1; h >= 0; --h) {
     const Level &L = levels[h];
     const int *fl = d_sched + L.fronts_off;
-    k_bgather<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(fl, d_fronts,
-                                                                             d_nodes, x, W);
-    if (L.bmax > 0) {
-      k_bwd_border<C><<<dim3(blocks_for(L.pmax, 128), L.nck_b, L.nfronts), 128, 0, st>>>(
-          fl, P, d_fronts, W, d_partial, L.nck_b, L.pmax);
-      k_bwd_border_reduce<C><<<dim3(blocks_for(L.pmax, 128), L.nfronts), 128, 0, st>>>(
-          fl, d_fronts, W, d_partial, L.nck_b, L.pmax);
-    }
-    for (int b = (int)L.blk_nf.size() - 1; b >= 0; --b) {
-      const int cols = L.pmax - (b + 1) * kSW;
-      k_bwd_blk<C><<<dim3(std::max(blocks_for(std::max(cols, 0), kBC), 1), L.blk_nf[b]), 256, 0,
-                     st>>>(fl, b, P, d_fronts, d_inv_off, static_cast<const C *>(uinv), W,
-                           d_partial, max_chunks, d_ticket);
-    }
-    k_bscatter<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(fl, d_fronts,
-                                                                              d_nodes, W, x);
+    { k_bgather<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(fl, d_fronts,
+                                                                             d_nodes, x, W); count_launches(); }
+    if (L.bmax > 0)
+      { k_border_gemv<C><<<dim3(blocks_for(L.pmax, 32), L.nck_b, L.nfronts), 256, 0, st>>>(
+          fl, P, d_fronts, W, d_partial, L.nck_b, L.pmax); count_launches(); }
+    { k_bwd_start<C><<<dim3((unsigned)L.blk_nf.size(), L.nfronts), 256, 0, st>>>(
+        fl, d_fronts, d_inv_off, static_cast<const C *>(dmat), W, d_partial, L.nck_b,
+        L.pmax); count_launches(); }
+    for (int b = (int)L.blk_nf.size() - 1; b >= 1; --b)
+      { k_blk_update<C><<<dim3(blocks_for(b * kSW, 32), L.blk_nf[b]), 256, 0, st>>>(
+          fl, b, 1, P, d_fronts, W); count_launches(); }
+    { k_bscatter<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(fl, d_fronts,
+                                                                              d_nodes, W, x); count_launches(); }
   }
   TLR_CUDA(ctx, cudaGetLastError());
   return TLR_OK;
@@ -1143,16 +1149,42 @@ int Factor::solve(tlr_ctx *ctx, void *x) {
   TLR_CUDA(ctx, cudaMemcpyAsync(vec_a, x, bytes, cudaMemcpyDeviceToDevice, st));
   if (!graph_exec) {
     TLR_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    const int rc = prec == 0 ? solve_impl<double2>(ctx, vec_a) : solve_impl<float2>(ctx, vec_a);
+    int rc;
+    {
+      CaptureScope cs;
+      rc = prec == 0 ? solve_impl<double2>(ctx, vec_a) : solve_impl<float2>(ctx, vec_a);
+    }
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(st, &g);
     if (rc) return rc;
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
+    size_t nn = 0;
+    graph_kernels = 0;
+    if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn > 0) {
+      std::vector<cudaGraphNode_t> nodes(nn);
+      if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+        for (size_t i = 0; i < nn; ++i) {
+          cudaGraphNodeType t;
+          if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+            ++graph_kernels;
+        }
+    }
     const cudaError_t e2 = cudaGraphInstantiate(&graph_exec, g, 0);
     cudaGraphDestroy(g);
     if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaGraphInstantiate");
   }
+  if (ev_used + 2 > ev_pool.size()) {
+    cudaEvent_t a, b;
+    TLR_CUDA(ctx, cudaEventCreate(&a));
+    TLR_CUDA(ctx, cudaEventCreate(&b));
+    ev_pool.push_back(a);
+    ev_pool.push_back(b);
+  }
+  TLR_CUDA(ctx, cudaEventRecord(ev_pool[ev_used], st));
   TLR_CUDA(ctx, cudaGraphLaunch(graph_exec, st));
+  TLR_CUDA(ctx, cudaEventRecord(ev_pool[ev_used + 1], st));
+  ev_used += 2;
+  count_launches(graph_kernels);
   TLR_CUDA(ctx, cudaMemcpyAsync(x, vec_a, bytes, cudaMemcpyDeviceToDevice, st));
   return TLR_OK;
 }

@@ -21,11 +21,12 @@ struct Step {  // one panel step of one level
 
 struct Level {
   int nfronts = 0, fronts_off = 0, max_m = 0;
-  int pmax = 0, bmax = 0, nck_f = 1, nck_b = 1;  // border GEMV chunking
+  int pmax = 0, bmax = 0, nck_b = 1;  // backward border GEMV chunks
   int kids[2] = {0, 0}, kids_off[2] = {0, 0}, kids_maxb[2] = {0, 0};
   long long entry_begin = 0, entry_end = 0, pool_begin = 0, pool_end = 0;
   std::vector<Step> steps;
-  std::vector<int> blk_nf;  // blk_nf[b]: fronts of the level with p > b kSW
+  std::vector<int> blk_nf;    // blk_nf[b]: fronts of the level with p > b kSW
+  std::vector<int> fwd_rows;  // rows below block b, largest over those fronts
 };
 
 struct Factor {
@@ -33,21 +34,28 @@ struct Factor {
   int prec = 0;  // 0: complex128 fronts, 1: complex64 fronts
   int w = 32;    // panel width
   std::vector<Level> levels;
-  int max_chunks = 1;
   void *pool = nullptr, *work = nullptr, *vec_a = nullptr;
   DevFront *d_fronts = nullptr;
   AsmEntry *d_entries = nullptr;
   int *d_cmap = nullptr, *d_nodes = nullptr, *d_ipiv = nullptr, *d_perm = nullptr;
-  int *d_pmap = nullptr, *d_sched = nullptr, *d_pert = nullptr, *d_ticket = nullptr;
-  // explicit inverses of the kSW x kSW diagonal blocks of every pivot block
-  void *linv = nullptr, *uinv = nullptr;
+  int *d_pmap = nullptr, *d_sched = nullptr, *d_pert = nullptr;
+  // kSW x kSW diagonal blocks of every pivot block: inv(L_bb), inv(U_bb)
+  // (scratch of the factor rewrite) and D_b = inv(U_bb) inv(L_bb)
+  void *linv = nullptr, *uinv = nullptr, *dmat = nullptr;
   long long *d_inv_off = nullptr;
   int2 *d_inv_blocks = nullptr;
+  int4 *d_ltiles = nullptr, *d_utiles = nullptr;
   int n_inv_blocks = 0;
-  long long inv_elems = 0;
+  long long inv_elems = 0, n_ltiles = 0, n_utiles = 0;
   cudaGraphExec_t graph_exec = nullptr;  // captured solve, replayed per call
+  long long graph_kernels = 0;           // kernel nodes of graph_exec
   double2 *d_partial = nullptr;
   int perturbed = 0;
+  // CUDA events around every replayed solve graph (device time of the
+  // triangular solves); collected and reset by take_solve_time()
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  double take_solve_time(int *count);
   bool factored = false;
   double sigma_re = 0.0, sigma_im = 0.0;
 

@@ -206,9 +206,9 @@ void forward(tlr_mlp *m, int n) {
     const int in = m->fan_in[l], out = m->fan_out[l];
     float *Z = m->pre + plane * (l + 1), *Y = m->act + plane * (l + 1);
     dim3 g((out + kT - 1) / kT, (n + kT - 1) / kT), b(kT, kT);
-    k_lin_fwd<<<g, b, 0, m->stream>>>(n, in, out, X, ldx, m->params + m->w_off[l],
+    { k_lin_fwd<<<g, b, 0, m->stream>>>(n, in, out, X, ldx, m->params + m->w_off[l],
                                       m->params + m->b_off[l], Z, Y, m->maxw,
-                                      l + 1 < m->n_layers);
+                                      l + 1 < m->n_layers); count_launches(); }
     X = Y;
     ldx = m->maxw;
   }
@@ -222,18 +222,18 @@ void backward(tlr_mlp *m, int n) {
     float *dZ = m->dact + plane * (l + 1);
     if (l + 1 < m->n_layers) {
       const long long cnt = (long long)n * out;
-      k_silu_bwd<<<blocks_for(cnt, 256), 256, 0, m->stream>>>(cnt, out, m->maxw,
-                                                             m->pre + plane * (l + 1), dZ);
+      { k_silu_bwd<<<blocks_for(cnt, 256), 256, 0, m->stream>>>(cnt, out, m->maxw,
+                                                             m->pre + plane * (l + 1), dZ); count_launches(); }
     }
     const float *X = l == 0 ? m->xbuf : m->act + plane * l;
     const int ldx = l == 0 ? m->n_in : m->maxw;
     dim3 gw((in + kT - 1) / kT, (out + kT - 1) / kT), b(kT, kT);
-    k_lin_bwd_weight<<<gw, b, 0, m->stream>>>(n, in, out, dZ, m->maxw, X, ldx,
-                                              m->grads + m->w_off[l], m->grads + m->b_off[l]);
+    { k_lin_bwd_weight<<<gw, b, 0, m->stream>>>(n, in, out, dZ, m->maxw, X, ldx,
+                                              m->grads + m->w_off[l], m->grads + m->b_off[l]); count_launches(); }
     if (l > 0) {
       dim3 gd((in + kT - 1) / kT, (n + kT - 1) / kT);
-      k_lin_bwd_data<<<gd, b, 0, m->stream>>>(n, in, out, dZ, m->maxw, m->params + m->w_off[l],
-                                              m->dact + plane * l, m->maxw);
+      { k_lin_bwd_data<<<gd, b, 0, m->stream>>>(n, in, out, dZ, m->maxw, m->params + m->w_off[l],
+                                              m->dact + plane * l, m->maxw); count_launches(); }
     }
   }
 }
@@ -321,8 +321,8 @@ int tlr_mlp_gradients(tlr_mlp *m, const float *X, const float *Y, int n, float *
   cudaMemsetAsync(m->grads, 0, sizeof(float) * m->n_params, m->stream);
   forward(m, n);
   const size_t plane = (size_t)m->cap * m->maxw;
-  k_mse<<<1, 256, 0, m->stream>>>(n, m->n_out, m->maxw, m->act + plane * m->n_layers, m->ybuf,
-                                  m->dact + plane * m->n_layers, m->loss);
+  { k_mse<<<1, 256, 0, m->stream>>>(n, m->n_out, m->maxw, m->act + plane * m->n_layers, m->ybuf,
+                                  m->dact + plane * m->n_layers, m->loss); count_launches(); }
   backward(m, n);
   if (grads)
     cudaMemcpyAsync(grads, m->grads, sizeof(float) * m->n_params, cudaMemcpyDeviceToHost,
@@ -361,14 +361,14 @@ int tlr_mlp_train(tlr_mlp *m, const float *X, const float *Y, int n, int epochs,
                       cudaMemcpyDeviceToDevice, m->stream);
       cudaMemsetAsync(m->grads, 0, sizeof(float) * m->n_params, m->stream);
       forward(m, nr);
-      k_mse<<<1, 256, 0, m->stream>>>(nr, m->n_out, m->maxw, m->act + plane * m->n_layers,
-                                      m->ybuf, m->dact + plane * m->n_layers, m->loss);
+      { k_mse<<<1, 256, 0, m->stream>>>(nr, m->n_out, m->maxw, m->act + plane * m->n_layers,
+                                      m->ybuf, m->dact + plane * m->n_layers, m->loss); count_launches(); }
       backward(m, nr);
       ++m->adam_t;
       const float c1 = 1.f - std::pow(b1, (float)m->adam_t), c2 = 1.f - std::pow(b2, (float)m->adam_t);
-      k_adam<<<blocks_for(m->n_params, 256), 256, 0, m->stream>>>(m->n_params, m->params, m->grads,
+      { k_adam<<<blocks_for(m->n_params, 256), 256, 0, m->stream>>>(m->n_params, m->params, m->grads,
                                                                   m->m1, m->m2, lr, b1, b2, c1, c2,
-                                                                  eps);
+                                                                  eps); count_launches(); }
       if (loss_history) {
         float l = 0.f;
         cudaMemcpyAsync(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->stream);
@@ -399,19 +399,19 @@ int tlr_mlp_forward(tlr_mlp *m, const float *X, int n, float *Y, int bf16) {
                       sizeof(float) * m->maxw, sizeof(float) * m->n_out, n,
                       cudaMemcpyDeviceToHost, m->stream);
   } else {
-    k_to_bf16<<<blocks_for(m->n_params, 256), 256, 0, m->stream>>>(m->n_params, m->params,
-                                                                   m->params16);
+    { k_to_bf16<<<blocks_for(m->n_params, 256), 256, 0, m->stream>>>(m->n_params, m->params,
+                                                                   m->params16); count_launches(); }
     __nv_bfloat16 *a = reinterpret_cast<__nv_bfloat16 *>(m->act);
     __nv_bfloat16 *bb = reinterpret_cast<__nv_bfloat16 *>(m->pre);
-    k_to_bf16<<<blocks_for((long long)n * m->n_in, 256), 256, 0, m->stream>>>(
-        (long long)n * m->n_in, m->xbuf, a);
+    { k_to_bf16<<<blocks_for((long long)n * m->n_in, 256), 256, 0, m->stream>>>(
+        (long long)n * m->n_in, m->xbuf, a); count_launches(); }
     for (int l = 0; l < m->n_layers; ++l) {
       const int in = m->fan_in[l], o = m->fan_out[l];
       const bool last = l + 1 == m->n_layers;
       dim3 g((o + kT - 1) / kT, (n + kT - 1) / kT), b(kT, kT);
-      k_lin_fwd16<<<g, b, 0, m->stream>>>(n, in, o, a, m->params16 + m->w_off[l],
+      { k_lin_fwd16<<<g, b, 0, m->stream>>>(n, in, o, a, m->params16 + m->w_off[l],
                                           m->params16 + m->b_off[l], last ? nullptr : bb,
-                                          last ? m->dact : nullptr, !last);
+                                          last ? m->dact : nullptr, !last); count_launches(); }
       std::swap(a, bb);
     }
     cudaMemcpyAsync(Y, m->dact, sizeof(float) * n * m->n_out, cudaMemcpyDeviceToHost, m->stream);

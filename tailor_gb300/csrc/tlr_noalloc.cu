@@ -105,9 +105,9 @@ extern "C" int tlr_frobenius_noalloc(const double *values, size_t count, double 
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int nb = count == 0 ? 1 : (int)(((long long)count + kPerBlock - 1) / kPerBlock);
-  k_partial<<<nb, 256, 0, st>>>((long long)count, reinterpret_cast<const double2 *>(values),
-                                scratch);
-  k_final<<<1, 32, 0, st>>>(nb, scratch);
+  { k_partial<<<nb, 256, 0, st>>>((long long)count, reinterpret_cast<const double2 *>(values),
+                                scratch); count_launches(); }
+  { k_final<<<1, 32, 0, st>>>(nb, scratch); count_launches(); }
   e = cudaGetLastError();
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(result, scratch + kMaxPartials, sizeof(double), cudaMemcpyDeviceToHost,

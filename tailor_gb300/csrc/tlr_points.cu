@@ -129,7 +129,7 @@ extern "C" int tlr_lns_points(const tlr_recipe *r, int np, const double *q,
   } else {
     PointParams p{np, r->reynolds, r->prandtl, r->mach, r->gamma,
                   r->sutherland_constant / r->reference_temperature};
-    k_lns_points<<<(np + 63) / 64, 64>>>(p, dq, dout, dst);
+    { k_lns_points<<<(np + 63) / 64, 64>>>(p, dq, dout, dst); count_launches(); }
     if (cudaMemcpy(blocks, dout, sizeof(double) * np * 275, cudaMemcpyDeviceToHost) ||
         cudaMemcpy(status, dst, sizeof(int) * np, cudaMemcpyDeviceToHost))
       rc = TLR_ERR_CUDA;
@@ -151,7 +151,7 @@ extern "C" int tlr_transform_points(int np, const double *alpha, const double *p
       up<double>(&dc, nullptr, (size_t)np * 350) || up<int>(&dst, nullptr, np)) {
     rc = TLR_ERR_CUDA;
   } else {
-    k_transform_points<<<(np + 63) / 64, 64>>>(np, da, dp, dm, df, dc, dst);
+    { k_transform_points<<<(np + 63) / 64, 64>>>(np, da, dp, dm, df, dc, dst); count_launches(); }
     if (cudaMemcpy(fourier, df, sizeof(double) * np * 350, cudaMemcpyDeviceToHost) ||
         cudaMemcpy(curvilinear, dc, sizeof(double) * np * 350, cudaMemcpyDeviceToHost) ||
         cudaMemcpy(status, dst, sizeof(int) * np, cudaMemcpyDeviceToHost))

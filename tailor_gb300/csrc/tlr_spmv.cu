@@ -8,6 +8,8 @@
 // load, and each lane accumulates its own complex partial sum over the row
 // before a five-lane reduction.  The blocks are streamed with evict-first
 // loads; x stays L2-resident.
+#include <atomic>
+
 #include "tlr_internal.h"
 
 namespace tlr {
@@ -107,20 +109,33 @@ int run_spmv(tlr_ctx *ctx, int which, const double2 *x, double2 *y) {
     rp = ctx->row_ptr + (ctx->nn + 1);
     cl = rp + (ctx->nn + 1);
   }
-  k_bsr_spmv<<<blocks_for(nrows, kRowsPerCta), 32 * kRowsPerCta, 0, ctx->stream>>>(
-      nrows, rp, cl, val, x, y);
+  { k_bsr_spmv<<<blocks_for(nrows, kRowsPerCta), 32 * kRowsPerCta, 0, ctx->stream>>>(
+      nrows, rp, cl, val, x, y); count_launches(); }
   TLR_CUDA(ctx, cudaGetLastError());
   return TLR_OK;
 }
 
 int frobenius(tlr_ctx *ctx, const double2 *v, long long count, double *out) {
   const int blocks = ctx->partial_blocks;
-  k_sq2_partial<<<blocks, 256, 0, ctx->stream>>>(count, v, ctx->partial);
-  k_sum_sqrt<<<1, 32, 0, ctx->stream>>>(blocks, ctx->partial, ctx->partial + blocks);
+  { k_sq2_partial<<<blocks, 256, 0, ctx->stream>>>(count, v, ctx->partial); count_launches(); }
+  { k_sum_sqrt<<<1, 32, 0, ctx->stream>>>(blocks, ctx->partial, ctx->partial + blocks); count_launches(); }
   TLR_CUDA(ctx, cudaMemcpyAsync(out, ctx->partial + blocks, sizeof(double),
                                 cudaMemcpyDeviceToHost, ctx->stream));
   TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return TLR_OK;
 }
+
+// ---------------------------------------------------------- launch count
+namespace {
+std::atomic<long long> g_launches{0};
+thread_local int t_capturing = 0;
+}  // namespace
+
+void count_launches(long long n) {
+  if (!t_capturing) g_launches.fetch_add(n, std::memory_order_relaxed);
+}
+long long launch_total() { return g_launches.load(std::memory_order_relaxed); }
+CaptureScope::CaptureScope() { ++t_capturing; }
+CaptureScope::~CaptureScope() { --t_capturing; }
 
 }  // namespace tlr
