@@ -418,11 +418,15 @@ __global__ void __launch_bounds__(256)
 
 // ------------------------------------------------------------------ solves
 
-// t[i] = b[unknown of front row perm[i]] for pivot rows, 0 for border rows.
+// Forward gather of one level: t[i] = b[unknown of front row perm[i]] for
+// pivot rows (0 for border rows), plus the children's updated border rows
+// that map to row i (cinv: absolute work index per child slot, -1: none),
+// added in child-slot order.
 template <class C>
 __global__ void k_sgather(const int *__restrict__ fl, const DevFront *__restrict__ fr,
                           const int *__restrict__ nodes, const int *__restrict__ perm,
-                          const C *__restrict__ b, C *__restrict__ work) {
+                          const int2 *__restrict__ cinv, const C *__restrict__ b,
+                          C *__restrict__ work) {
   const DevFront f = fr[fl[blockIdx.y]];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= f.m) return;
@@ -431,21 +435,10 @@ __global__ void k_sgather(const int *__restrict__ fl, const DevFront *__restrict
     const int q = perm[f.toff + i];
     v = b[(long long)nodes[f.node_off + q / 5] * 5 + q % 5];
   }
+  const int2 c = cinv[f.toff + i];
+  if (c.x >= 0) v = cadd(v, work[c.x]);
+  if (c.y >= 0) v = cadd(v, work[c.y]);
   work[f.toff + i] = v;
-}
-
-// parent's t += child's border update, at the permuted positions.
-template <class C>
-__global__ void k_saddchild(const int *__restrict__ kids, const DevFront *__restrict__ fr,
-                            const int *__restrict__ pmap, C *__restrict__ work) {
-  const DevFront fc = fr[kids[blockIdx.y]];
-  const DevFront fp = fr[fc.parent];
-  const int bc = fc.m - fc.p;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= bc) return;
-  const int q = pmap[fc.toff + x];
-  C &d = work[fp.toff + q];
-  d = cadd(d, work[fc.toff + fc.p + x]);
 }
 
 // ---- block-scaled triangular solves ---------------------------------------
@@ -628,10 +621,13 @@ __global__ void __launch_bounds__(256)
 // One solve step of every front of the level that owns block b: rows
 // [lo, hi) take t[r] -= F(r, b0:b1) t[b0:b1] (forward: lo = b1, hi = m;
 // backward: lo = 0, hi = b0).  CTA = 32 rows x 8 warps of kSW/8 columns.
+// Backward steps run on the pivot-row vector of the backward pass; rows of
+// block b-1 are final after step b and are written to the solution x.
 template <class C>
 __global__ void __launch_bounds__(256)
     k_blk_update(const int *__restrict__ fl, int b, int backward, const C *__restrict__ pool,
-                 const DevFront *__restrict__ fr, C *__restrict__ work) {
+                 const DevFront *__restrict__ fr, C *__restrict__ work,
+                 const int *__restrict__ nodes, C *__restrict__ x) {
   __shared__ C vs[kSW];
   __shared__ C red[8][32];
   const DevFront f = fr[fl[blockIdx.y]];
@@ -663,33 +659,42 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int k = 0; k < 8; ++k) v = csub(v, red[k][lane]);
     t[r] = v;
+    if (backward && r >= b0 - kSW) x[(long long)nodes[f.node_off + r / 5] * 5 + r % 5] = v;
   }
 }
 
 // Backward border product, pass 1: partial[front][chunk][i] = sum over a
-// kBC-column chunk of the border of U'(i, c) t[c], pivot rows i.  CTA = 32
-// rows x 8 warps of kBC/8 columns.
+// kBC-column chunk of the border of U'(i, c) x[unknown of border row c],
+// pivot rows i (the border unknowns belong to ancestors, already solved).
+// CTA = 32 rows x 8 warps of kBC/8 columns.
 constexpr int kBC = 256;
 
 template <class C>
 __global__ void __launch_bounds__(256)
     k_border_gemv(const int *__restrict__ fl, const C *__restrict__ pool,
-                  const DevFront *__restrict__ fr, const C *__restrict__ work,
-                  double2 *__restrict__ partial, int nck, int pmax) {
+                  const DevFront *__restrict__ fr, const int *__restrict__ nodes,
+                  const C *__restrict__ x, double2 *__restrict__ partial, int nck, int pmax) {
+  __shared__ C xs[kBC];
   __shared__ C red[8][32];
   const int fq = blockIdx.z;
   const DevFront f = fr[fl[fq]];
   const int r0 = blockIdx.x * 32;
   const int c0 = f.p + blockIdx.y * kBC;
-  if (r0 >= f.p) return;
-  const C *t = work + f.toff;
+  if (r0 >= f.p || c0 >= f.m) return;
+  const int nc = min(kBC, f.m - c0);
+  for (int k = threadIdx.x; k < nc; k += blockDim.x) {
+    const int c = c0 + k;
+    xs[k] = x[(long long)nodes[f.node_off + c / 5] * 5 + c % 5];
+  }
+  __syncthreads();
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const int r = r0 + lane;
   C acc = czero<C>();
   if (r < f.p) {
-    const int ca = c0 + wp * (kBC / 8), cb = min(f.m, ca + kBC / 8);
+    const int ka = wp * (kBC / 8), kb = min(nc, ka + kBC / 8);
+    const C *F = pool + f.off + (long long)c0 * f.m + r;
 #pragma unroll 8
-    for (int c = ca; c < cb; ++c) acc = cfma(acc, pool[f.off + (long long)c * f.m + r], t[c]);
+    for (int k = ka; k < kb; ++k) acc = cfma(acc, F[(long long)k * f.m], xs[k]);
   }
   red[wp][lane] = acc;
   __syncthreads();
@@ -701,65 +706,59 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Start of a front's backward pass, block b: t_b = D_b z_b minus the
-// border chunks of pass 1 (summed in chunk order).  256 threads = 2 halves
-// of the q range for each of kSW rows.
+// Start of a front's backward pass: rows of block b = blockIdx.x / 4
+// (32 per CTA) take w = D_b z_b minus the border chunks of pass 1 (summed
+// in chunk order), written to the backward vector (z stays in work for the
+// other CTAs of the block).  The last block's rows are final and go to x.
 template <class C>
 __global__ void __launch_bounds__(256)
     k_bwd_start(const int *__restrict__ fl, const DevFront *__restrict__ fr,
                 const long long *__restrict__ inv_off, const C *__restrict__ dmat,
-                C *__restrict__ work, const double2 *__restrict__ partial, int nck, int pmax) {
+                const C *__restrict__ work, C *__restrict__ work2,
+                const double2 *__restrict__ partial, int nck, int pmax,
+                const int *__restrict__ nodes, C *__restrict__ x) {
   __shared__ C zs[kSW];
-  __shared__ C red[2][kSW];
+  __shared__ C red[8][32];
   const int fq = blockIdx.y, fid = fl[fq];
   const DevFront f = fr[fid];
-  const int b0 = blockIdx.x * kSW, nb = min(kSW, f.p - b0);
-  if (nb <= 0) return;
-  C *t = work + f.toff + b0;
-  for (int q = threadIdx.x; q < nb; q += blockDim.x) zs[q] = t[q];
+  const int blk = blockIdx.x / (kSW / 32), quarter = blockIdx.x % (kSW / 32);
+  const int b0 = blk * kSW, nb = min(kSW, f.p - b0);
+  const int rr0 = quarter * 32;
+  if (nb <= 0 || rr0 >= nb) return;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int rr = rr0 + lane;  // row inside the block
+  const C *Dm = dmat + inv_off[fid] + (long long)blk * kSW * kSW;
+  constexpr int kQ = kSW / 8;
+  const int q0 = wp * kQ;
+  C dv[kQ];
+#pragma unroll
+  for (int k = 0; k < kQ; ++k)
+    dv[k] = (rr < nb && q0 + k < nb) ? Dm[(long long)(q0 + k) * nb + rr] : czero<C>();
+  const C *z = work + f.toff + b0;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) zs[q] = z[q];
   __syncthreads();
-  const C *Dm = dmat + inv_off[fid] + (long long)blockIdx.x * kSW * kSW;
-  const int r = threadIdx.x & (kSW - 1), half = threadIdx.x / kSW;
-  C v = czero<C>();
-  if (r < nb) {
-    const int q0 = half * (nb / 2), q1 = half ? nb : nb / 2;
-#pragma unroll 8
-    for (int q = q0; q < q1; ++q) v = cfma(v, Dm[(long long)q * nb + r], zs[q]);
-  }
-  red[half][r] = v;
+  C acc = czero<C>();
+#pragma unroll
+  for (int k = 0; k < kQ; ++k)
+    if (q0 + k < nb) acc = cfma(acc, dv[k], zs[q0 + k]);
+  red[wp][lane] = acc;
   __syncthreads();
-  if (threadIdx.x < nb) {
-    C w = cadd(red[0][threadIdx.x], red[1][threadIdx.x]);
+  if (wp == 0 && rr < nb) {
+    C w = czero<C>();
+#pragma unroll
+    for (int k = 0; k < 8; ++k) w = cadd(w, red[k][lane]);
+    const int r = b0 + rr;
     const int nchf = f.m > f.p ? (f.m - f.p + kBC - 1) / kBC : 0;
     double2 s = make_double2(0, 0);
     for (int k = 0; k < nchf; ++k) {
-      const double2 pv = partial[((long long)fq * nck + k) * pmax + b0 + threadIdx.x];
+      const double2 pv = partial[((long long)fq * nck + k) * pmax + r];
       s.x += pv.x;
       s.y += pv.y;
     }
-    t[threadIdx.x] = csub(w, from64<C>(s));
+    w = csub(w, from64<C>(s));
+    work2[f.toff + r] = w;
+    if (b0 + kSW >= f.p) x[(long long)nodes[f.node_off + r / 5] * 5 + r % 5] = w;
   }
-}
-
-// backward: t[p:m] = x at the border unknowns (already solved ancestors)
-template <class C>
-__global__ void k_bgather(const int *__restrict__ fl, const DevFront *__restrict__ fr,
-                          const int *__restrict__ nodes, const C *__restrict__ x,
-                          C *__restrict__ work) {
-  const DevFront f = fr[fl[blockIdx.y]];
-  const int i = f.p + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= f.m) return;
-  work[f.toff + i] = x[(long long)nodes[f.node_off + i / 5] * 5 + i % 5];
-}
-
-template <class C>
-__global__ void k_bscatter(const int *__restrict__ fl, const DevFront *__restrict__ fr,
-                           const int *__restrict__ nodes, const C *__restrict__ work,
-                           C *__restrict__ x) {
-  const DevFront f = fr[fl[blockIdx.y]];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= f.p) return;
-  x[(long long)nodes[f.node_off + i / 5] * 5 + i % 5] = work[f.toff + i];
 }
 
 }  // namespace
@@ -929,7 +928,8 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
       (rc = alloc((void **)&d_nodes, nodes.size() * sizeof(int))) ||
       (rc = alloc((void **)&d_ipiv, sym.work_elems * sizeof(int))) ||
       (rc = alloc((void **)&d_perm, sym.work_elems * sizeof(int))) ||
-      (rc = alloc((void **)&d_pmap, sym.work_elems * sizeof(int))) ||
+      (rc = alloc((void **)&d_cinv, sym.work_elems * sizeof(int2))) ||
+      (rc = alloc(&work2, (size_t)sym.work_elems * csize)) ||
       (rc = alloc((void **)&d_sched, sched.size() * sizeof(int))) ||
       (rc = alloc((void **)&d_partial, (size_t)partial_elems * sizeof(double2))) ||
       (rc = alloc((void **)&d_pert, sizeof(int))) ||
@@ -980,7 +980,7 @@ void Factor::release() {
   ev_used = 0;
   cudaFree(pool); cudaFree(work); cudaFree(d_fronts); cudaFree(d_entries);
   cudaFree(d_cmap); cudaFree(d_nodes); cudaFree(d_ipiv); cudaFree(d_perm);
-  cudaFree(d_pmap); cudaFree(d_sched); cudaFree(d_partial); cudaFree(d_pert);
+  cudaFree(d_cinv); cudaFree(work2); cudaFree(d_sched); cudaFree(d_partial); cudaFree(d_pert);
   cudaFree(vec_a); cudaFree(linv); cudaFree(uinv); cudaFree(dmat);
   cudaFree(d_inv_off); cudaFree(d_inv_blocks); cudaFree(d_ltiles); cudaFree(d_utiles);
   linv = uinv = dmat = nullptr;
@@ -989,7 +989,7 @@ void Factor::release() {
   d_inv_blocks = nullptr;
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   graph_exec = nullptr;
-  pool = work = vec_a = nullptr;
+  pool = work = work2 = vec_a = nullptr;
 }
 
 template <class C>
@@ -1093,7 +1093,20 @@ int Factor::factor(tlr_ctx *ctx, double sr, double si, double tiny) {
   }
   TLR_CUDA(ctx, cudaMemcpyAsync(d_perm, perm.data(), perm.size() * sizeof(int),
                                 cudaMemcpyHostToDevice, ctx->stream));
-  TLR_CUDA(ctx, cudaMemcpyAsync(d_pmap, pmap.data(), pmap.size() * sizeof(int),
+  // per parent row, the work index of each child slot's border row mapped
+  // onto it (the forward gather adds them in slot order)
+  std::vector<int2> cinv(sym.work_elems, make_int2(-1, -1));
+  for (int t = 0; t < nf; ++t) {
+    const FrontInfo &f = sym.fronts[t];
+    for (size_t slot = 0; slot < f.children.size() && slot < 2; ++slot) {
+      const FrontInfo &c = sym.fronts[f.children[slot]];
+      for (int x = 0; x < c.m - c.p; ++x) {
+        int2 &e = cinv[f.toff + pmap[c.toff + x]];
+        (slot == 0 ? e.x : e.y) = (int)(c.toff + c.p + x);
+      }
+    }
+  }
+  TLR_CUDA(ctx, cudaMemcpyAsync(d_cinv, cinv.data(), cinv.size() * sizeof(int2),
                                 cudaMemcpyHostToDevice, ctx->stream));
   TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   factored = true;
@@ -1105,39 +1118,32 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
   cudaStream_t st = ctx->stream;
   const C *P = static_cast<const C *>(pool);
   C *W = static_cast<C *>(work);
+  C *W2 = static_cast<C *>(work2);
   C *x = static_cast<C *>(xv);
   for (size_t h = 0; h < levels.size(); ++h) {
     const Level &L = levels[h];
     const int *fl = d_sched + L.fronts_off;
     { k_sgather<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(
-        fl, d_fronts, d_nodes, d_perm, x, W); count_launches(); }
-    for (int slot = 0; slot < 2; ++slot)
-      if (L.kids[slot])
-        { k_saddchild<C><<<dim3(blocks_for(std::max(L.kids_maxb[slot], 1), 128), L.kids[slot]),
-                         128, 0, st>>>(d_sched + L.kids_off[slot], d_fronts, d_pmap, W); count_launches(); }
+        fl, d_fronts, d_nodes, d_perm, d_cinv, x, W); count_launches(); }
     for (int b = 0; b < (int)L.blk_nf.size(); ++b) {
       const int rows = L.fwd_rows[b];
       if (rows > 0)
         { k_blk_update<C><<<dim3(blocks_for(rows, 32), L.blk_nf[b]), 256, 0, st>>>(
-            fl, b, 0, P, d_fronts, W); count_launches(); }
+            fl, b, 0, P, d_fronts, W, d_nodes, x); count_launches(); }
     }
   }
   for (int h = (int)levels.size() - 1; h >= 0; --h) {
     const Level &L = levels[h];
     const int *fl = d_sched + L.fronts_off;
-    { k_bgather<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(fl, d_fronts,
-                                                                             d_nodes, x, W); count_launches(); }
     if (L.bmax > 0)
       { k_border_gemv<C><<<dim3(blocks_for(L.pmax, 32), L.nck_b, L.nfronts), 256, 0, st>>>(
-          fl, P, d_fronts, W, d_partial, L.nck_b, L.pmax); count_launches(); }
-    { k_bwd_start<C><<<dim3((unsigned)L.blk_nf.size(), L.nfronts), 256, 0, st>>>(
-        fl, d_fronts, d_inv_off, static_cast<const C *>(dmat), W, d_partial, L.nck_b,
-        L.pmax); count_launches(); }
+          fl, P, d_fronts, d_nodes, x, d_partial, L.nck_b, L.pmax); count_launches(); }
+    { k_bwd_start<C><<<dim3((unsigned)L.blk_nf.size() * (kSW / 32), L.nfronts), 256, 0, st>>>(
+        fl, d_fronts, d_inv_off, static_cast<const C *>(dmat), W, W2, d_partial, L.nck_b,
+        L.pmax, d_nodes, x); count_launches(); }
     for (int b = (int)L.blk_nf.size() - 1; b >= 1; --b)
       { k_blk_update<C><<<dim3(blocks_for(b * kSW, 32), L.blk_nf[b]), 256, 0, st>>>(
-          fl, b, 1, P, d_fronts, W); count_launches(); }
-    { k_bscatter<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(fl, d_fronts,
-                                                                              d_nodes, W, x); count_launches(); }
+          fl, b, 1, P, d_fronts, W2, d_nodes, x); count_launches(); }
   }
   TLR_CUDA(ctx, cudaGetLastError());
   return TLR_OK;

@@ -34,11 +34,12 @@ struct Factor {
   int prec = 0;  // 0: complex128 fronts, 1: complex64 fronts
   int w = 32;    // panel width
   std::vector<Level> levels;
-  void *pool = nullptr, *work = nullptr, *vec_a = nullptr;
+  void *pool = nullptr, *work = nullptr, *work2 = nullptr, *vec_a = nullptr;
   DevFront *d_fronts = nullptr;
   AsmEntry *d_entries = nullptr;
   int *d_cmap = nullptr, *d_nodes = nullptr, *d_ipiv = nullptr, *d_perm = nullptr;
-  int *d_pmap = nullptr, *d_sched = nullptr, *d_pert = nullptr;
+  int *d_sched = nullptr, *d_pert = nullptr;
+  int2 *d_cinv = nullptr;  // child border rows mapped onto each front row
   // kSW x kSW diagonal blocks of every pivot block: inv(L_bb), inv(U_bb)
   // (scratch of the factor rewrite) and D_b = inv(U_bb) inv(L_bb)
   void *linv = nullptr, *uinv = nullptr, *dmat = nullptr;
