@@ -192,6 +192,9 @@ typedef struct {
   double sigma_re, sigma_im; /* used when use_sigma != 0                    */
   int use_sigma;          /* 0: sigma = lambda target from omega            */
   const double *start;    /* optional complex [5N] host start vector        */
+  int cuda_core_schur;    /* mixed form: 0 (default) Schur updates on the
+                             tensor cores (tcgen05, 3xTF32); 1 on the CUDA
+                             cores (FP32 FMA)                                */
 } tlr_solve_opts;
 
 typedef struct {
@@ -251,6 +254,16 @@ int tlr_frobenius_noalloc(const double *values, size_t count, double *result,
 /* The context's CUDA stream (cudaStream_t) -- all device work of the
  * context is ordered on it; callers time or synchronise against it. */
 void *tlr_stream(tlr_ctx *ctx);
+
+/* Test hook, no counterpart in the reference: one Schur-complement update
+ * F22 -= L21 U12 of a single dense complex64 front (m x m, column-major,
+ * interleaved re/im) for the panel columns [k0, k0 + min(w, p - k0)), on
+ * the tensor-core (tcgen05, 3xTF32) path the mixed factorisation uses.
+ * k0 must be a multiple of w, w <= 64.  lbo/sbo: shared-memory descriptor
+ * strides of the operand planes in bytes (0: the library's values).
+ * Writes the updated front to out. */
+int tlr_schur_update_c64(const float *front, int m, int p, int k0, int w, unsigned lbo,
+                         unsigned sbo, float *out);
 
 /* Kernels of this library launched by the process so far (every kernel
  * node of a replayed CUDA graph counts once per replay; cuBLAS kernels are

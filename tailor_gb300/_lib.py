@@ -74,7 +74,7 @@ class SolveOpts(ctypes.Structure):
                 ("tol", ctypes.c_double), ("max_it", ctypes.c_int),
                 ("precision", ctypes.c_int), ("sigma_re", ctypes.c_double),
                 ("sigma_im", ctypes.c_double), ("use_sigma", ctypes.c_int),
-                ("start", ctypes.c_void_p)]
+                ("start", ctypes.c_void_p), ("cuda_core_schur", ctypes.c_int)]
 
 
 class EigDiag(ctypes.Structure):
@@ -112,6 +112,7 @@ SIGNATURES = {
     "tlr_solve": ([_P, _P, _P, _P, _P, _P], _I),
     "tlr_stream": ([_P], ctypes.c_void_p),
     "tlr_kernel_launches": ([], ctypes.c_longlong),
+    "tlr_schur_update_c64": ([_P, _I, _I, _I, _I, ctypes.c_uint, ctypes.c_uint, _P], _I),
     "tlr_frobenius_noalloc": ([_P, ctypes.c_size_t, _P, _P], _I),
     "tlr_mlp_create": ([_I, _I, _I, _I, ctypes.c_ulonglong, _P], _I),
     "tlr_mlp_destroy": ([_P], None),

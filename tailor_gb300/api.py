@@ -211,13 +211,14 @@ class EigenSolver:
 
     def solve(self, nev: int = 0, ncv: int = 0, tol: float = 0.0,
               max_it: int = 0, precision: int = 0, sigma: complex | None = None,
-              start: np.ndarray | None = None, modes: bool = False) -> EigenSolution:
+              start: np.ndarray | None = None, modes: bool = False,
+              cuda_core_schur: bool = False) -> EigenSolution:
         ph = self.p.case.physics
         k = nev or ph.nev
         opts = L.SolveOpts(nev, ncv, tol, max_it, precision,
                            0.0 if sigma is None else complex(sigma).real,
                            0.0 if sigma is None else complex(sigma).imag,
-                           0 if sigma is None else 1, None)
+                           0 if sigma is None else 1, None, int(bool(cuda_core_schur)))
         if start is not None:
             s = np.ascontiguousarray(np.stack([start.real, start.imag], -1),
                                      dtype=np.float64)

@@ -145,6 +145,12 @@ struct CaptureScope {  // suppresses counting on this thread during capture
   ~CaptureScope();
 };
 
+struct DevFront;
+// Tensor-core Schur update of one panel step (tlr_tc.cu).
+int launch_gemm_tc(tlr_ctx *ctx, const int *fl, const int *prefix, int nf, int s, int w,
+                   float2 *pool, const DevFront *fr, int tiles, int *err, cudaStream_t st,
+                   uint32_t lbo = 128, uint32_t sbo = 256);
+
 inline int blocks_for(long long n, int threads) {
   return static_cast<int>((n + threads - 1) / threads);
 }

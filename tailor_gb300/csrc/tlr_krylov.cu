@@ -185,11 +185,12 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   const cd target(rcp.omega_im, -rcp.omega_re);
   const cd sigma = o.use_sigma ? cd(o.sigma_re, o.sigma_im) : target;
   const int prec = o.precision == 1 ? 1 : 0;
+  const bool tc = prec == 1 && !o.cuda_core_schur;
 
-  // factorisation (reused when sigma and precision are unchanged)
+  // factorisation (reused when sigma, precision and Schur kernel are unchanged)
   Factor *F = ctx->factor;
   if (F && (F->prec != prec || F->sigma_re != sigma.real() || F->sigma_im != sigma.imag() ||
-            !F->factored)) {
+            F->tensor_cores != tc || !F->factored)) {
     if (F->prec != prec) {
       free_factor(ctx);
       F = nullptr;
@@ -208,6 +209,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
       return rc;
     }
   }
+  F->tensor_cores = tc;
   if (!F->factored) {
     double anorm = 0.0;
     int rc = frobenius(ctx, ctx->A, ctx->nnzb * 25, &anorm);

@@ -933,6 +933,7 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
       (rc = alloc((void **)&d_sched, sched.size() * sizeof(int))) ||
       (rc = alloc((void **)&d_partial, (size_t)partial_elems * sizeof(double2))) ||
       (rc = alloc((void **)&d_pert, sizeof(int))) ||
+      (rc = alloc((void **)&d_tc_err, sizeof(int))) ||
       (rc = alloc(&linv, (size_t)inv_elems * csize)) ||
       (rc = alloc(&uinv, (size_t)inv_elems * csize)) ||
       (rc = alloc(&dmat, (size_t)inv_elems * csize)) ||
@@ -980,7 +981,7 @@ void Factor::release() {
   ev_used = 0;
   cudaFree(pool); cudaFree(work); cudaFree(d_fronts); cudaFree(d_entries);
   cudaFree(d_cmap); cudaFree(d_nodes); cudaFree(d_ipiv); cudaFree(d_perm);
-  cudaFree(d_cinv); cudaFree(work2); cudaFree(d_sched); cudaFree(d_partial); cudaFree(d_pert);
+  cudaFree(d_cinv); cudaFree(work2); cudaFree(d_sched); cudaFree(d_partial); cudaFree(d_pert); cudaFree(d_tc_err);
   cudaFree(vec_a); cudaFree(linv); cudaFree(uinv); cudaFree(dmat);
   cudaFree(d_inv_off); cudaFree(d_inv_blocks); cudaFree(d_ltiles); cudaFree(d_utiles);
   linv = uinv = dmat = nullptr;
@@ -997,6 +998,7 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
   cudaStream_t st = ctx->stream;
   C *P = static_cast<C *>(pool);
   TLR_CUDA(ctx, cudaMemsetAsync(d_pert, 0, sizeof(int), st));
+  TLR_CUDA(ctx, cudaMemsetAsync(d_tc_err, 0, sizeof(int), st));
   const size_t tsm = sizeof(C) * (size_t)(w * w + w);
   TLR_CUDA(ctx, cudaFuncSetAttribute(k_trsm_border<C>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
@@ -1030,9 +1032,16 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
         { k_trsm_urow<C><<<dim3(blocks_for(S.max_ext, 128), S.nf), 128, tsm, st>>>(fl, s, w, P,
                                                                                  d_fronts); count_launches(); }
         if (S.tiles > 0) {
-          if constexpr (sizeof(C) == sizeof(float2))
-            { k_gemm32<<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w,
-                                              reinterpret_cast<float2 *>(P), d_fronts); count_launches(); }
+          if constexpr (sizeof(C) == sizeof(float2)) {
+            if (tensor_cores) {
+              const int rc = launch_gemm_tc(ctx, fl, d_sched + S.prefix_off, S.nf, s, w,
+                                            reinterpret_cast<float2 *>(P), d_fronts, S.tiles,
+                                            d_tc_err, st);
+              if (rc) return rc;
+            } else
+              { k_gemm32<<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w,
+                                                reinterpret_cast<float2 *>(P), d_fronts); count_launches(); }
+          }
           else
             { k_gemm<C><<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w, P,
                                                d_fronts); count_launches(); }
@@ -1070,7 +1079,12 @@ int Factor::factor(tlr_ctx *ctx, double sr, double si, double tiny) {
                                 cudaMemcpyDeviceToHost, ctx->stream));
   TLR_CUDA(ctx, cudaMemcpyAsync(&perturbed, d_pert, sizeof(int), cudaMemcpyDeviceToHost,
                                 ctx->stream));
+  int tc_err = 0;
+  TLR_CUDA(ctx, cudaMemcpyAsync(&tc_err, d_tc_err, sizeof(int), cudaMemcpyDeviceToHost,
+                                ctx->stream));
   TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (tc_err)
+    return fail(ctx, TLR_ERR_CUDA, "tensor-core Schur update: an mbarrier wait timed out");
   const int nf = (int)sym.fronts.size();
   std::vector<int> inv;
   for (int t = 0; t < nf; ++t) {

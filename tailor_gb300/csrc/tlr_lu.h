@@ -32,6 +32,8 @@ struct Level {
 struct Factor {
   Symbolic sym;
   int prec = 0;  // 0: complex128 fronts, 1: complex64 fronts
+  bool tensor_cores = true;  // complex64 Schur updates on tcgen05 (3xTF32)
+  int *d_tc_err = nullptr;   // set by a tensor-core kernel whose wait timed out
   int w = 32;    // panel width
   std::vector<Level> levels;
   void *pool = nullptr, *work = nullptr, *work2 = nullptr, *vec_a = nullptr;

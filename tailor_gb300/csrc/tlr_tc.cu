@@ -1,0 +1,355 @@
+// tlr_tc.cu -- tensor-core (tcgen05) Schur-complement update of complex64
+// fronts: F22 -= L21 U12 for one panel step of every front of a level.
+//
+// A complex product is a real product of doubled inner dimension:
+//   A = [Lr | Li]            (128 rows  x 2K)
+//   B = [Ur ; -Ui] -> Cr     (first 64 "rows" of the N x 2K operand)
+//       [Ui ;  Ur] -> Ci     (last 64)
+// so one 128 x 128 x 2K real MMA chain yields [Cr | Ci] for a 128 x 64
+// complex tile.  FP32 accuracy on the TF32 pipe comes from the 3xTF32
+// split (x = hi + lo, both TF32): A_lo B_hi + A_hi B_lo + A_hi B_hi,
+// accumulated in FP32 in tensor memory.
+//
+// Per CTA (256 threads, one output tile): threads stage K chunks of 16
+// complex columns (32 real) as TF32 hi/lo planes in shared memory in the
+// canonical K-major no-swizzle layout (8-row x 16-byte core matrices),
+// double-buffered; one thread issues tcgen05.mma (M = 128, N = 128, K = 8)
+// and commits each chunk to an mbarrier; the accumulator lives in 128 TMEM
+// columns and is read back with tcgen05.ld for the F22 -= epilogue.  Every
+// mbarrier wait is bounded: on timeout the kernel records an error, waits
+// (bounded) once more, frees its TMEM and returns.
+#include <algorithm>
+#include <cstdint>
+
+#include "tlr_complex.cuh"
+#include "tlr_internal.h"
+#include "tlr_lu.h"
+
+namespace tlr {
+namespace {
+
+constexpr int kTcM = 128;      // complex rows per tile
+constexpr int kTcN = 64;       // complex columns per tile
+constexpr int kTcKC = 8;       // complex K columns per stage (16 real: re | im)
+constexpr int kPlane = 8192;   // bytes of one 128 x 16 TF32 operand plane
+constexpr int kStage = 4 * kPlane;  // A_hi, A_lo, B_hi, B_lo
+constexpr int kTmemCols = 128;
+constexpr unsigned kWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// byte offset of element (row, kk) of a 128 x 16 K-major plane: k-step
+// kk/8 owns 4 KB; inside, 8-row group g at 256 g, the two core matrices of
+// the k-step at +0 / +128, row r % 8 at 16 (r % 8), element kk % 4 at 4 (kk % 4)
+__device__ __forceinline__ uint32_t plane_off(int row, int kk) {
+  return (uint32_t)((kk >> 3) * 4096 + (row >> 3) * 256 + ((kk >> 2) & 1) * 128 + (row & 7) * 16 +
+                    (kk & 3) * 4);
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// kind::tf32, D f32, A/B tf32 K-major, M = 128, N = 128
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 3) << 17) |
+                            ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  for (unsigned it = 0; it < kWaitLimit; ++it)
+    if (mbar_test(bar, parity)) return true;
+  return false;
+}
+
+#define TLR_TC_LD16(taddr, r)                                                                    \
+  asm volatile(                                                                                  \
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14," \
+      "%15}, [%16];"                                                                             \
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),     \
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),              \
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])                                                    \
+      : "r"(taddr))
+
+__global__ void __launch_bounds__(256)
+    k_gemm_tc(const int *__restrict__ fl, const int *__restrict__ prefix, int nf, int s, int w,
+              float2 *__restrict__ pool, const DevFront *__restrict__ fr, int *__restrict__ err,
+              uint32_t lbo, uint32_t sbo) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int wait_ok;
+  unsigned char *stage0 =
+      tc_smem + ((1024 - (smem_addr(tc_smem) & 1023)) & 1023);  // 1 KB aligned
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  // tile decode (same schedule as the CUDA-core kernel: 128 x 64 tiles)
+  const int t = blockIdx.x;
+  int lo = 0, hi = nf;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) / 2;
+    if (prefix[mid] <= t) lo = mid; else hi = mid;
+  }
+  const DevFront f = fr[fl[lo]];
+  const int m = f.m, k0 = s * w, ww = min(w, f.p - k0);
+  const int base = k0 + ww, ext = m - base;
+  const int ntm = (ext + kTcM - 1) / kTcM;
+  const int lt = t - prefix[lo];
+  const int R0 = base + (lt % ntm) * kTcM, C0 = base + (lt / ntm) * kTcN;
+  float2 *F = pool + f.off;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(&tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  const int nch = (ww + kTcKC - 1) / kTcKC;
+  // A: thread (row ar, quad aq) stages complex columns 4 aq .. 4 aq + 3 of
+  // the chunk; B: thread (column bn, quad bq) stages K rows 4 bq .. 4 bq + 3
+  // (threads 128..255 take the second 64 of nothing: B has 64 x 2 quads).
+  const int ar = tid & (kTcM - 1), aq = tid >> 7;
+  const int bn = tid & 63, bq = (tid >> 6) & 1;
+  const bool bact = tid < 128;
+  float2 va[4], vb[4];
+  auto load = [&](int c) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int kc = c * kTcKC + 4 * aq + j;
+      va[j] = (R0 + ar < m && kc < ww) ? F[(long long)(k0 + kc) * m + R0 + ar]
+                                        : make_float2(0.f, 0.f);
+      const int kb = c * kTcKC + 4 * bq + j;
+      vb[j] = (bact && C0 + bn < m && kb < ww) ? F[(long long)(C0 + bn) * m + k0 + kb]
+                                               : make_float2(0.f, 0.f);
+    }
+  };
+  auto split4 = [](const float *x, uint4 &hi4, uint4 &lo4) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      h[j] = to_tf32(x[j]);
+      l[j] = to_tf32(x[j] - __uint_as_float(h[j]));
+    }
+    hi4 = make_uint4(h[0], h[1], h[2], h[3]);
+    lo4 = make_uint4(l[0], l[1], l[2], l[3]);
+  };
+  auto store = [&](unsigned char *st) {
+    float re[4], im[4];
+    uint4 h, l;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { re[j] = va[j].x; im[j] = va[j].y; }
+    // A row ar: K' 4 aq .. +3 = Lr, K' 8 + 4 aq .. +3 = Li
+    split4(re, h, l);
+    *reinterpret_cast<uint4 *>(st + plane_off(ar, 4 * aq)) = h;
+    *reinterpret_cast<uint4 *>(st + kPlane + plane_off(ar, 4 * aq)) = l;
+    split4(im, h, l);
+    *reinterpret_cast<uint4 *>(st + plane_off(ar, 8 + 4 * aq)) = h;
+    *reinterpret_cast<uint4 *>(st + kPlane + plane_off(ar, 8 + 4 * aq)) = l;
+    if (bact) {
+      unsigned char *bh = st + 2 * kPlane, *bl = st + 3 * kPlane;
+      float ur[4], ui[4], nui[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) { ur[j] = vb[j].x; ui[j] = vb[j].y; nui[j] = -vb[j].y; }
+      // Cr row bn: [Ur ; -Ui]; Ci row 64 + bn: [Ui ; Ur]
+      split4(ur, h, l);
+      *reinterpret_cast<uint4 *>(bh + plane_off(bn, 4 * bq)) = h;
+      *reinterpret_cast<uint4 *>(bl + plane_off(bn, 4 * bq)) = l;
+      *reinterpret_cast<uint4 *>(bh + plane_off(64 + bn, 8 + 4 * bq)) = h;
+      *reinterpret_cast<uint4 *>(bl + plane_off(64 + bn, 8 + 4 * bq)) = l;
+      split4(nui, h, l);
+      *reinterpret_cast<uint4 *>(bh + plane_off(bn, 8 + 4 * bq)) = h;
+      *reinterpret_cast<uint4 *>(bl + plane_off(bn, 8 + 4 * bq)) = l;
+      split4(ui, h, l);
+      *reinterpret_cast<uint4 *>(bh + plane_off(64 + bn, 4 * bq)) = h;
+      *reinterpret_cast<uint4 *>(bl + plane_off(64 + bn, 4 * bq)) = l;
+    }
+  };
+  bool ok = true;
+  if (nch > 0) load(0);
+  for (int c = 0; c < nch; ++c) {
+    const int sb = c & 1;
+    unsigned char *st = stage0 + sb * kStage;
+    if (c >= 2) {  // the MMAs of chunk c - 2 read this buffer
+      if (tid == 0) wait_ok = mbar_wait(&bars[sb], ((c - 2) >> 1) & 1);
+      __syncthreads();
+      if (!wait_ok) {
+        ok = false;
+        break;
+      }
+    }
+    store(st);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a_hi = smem_addr(st), a_lo = a_hi + kPlane;
+      const uint32_t b_hi = a_hi + 2 * kPlane, b_lo = a_hi + 3 * kPlane;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const uint32_t o = j * 4096;
+        const uint32_t acc0 = (c > 0 || j > 0) ? 1u : 0u;
+        mma_tf32(tmem, smem_desc(a_lo + o, lbo, sbo), smem_desc(b_hi + o, lbo, sbo), acc0);
+        mma_tf32(tmem, smem_desc(a_hi + o, lbo, sbo), smem_desc(b_lo + o, lbo, sbo), 1u);
+        mma_tf32(tmem, smem_desc(a_hi + o, lbo, sbo), smem_desc(b_hi + o, lbo, sbo), 1u);
+      }
+      mma_commit(&bars[sb]);
+    }
+    if (c + 1 < nch) load(c + 1);  // next chunk's loads overlap these MMAs
+  }
+  if (tid == 0) {
+    // the last commit covers every MMA of the tile
+    int fine = ok && nch > 0 ? mbar_wait(&bars[(nch - 1) & 1], ((nch - 1) >> 1) & 1) : ok;
+    if (!fine) {
+      atomicExch(err, 1);
+      // let any MMA still in flight land before the memory is released
+      if (nch > 0) mbar_wait(&bars[(nch - 1) & 1], ((nch - 1) >> 1) & 1);
+    }
+    wait_ok = fine;
+  }
+  __syncthreads();
+  ok = wait_ok != 0;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+  if (ok) {
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (tile rows), column
+    // half w / 4 of Cr (TMEM columns 0..63) and Ci (64..127)
+    const int q = warp & 3, h = warp >> 2;
+    const int row = 32 * q + (tid & 31);
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+      uint32_t cr[16], ci[16];
+      const int n0 = 32 * h + 16 * part;
+      TLR_TC_LD16(lane_addr + n0, cr);
+      TLR_TC_LD16(lane_addr + 64 + n0, ci);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (R0 + row < m) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int n = n0 + j;
+          if (C0 + n < m) {
+            float2 &d = F[(long long)(C0 + n) * m + R0 + row];
+            d.x -= __uint_as_float(cr[j]);
+            d.y -= __uint_as_float(ci[j]);
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols));
+}
+
+}  // namespace
+
+size_t gemm_tc_smem() { return 2 * kStage + 1024; }
+
+int launch_gemm_tc(tlr_ctx *ctx, const int *fl, const int *prefix, int nf, int s, int w,
+                   float2 *pool, const DevFront *fr, int tiles, int *err, cudaStream_t st,
+                   uint32_t lbo, uint32_t sbo) {
+  TLR_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)gemm_tc_smem()));
+  { k_gemm_tc<<<tiles, 256, gemm_tc_smem(), st>>>(fl, prefix, nf, s, w, pool, fr, err, lbo, sbo); count_launches(); }
+  return TLR_OK;
+}
+
+}  // namespace tlr
+
+// ---------------------------------------------------------------- test hook
+extern "C" int tlr_schur_update_c64(const float *front, int m, int p, int k0, int w,
+                                    unsigned lbo, unsigned sbo, float *out) {
+  using namespace tlr;
+  if (!front || !out || m <= 0 || p <= 0 || p > m || k0 < 0 || k0 >= p || w <= 0 || w > 64 ||
+      k0 % w != 0)
+    return TLR_ERR_ARG;
+  if (lbo == 0) lbo = 128;
+  if (sbo == 0) sbo = 256;
+  const int ww = std::min(w, p - k0), base = k0 + ww, ext = m - base;
+  const size_t bytes = (size_t)m * m * sizeof(float2);
+  float2 *F = nullptr;
+  DevFront *fr = nullptr;
+  int *ints = nullptr;  // fl[1], prefix[2], err[1]
+  int rc = TLR_OK;
+  cudaStream_t st = nullptr;
+  const int tiles = ext > 0 ? ((ext + kTcM - 1) / kTcM) * ((ext + kTcN - 1) / kTcN) : 0;
+  DevFront h{};
+  h.off = 0;
+  h.toff = 0;
+  h.cmap_off = 0;
+  h.p = p;
+  h.m = m;
+  h.parent = -1;
+  h.node_off = 0;
+  const int hi[4] = {0, 0, tiles, 0};
+  int herr = 0;
+  if (cudaMalloc(&F, bytes) != cudaSuccess || cudaMalloc(&fr, sizeof(DevFront)) != cudaSuccess ||
+      cudaMalloc(&ints, 4 * sizeof(int)) != cudaSuccess || cudaStreamCreate(&st) != cudaSuccess) {
+    rc = TLR_ERR_NOMEM;
+  } else if (cudaMemcpy(F, front, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+             cudaMemcpy(fr, &h, sizeof(h), cudaMemcpyHostToDevice) != cudaSuccess ||
+             cudaMemcpy(ints, hi, sizeof(hi), cudaMemcpyHostToDevice) != cudaSuccess) {
+    rc = TLR_ERR_CUDA;
+  } else {
+    if (tiles > 0) {
+      cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)gemm_tc_smem());
+      { k_gemm_tc<<<tiles, 256, gemm_tc_smem(), st>>>(ints, ints + 1, 1, k0 / w, w, F, fr, ints + 3, lbo, sbo); count_launches(); }
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess ||
+        cudaMemcpy(out, F, bytes, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(&herr, ints + 3, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = TLR_ERR_CUDA;
+    else if (herr)
+      rc = TLR_ERR_CUDA;
+  }
+  cudaFree(F);
+  cudaFree(fr);
+  cudaFree(ints);
+  if (st) cudaStreamDestroy(st);
+  return rc;
+}
