@@ -14,7 +14,7 @@
 //   k_gemm         trailing update F22 -= L21 U12 (the Schur complement)
 // Pivot search is restricted to fully summed rows (no delayed pivots); an
 // exactly zero pivot column is perturbed and counted, and the caller
-// refines.  After the last level every pivot block's kSW x kSW diagonal
+// refines.  After the last level every pivot block's SW x SW diagonal
 // blocks are inverted explicitly (k_tri_inv), so each solve step is a
 // parallel GEMV plus one small dense product instead of a serial
 // substitution; the solves walk the same levels.
@@ -443,7 +443,7 @@ __global__ void k_sgather(const int *__restrict__ fl, const DevFront *__restrict
 
 // ---- block-scaled triangular solves ---------------------------------------
 // After factorisation each front's pivot block is cut into diagonal blocks
-// of kSW rows.  With Dl = blockdiag(L_bb) and Du = blockdiag(U_bb), the
+// of SW rows (SW = 128 or 256).  With Dl = blockdiag(L_bb) and Du = blockdiag(U_bb), the
 // factors are rewritten in place as L' = L Dl^-1 (every block column right-
 // multiplied by inv(L_bb), border rows included) and U' = Du^-1 U (every
 // block row left-multiplied by inv(U_bb), border columns included), and
@@ -463,19 +463,19 @@ __global__ void k_sgather(const int *__restrict__ fl, const DevFront *__restrict
 // (column-oriented substitution).  Stored column-major, leading dim nb.
 constexpr int kIC = 32;
 
-template <class C>
-__global__ void __launch_bounds__(kSW)
+template <class C, int SW>
+__global__ void __launch_bounds__(SW)
     k_tri_inv(const int2 *__restrict__ blocks, const C *__restrict__ pool,
               const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
               C *__restrict__ Linv, C *__restrict__ Uinv) {
   __shared__ C rowq[kIC];
   const int2 fb = blocks[blockIdx.x];
   const DevFront f = fr[fb.x];
-  const int b0 = fb.y * kSW, nb = min(kSW, f.p - b0);
+  const int b0 = fb.y * SW, nb = min(SW, f.p - b0);
   const C *F = pool + f.off + (long long)b0 * f.m + b0;  // F[c * m + r] = K_bb(r, c)
   const int m = f.m, r = threadIdx.x;
   const bool lower = blockIdx.y == 0;
-  C *out = (lower ? Linv : Uinv) + inv_off[fb.x] + (long long)fb.y * kSW * kSW;
+  C *out = (lower ? Linv : Uinv) + inv_off[fb.x] + (long long)fb.y * SW * SW;
   for (int c0 = 0; c0 < nb; c0 += kIC) {
     C x[kIC];
 #pragma unroll
@@ -525,16 +525,16 @@ __global__ void __launch_bounds__(kSW)
 // tiles: {front, block c, first row, -}.
 constexpr int kRT = 32;
 
-template <class C>
+template <class C, int SW>
 __global__ void __launch_bounds__(256)
     k_scale_l(const int4 *__restrict__ tiles, C *__restrict__ pool,
               const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
               const C *__restrict__ Linv) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C *As = reinterpret_cast<C *>(smem_raw);  // [kSW][kRT], As[q * kRT + r]
+  C *As = reinterpret_cast<C *>(smem_raw);  // [SW][kRT], As[q * kRT + r]
   const int4 tl = tiles[blockIdx.x];
   const DevFront f = fr[tl.x];
-  const int c0 = tl.y * kSW, nb = min(kSW, f.p - c0);
+  const int c0 = tl.y * SW, nb = min(SW, f.p - c0);
   const int r0 = tl.z, nr = min(kRT, f.m - r0);
   C *F = pool + f.off;
   for (int x = threadIdx.x; x < nb * kRT; x += blockDim.x) {
@@ -542,43 +542,43 @@ __global__ void __launch_bounds__(256)
     As[x] = r < nr ? F[(long long)(c0 + q) * f.m + r0 + r] : czero<C>();
   }
   __syncthreads();
-  const C *Li = Linv + inv_off[tl.x] + (long long)tl.y * kSW * kSW;  // (q, j) at j nb + q
+  const C *Li = Linv + inv_off[tl.x] + (long long)tl.y * SW * SW;  // (q, j) at j nb + q
   const int r = threadIdx.x & (kRT - 1), g = threadIdx.x / kRT;
-  C acc[kSW / 8];
+  C acc[SW / 8];
 #pragma unroll
-  for (int k = 0; k < kSW / 8; ++k) acc[k] = czero<C>();
+  for (int k = 0; k < SW / 8; ++k) acc[k] = czero<C>();
   for (int q = 0; q < nb; ++q) {
     const C a = As[q * kRT + r];
 #pragma unroll
-    for (int k = 0; k < kSW / 8; ++k) {
+    for (int k = 0; k < SW / 8; ++k) {
       const int j = g + 8 * k;
       if (j <= q) acc[k] = cfma(acc[k], a, Li[(long long)j * nb + q]);
     }
   }
   if (r < nr)
 #pragma unroll
-    for (int k = 0; k < kSW / 8; ++k) {
+    for (int k = 0; k < SW / 8; ++k) {
       const int j = g + 8 * k;
       if (j < nb) F[(long long)(c0 + j) * f.m + r0 + r] = acc[k];
     }
 }
 
 // Left product by inv(U_bb), in place over a tile of 32 columns (staged in
-// shared memory before any write); thread (row i, half h) forms columns
-// h, h+2, ... of row i.  tiles: {front, block b, first column, kind}:
+// shared memory before any write); thread (row i, group h of the 256 / SW
+// groups) forms columns h, h + 256 / SW, ... of row i.  tiles: {front, block b, first column, kind}:
 //   kind 0: U'(b rows, cols) = inv(U_bb) U(b rows, cols) inside the front;
 //   kind 1: D_b(:, cols) = inv(U_bb) inv(L_bb)(:, cols) into dmat.
-template <class C>
+template <class C, int SW>
 __global__ void __launch_bounds__(256)
     k_scale_u(const int4 *__restrict__ tiles, C *__restrict__ pool,
               const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
               const C *__restrict__ Linv, const C *__restrict__ Uinv, C *__restrict__ dmat) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C *As = reinterpret_cast<C *>(smem_raw);  // [kSW][kRT], As[q * kRT + cc]
+  C *As = reinterpret_cast<C *>(smem_raw);  // [SW][kRT], As[q * kRT + cc]
   const int4 tl = tiles[blockIdx.x];
   const DevFront f = fr[tl.x];
-  const int b0 = tl.y * kSW, nb = min(kSW, f.p - b0);
-  const long long io = inv_off[tl.x] + (long long)tl.y * kSW * kSW;
+  const int b0 = tl.y * SW, nb = min(SW, f.p - b0);
+  const long long io = inv_off[tl.x] + (long long)tl.y * SW * SW;
   const C *src;
   C *dst;
   long long ld, ncol;
@@ -600,19 +600,20 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   const C *Ui = Uinv + io;  // (i, q) at q nb + i, upper triangular
-  const int i = threadIdx.x & (kSW - 1), h = threadIdx.x / kSW;
-  C acc[kRT / 2];
+  constexpr int H = 256 / SW;  // column groups over the 256 threads
+  const int i = threadIdx.x & (SW - 1), h = threadIdx.x / SW;
+  C acc[kRT / H];
 #pragma unroll
-  for (int k = 0; k < kRT / 2; ++k) acc[k] = czero<C>();
+  for (int k = 0; k < kRT / H; ++k) acc[k] = czero<C>();
   if (i < nb) {
     for (int q = i & ~31; q < nb; ++q) {
       const C u = q >= i ? Ui[(long long)q * nb + i] : czero<C>();
 #pragma unroll
-      for (int k = 0; k < kRT / 2; ++k) acc[k] = cfma(acc[k], u, As[q * kRT + h + 2 * k]);
+      for (int k = 0; k < kRT / H; ++k) acc[k] = cfma(acc[k], u, As[q * kRT + h + H * k]);
     }
 #pragma unroll
-    for (int k = 0; k < kRT / 2; ++k) {
-      const int cc = h + 2 * k;
+    for (int k = 0; k < kRT / H; ++k) {
+      const int cc = h + H * k;
       if (cc < nc) dst[(long long)(col0 + cc) * ld + i] = acc[k];
     }
   }
@@ -620,18 +621,18 @@ __global__ void __launch_bounds__(256)
 
 // One solve step of every front of the level that owns block b: rows
 // [lo, hi) take t[r] -= F(r, b0:b1) t[b0:b1] (forward: lo = b1, hi = m;
-// backward: lo = 0, hi = b0).  CTA = 32 rows x 8 warps of kSW/8 columns.
+// backward: lo = 0, hi = b0).  CTA = 32 rows x 8 warps of SW/8 columns.
 // Backward steps run on the pivot-row vector of the backward pass; rows of
 // block b-1 are final after step b and are written to the solution x.
-template <class C>
+template <class C, int SW>
 __global__ void __launch_bounds__(256)
     k_blk_update(const int *__restrict__ fl, int b, int backward, const C *__restrict__ pool,
                  const DevFront *__restrict__ fr, C *__restrict__ work,
                  const int *__restrict__ nodes, C *__restrict__ x) {
-  __shared__ C vs[kSW];
+  __shared__ C vs[SW];
   __shared__ C red[8][32];
   const DevFront f = fr[fl[blockIdx.y]];
-  const int b0 = b * kSW, b1 = min(f.p, b0 + kSW), nb = b1 - b0;
+  const int b0 = b * SW, b1 = min(f.p, b0 + SW), nb = b1 - b0;
   const int lo = backward ? 0 : b1, hi = backward ? b0 : f.m;
   const int r0 = lo + blockIdx.x * 32;
   if (nb <= 0 || r0 >= hi) return;
@@ -640,7 +641,7 @@ __global__ void __launch_bounds__(256)
   const int r = r0 + lane;
   const C *F = pool + f.off + (long long)b0 * f.m;
   // the matrix loads go out before the vector is staged (independent)
-  constexpr int kQ = kSW / 8;
+  constexpr int kQ = SW / 8;
   const int q0 = wp * kQ;
   C fv[kQ];
 #pragma unroll
@@ -659,7 +660,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int k = 0; k < 8; ++k) v = csub(v, red[k][lane]);
     t[r] = v;
-    if (backward && r >= b0 - kSW) x[(long long)nodes[f.node_off + r / 5] * 5 + r % 5] = v;
+    if (backward && r >= b0 - SW) x[(long long)nodes[f.node_off + r / 5] * 5 + r % 5] = v;
   }
 }
 
@@ -710,25 +711,25 @@ __global__ void __launch_bounds__(256)
 // (32 per CTA) take w = D_b z_b minus the border chunks of pass 1 (summed
 // in chunk order), written to the backward vector (z stays in work for the
 // other CTAs of the block).  The last block's rows are final and go to x.
-template <class C>
+template <class C, int SW>
 __global__ void __launch_bounds__(256)
     k_bwd_start(const int *__restrict__ fl, const DevFront *__restrict__ fr,
                 const long long *__restrict__ inv_off, const C *__restrict__ dmat,
                 const C *__restrict__ work, C *__restrict__ work2,
                 const double2 *__restrict__ partial, int nck, int pmax,
                 const int *__restrict__ nodes, C *__restrict__ x) {
-  __shared__ C zs[kSW];
+  __shared__ C zs[SW];
   __shared__ C red[8][32];
   const int fq = blockIdx.y, fid = fl[fq];
   const DevFront f = fr[fid];
-  const int blk = blockIdx.x / (kSW / 32), quarter = blockIdx.x % (kSW / 32);
-  const int b0 = blk * kSW, nb = min(kSW, f.p - b0);
+  const int blk = blockIdx.x / (SW / 32), quarter = blockIdx.x % (SW / 32);
+  const int b0 = blk * SW, nb = min(SW, f.p - b0);
   const int rr0 = quarter * 32;
   if (nb <= 0 || rr0 >= nb) return;
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const int rr = rr0 + lane;  // row inside the block
-  const C *Dm = dmat + inv_off[fid] + (long long)blk * kSW * kSW;
-  constexpr int kQ = kSW / 8;
+  const C *Dm = dmat + inv_off[fid] + (long long)blk * SW * SW;
+  constexpr int kQ = SW / 8;
   const int q0 = wp * kQ;
   C dv[kQ];
 #pragma unroll
@@ -757,7 +758,7 @@ __global__ void __launch_bounds__(256)
     }
     w = csub(w, from64<C>(s));
     work2[f.toff + r] = w;
-    if (b0 + kSW >= f.p) x[(long long)nodes[f.node_off + r / 5] * 5 + r % 5] = w;
+    if (b0 + SW >= f.p) x[(long long)nodes[f.node_off + r / 5] * 5 + r % 5] = w;
   }
 }
 
@@ -768,6 +769,7 @@ __global__ void __launch_bounds__(256)
 int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
   prec = precision;
   w = precision == 0 ? 32 : 64;
+  sw = precision == 0 ? 128 : 256;
   std::vector<int> rp(ctx->nn + 1), cl((size_t)ctx->nnzb);
   TLR_CUDA(ctx, cudaMemcpy(rp.data(), ctx->row_ptr, rp.size() * sizeof(int),
                            cudaMemcpyDeviceToHost));
@@ -875,13 +877,13 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
     L.nck_b = std::max(1, (L.bmax + kBC - 1) / kBC);
     L.blk_nf.clear();
     L.fwd_rows.clear();
-    for (int b = 0; b * kSW < L.pmax; ++b) {
+    for (int b = 0; b * sw < L.pmax; ++b) {
       int n = 0, rows = 0;
       for (int q = 0; q < L.nfronts; ++q) {
         const FrontInfo &f = sym.fronts[sched[L.fronts_off + q]];
-        if (f.p > b * kSW) {
+        if (f.p > b * sw) {
           ++n;
-          rows = std::max(rows, f.m - std::min(f.p, (b + 1) * kSW));
+          rows = std::max(rows, f.m - std::min(f.p, (b + 1) * sw));
         }
       }
       L.blk_nf.push_back(n);
@@ -889,7 +891,7 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
     }
     partial_elems = std::max(partial_elems, (long long)L.nfronts * L.nck_b * std::max(L.pmax, 1));
   }
-  // diagonal blocks (full blocks kSW x kSW, the last one nb x nb) and the
+  // diagonal blocks (full blocks sw x sw, the last one nb x nb) and the
   // tiles of the factor rewrite L' = L Dl^-1, U' = Du^-1 U, D = Du^-1 Dl^-1
   std::vector<long long> inv_off(nf);
   std::vector<int2> inv_blocks;
@@ -898,8 +900,8 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
   for (int t = 0; t < nf; ++t) {
     const int p = sym.fronts[t].p, m = sym.fronts[t].m;
     inv_off[t] = inv_elems;
-    for (int b = 0; b * kSW < p; ++b) {
-      const int b1 = std::min(p, (b + 1) * kSW), nb = b1 - b * kSW;
+    for (int b = 0; b * sw < p; ++b) {
+      const int b1 = std::min(p, (b + 1) * sw), nb = b1 - b * sw;
       inv_blocks.push_back(make_int2(t, b));
       inv_elems += (long long)nb * nb;
       for (int r = b1; r < m; r += kRT) ltiles.push_back(make_int4(t, b, r, 0));
@@ -993,6 +995,27 @@ void Factor::release() {
   pool = work = work2 = vec_a = nullptr;
 }
 
+template <class C, int SW>
+int Factor::rewrite_factors(tlr_ctx *ctx) {
+  cudaStream_t st = ctx->stream;
+  C *P = static_cast<C *>(pool);
+  C *Li = static_cast<C *>(linv), *Ui = static_cast<C *>(uinv);
+  { k_tri_inv<C, SW><<<dim3(n_inv_blocks, 2), SW, 0, st>>>(d_inv_blocks, P, d_fronts, d_inv_off,
+                                                          Li, Ui); count_launches(); }
+  const size_t ssm = sizeof(C) * SW * kRT;
+  TLR_CUDA(ctx, cudaFuncSetAttribute(k_scale_u<C, SW>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+  TLR_CUDA(ctx, cudaFuncSetAttribute(k_scale_l<C, SW>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+  if (n_utiles > 0)
+    { k_scale_u<C, SW><<<(unsigned)n_utiles, 256, ssm, st>>>(d_utiles, P, d_fronts, d_inv_off, Li,
+                                                            Ui, static_cast<C *>(dmat)); count_launches(); }
+  if (n_ltiles > 0)
+    { k_scale_l<C, SW><<<(unsigned)n_ltiles, 256, ssm, st>>>(d_ltiles, P, d_fronts, d_inv_off,
+                                                            Li); count_launches(); }
+  return TLR_OK;
+}
+
 template <class C>
 int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
   cudaStream_t st = ctx->stream;
@@ -1050,20 +1073,12 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
     }
   }
   if (n_inv_blocks > 0) {
-    C *Li = static_cast<C *>(linv), *Ui = static_cast<C *>(uinv);
-    { k_tri_inv<C><<<dim3(n_inv_blocks, 2), kSW, 0, st>>>(d_inv_blocks, P, d_fronts, d_inv_off,
-                                                         Li, Ui); count_launches(); }
-    const size_t ssm = sizeof(C) * kSW * kRT;
-    TLR_CUDA(ctx, cudaFuncSetAttribute(k_scale_u<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)ssm));
-    TLR_CUDA(ctx, cudaFuncSetAttribute(k_scale_l<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)ssm));
-    if (n_utiles > 0)
-      { k_scale_u<C><<<(unsigned)n_utiles, 256, ssm, st>>>(d_utiles, P, d_fronts, d_inv_off, Li,
-                                                           Ui, static_cast<C *>(dmat)); count_launches(); }
-    if (n_ltiles > 0)
-      { k_scale_l<C><<<(unsigned)n_ltiles, 256, ssm, st>>>(d_ltiles, P, d_fronts, d_inv_off,
-                                                           Li); count_launches(); }
+    int rc;
+    if constexpr (sizeof(C) == sizeof(float2))
+      rc = sw == 256 ? rewrite_factors<C, 256>(ctx) : rewrite_factors<C, 128>(ctx);
+    else
+      rc = rewrite_factors<C, 128>(ctx);
+    if (rc) return rc;
   }
   TLR_CUDA(ctx, cudaGetLastError());
   return TLR_OK;
@@ -1127,7 +1142,7 @@ int Factor::factor(tlr_ctx *ctx, double sr, double si, double tiny) {
   return TLR_OK;
 }
 
-template <class C>
+template <class C, int SW>
 int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
   cudaStream_t st = ctx->stream;
   const C *P = static_cast<const C *>(pool);
@@ -1142,7 +1157,7 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
     for (int b = 0; b < (int)L.blk_nf.size(); ++b) {
       const int rows = L.fwd_rows[b];
       if (rows > 0)
-        { k_blk_update<C><<<dim3(blocks_for(rows, 32), L.blk_nf[b]), 256, 0, st>>>(
+        { k_blk_update<C, SW><<<dim3(blocks_for(rows, 32), L.blk_nf[b]), 256, 0, st>>>(
             fl, b, 0, P, d_fronts, W, d_nodes, x); count_launches(); }
     }
   }
@@ -1152,11 +1167,11 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
     if (L.bmax > 0)
       { k_border_gemv<C><<<dim3(blocks_for(L.pmax, 32), L.nck_b, L.nfronts), 256, 0, st>>>(
           fl, P, d_fronts, d_nodes, x, d_partial, L.nck_b, L.pmax); count_launches(); }
-    { k_bwd_start<C><<<dim3((unsigned)L.blk_nf.size() * (kSW / 32), L.nfronts), 256, 0, st>>>(
+    { k_bwd_start<C, SW><<<dim3((unsigned)L.blk_nf.size() * (SW / 32), L.nfronts), 256, 0, st>>>(
         fl, d_fronts, d_inv_off, static_cast<const C *>(dmat), W, W2, d_partial, L.nck_b,
         L.pmax, d_nodes, x); count_launches(); }
     for (int b = (int)L.blk_nf.size() - 1; b >= 1; --b)
-      { k_blk_update<C><<<dim3(blocks_for(b * kSW, 32), L.blk_nf[b]), 256, 0, st>>>(
+      { k_blk_update<C, SW><<<dim3(blocks_for(b * SW, 32), L.blk_nf[b]), 256, 0, st>>>(
           fl, b, 1, P, d_fronts, W2, d_nodes, x); count_launches(); }
   }
   TLR_CUDA(ctx, cudaGetLastError());
@@ -1172,7 +1187,9 @@ int Factor::solve(tlr_ctx *ctx, void *x) {
     int rc;
     {
       CaptureScope cs;
-      rc = prec == 0 ? solve_impl<double2>(ctx, vec_a) : solve_impl<float2>(ctx, vec_a);
+      rc = prec == 0 ? solve_impl<double2, 128>(ctx, vec_a)
+                     : (sw == 256 ? solve_impl<float2, 256>(ctx, vec_a)
+                                  : solve_impl<float2, 128>(ctx, vec_a));
     }
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(st, &g);

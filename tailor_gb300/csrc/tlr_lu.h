@@ -13,7 +13,6 @@ struct DevFront {
   int p, m, parent, node_off;
 };
 
-constexpr int kSW = 128;  // rows of a diagonal block of the solves (explicit inverses)
 
 struct Step {  // one panel step of one level
   int nf, max_m, max_b, max_ext, prefix_off, tiles;
@@ -25,7 +24,7 @@ struct Level {
   int kids[2] = {0, 0}, kids_off[2] = {0, 0}, kids_maxb[2] = {0, 0};
   long long entry_begin = 0, entry_end = 0, pool_begin = 0, pool_end = 0;
   std::vector<Step> steps;
-  std::vector<int> blk_nf;    // blk_nf[b]: fronts of the level with p > b kSW
+  std::vector<int> blk_nf;    // blk_nf[b]: fronts of the level with p > b sw
   std::vector<int> fwd_rows;  // rows below block b, largest over those fronts
 };
 
@@ -35,6 +34,7 @@ struct Factor {
   bool tensor_cores = true;  // complex64 Schur updates on tcgen05 (3xTF32)
   int *d_tc_err = nullptr;   // set by a tensor-core kernel whose wait timed out
   int w = 32;    // panel width
+  int sw = 128;  // rows of a diagonal block of the solves (128 or 256)
   std::vector<Level> levels;
   void *pool = nullptr, *work = nullptr, *work2 = nullptr, *vec_a = nullptr;
   DevFront *d_fronts = nullptr;
@@ -42,7 +42,7 @@ struct Factor {
   int *d_cmap = nullptr, *d_nodes = nullptr, *d_ipiv = nullptr, *d_perm = nullptr;
   int *d_sched = nullptr, *d_pert = nullptr;
   int2 *d_cinv = nullptr;  // child border rows mapped onto each front row
-  // kSW x kSW diagonal blocks of every pivot block: inv(L_bb), inv(U_bb)
+  // sw x sw diagonal blocks of every pivot block: inv(L_bb), inv(U_bb)
   // (scratch of the factor rewrite) and D_b = inv(U_bb) inv(L_bb)
   void *linv = nullptr, *uinv = nullptr, *dmat = nullptr;
   long long *d_inv_off = nullptr;
@@ -69,7 +69,8 @@ struct Factor {
   int solve(tlr_ctx *ctx, void *x);
 
   template <class C> int factor_impl(tlr_ctx *ctx, double sr, double si, double tiny);
-  template <class C> int solve_impl(tlr_ctx *ctx, void *x);
+  template <class C, int SW> int solve_impl(tlr_ctx *ctx, void *x);
+  template <class C, int SW> int rewrite_factors(tlr_ctx *ctx);
 };
 
 }  // namespace tlr
