@@ -209,6 +209,9 @@ typedef struct {
   double trisolve_ms;     /* device time of the triangular solves (CUDA
                              events around each solve graph)               */
   int trisolves;          /* triangular solves timed in trisolve_ms         */
+  double ortho_ms;        /* Gram-Schmidt of the Arnoldi steps (host clock) */
+  double dense_ms;        /* projected Schur problem on the host            */
+  double residual_ms;     /* Ritz vectors and explicit residuals            */
 } tlr_eig_diag;
 
 /* lambda [nev] complex, residual [nev]; modes [nev][5N] complex or NULL. */

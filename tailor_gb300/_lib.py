@@ -87,7 +87,9 @@ class EigDiag(ctypes.Structure):
                 ("factor_ms", ctypes.c_double), ("krylov_ms", ctypes.c_double),
                 ("total_ms", ctypes.c_double), ("factor_flops", ctypes.c_double),
                 ("solve_ms", ctypes.c_double), ("factor_bytes", ctypes.c_double),
-                ("trisolve_ms", ctypes.c_double), ("trisolves", ctypes.c_int)]
+                ("trisolve_ms", ctypes.c_double), ("trisolves", ctypes.c_int),
+                ("ortho_ms", ctypes.c_double), ("dense_ms", ctypes.c_double),
+                ("residual_ms", ctypes.c_double)]
 
 
 # Exported symbols and their signatures (argtypes, restype).

@@ -260,6 +260,7 @@ void tlr_ctx_destroy(tlr_ctx *ctx) {
   cudaFree(ctx->row_ptr); cudaFree(ctx->col); cudaFree(ctx->L); cudaFree(ctx->A);
   cudaFree(ctx->M); cudaFree(ctx->B); cudaFree(ctx->status); cudaFree(ctx->red);
   cudaFree(ctx->partial); cudaFree(ctx->bc_modes); cudaFree(ctx->bc_cond);
+  cudaFree(ctx->aff); cudaFree(ctx->wff);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -96,6 +96,10 @@ struct tlr_ctx {
   double *metrics = nullptr, *derivs = nullptr, *coef = nullptr;
   int *row_ptr = nullptr, *col = nullptr;
   double2 *L = nullptr, *M = nullptr, *A = nullptr, *B = nullptr;
+  // A_bc split into FP32 hi/lo pairs (re_hi, re_lo, im_hi, im_lo) for the
+  // float-float refinement residual; rebuilt when the operator changes
+  float4 *aff = nullptr, *wff = nullptr;  // wff: the iterate split the same way
+  bool aff_valid = false;
   int *status = nullptr;     // [ST_COUNT]
   double *red = nullptr;     // [RD_COUNT]
   double *partial = nullptr; // per-block partial sums for norms
@@ -129,6 +133,10 @@ int run_assemble(tlr_ctx *ctx, tlr_operator_diag *diag);
 int run_bc(tlr_ctx *ctx, tlr_bc_diag *diag);
 int run_spmv(tlr_ctx *ctx, int which, const double2 *x, double2 *y);
 int frobenius(tlr_ctx *ctx, const double2 *v, long long count, double *out);
+// r = y - (A_bc - sigma B_bc) w with A_bc w in float-float arithmetic on the
+// FP32 pipe (about 48-bit significands); builds ctx->aff on first use.
+int residual_ff(tlr_ctx *ctx, const double2 *y, const double2 *w, double sr, double si,
+                double2 *r);
 int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
               double *residual, double *modes, tlr_eig_diag *diag);
 void free_factor(tlr_ctx *ctx);

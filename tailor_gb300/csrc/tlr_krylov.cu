@@ -102,6 +102,17 @@ struct Solver {
     return rc;
   }
 
+  bool use_ff = true;  // float-float residuals between FP64 acceptance tests
+
+  // r = in - (A - sigma B) out in FP64
+  int residual64(const double2 *in, const double2 *out) {
+    int rc;
+    if ((rc = run_spmv(ctx, TLR_MAT_A, out, aw))) return rc;
+    if ((rc = run_spmv(ctx, TLR_MAT_B, out, bw))) return rc;
+    { k_residual<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, in, aw, bw, sr, si, r); count_launches(); }
+    return TLR_OK;
+  }
+
   int apply_inverse_impl(const double2 *in, double2 *out) {
     cudaStream_t st = ctx->stream;
     const int blocks = blocks_for(n, 256);
@@ -119,11 +130,26 @@ struct Solver {
     TLR_CUDA(ctx, cudaMemsetAsync(out, 0, n * sizeof(double2), st));
     { k_add32<<<blocks, 256, 0, st>>>(n, x32, out); count_launches(); }
     const double ny = nrm(in);
+    // Residuals in float-float (FP32 pipe) drive the corrections; the
+    // acceptance test is always an FP64 residual.  If the float-float
+    // residual stops decreasing (its rounding floor), switch to FP64.
+    bool ff = use_ff;
+    double prev = 0.0;
     for (int it = 0; it < max_refine; ++it) {
-      if ((rc = run_spmv(ctx, TLR_MAT_A, out, aw))) return rc;
-      if ((rc = run_spmv(ctx, TLR_MAT_B, out, bw))) return rc;
-      { k_residual<<<blocks, 256, 0, st>>>(n, in, aw, bw, sr, si, r); count_launches(); }
-      const double nr = nrm(r);
+      double nr;
+      if (ff) {
+        if ((rc = residual_ff(ctx, in, out, sr, si, r))) return rc;
+        nr = nrm(r);
+        if (it > 0 && nr > 0.5 * prev) ff = false;
+        prev = nr;
+        if (nr <= refine_tol * ny || !ff) {
+          if ((rc = residual64(in, out))) return rc;
+          nr = nrm(r);
+        }
+      } else {
+        if ((rc = residual64(in, out))) return rc;
+        nr = nrm(r);
+      }
       if (nr <= refine_tol * ny) break;
       { k_to32<<<blocks, 256, 0, st>>>(n, r, x32); count_launches(); }
       if ((rc = F->solve(ctx, x32))) return rc;
@@ -155,6 +181,7 @@ void fill_start(std::vector<double2> &v, unsigned long long seed) {
 }  // namespace
 
 void invalidate_factor(tlr_ctx *ctx) {
+  if (ctx) ctx->aff_valid = false;
   if (ctx && ctx->factor) ctx->factor->factored = false;
 }
 
@@ -267,7 +294,12 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   const int nout = nev;
   // Ritz vectors x_i = V Q y_i, lambda_i = sigma + 1/theta_i and explicit
   // relative residuals ||A x - lambda B x|| / (|lambda| ||x||).
+  double ortho_ms = 0.0, dense_ms = 0.0, residual_ms = 0.0;
+  auto ms_since = [](clock::time_point t) {
+    return std::chrono::duration<double, std::milli>(clock::now() - t).count();
+  };
   auto finalize = [&](const dense::Mat &Tq, const dense::Mat &Qq) -> int {
+    const auto tf = clock::now();
     std::vector<double2> yh((size_t)ncv * nout);
     for (int i = 0; i < nout; ++i) {
       const auto yv = dense::tri_eigvec(Tq, i);
@@ -305,6 +337,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
       residual[i] = res;
       maxerr = std::max(maxerr, res);
     }
+    residual_ms += ms_since(tf);
     return TLR_OK;
   };
   double tol_int = tol;
@@ -321,6 +354,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     for (int j = k; j < ncv; ++j) {
       int rc = S.op(S.V + (size_t)j * n, S.w);
       if (rc) return rc;
+      const auto to = clock::now();
       for (int pass = 0; pass < 2; ++pass) {
         cublasZgemv(S.h, CUBLAS_OP_C, (int)n, j + 1, &one, Vc(0), (int)n,
                     reinterpret_cast<cuDoubleComplex *>(S.w), 1, &zero,
@@ -341,8 +375,10 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
       TLR_CUDA(ctx, cudaMemcpyAsync(S.V + (size_t)(j + 1) * n, S.w, vb,
                                     cudaMemcpyDeviceToDevice, ctx->stream));
       cublasZdscal(S.h, (int)n, &inv, Vc(j + 1), 1);
+      ortho_ms += ms_since(to);
     }
     // projected problem: Schur form, wanted first
+    const auto td = clock::now();
     dense::Mat T(ncv, ncv), Q(ncv, ncv);
     for (int j = 0; j < ncv; ++j) {
       for (int i = 0; i < ncv; ++i) T(i, j) = H(i, j);
@@ -377,6 +413,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     };
     nconv = count_conv(tol_int);
     for (int i = 0; i < ncv; ++i) theta[i] = T(i, i);
+    dense_ms += ms_since(td);
     bool done = false;
     if (nconv >= nev) {
       int rc = finalize(T, Q);
@@ -450,6 +487,9 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     d.solve_ms = S.solve_ms;
     d.factor_bytes = (double)F->sym.factor_elems * (prec == 0 ? 16.0 : 8.0);
     d.trisolve_ms = F->take_solve_time(&d.trisolves);
+    d.ortho_ms = ortho_ms;
+    d.dense_ms = dense_ms;
+    d.residual_ms = residual_ms;
     *diag = d;
   }
   if (reason != 1) {

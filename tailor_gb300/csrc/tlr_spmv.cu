@@ -115,6 +115,116 @@ int run_spmv(tlr_ctx *ctx, int which, const double2 *x, double2 *y) {
   return TLR_OK;
 }
 
+namespace {
+
+// float-float helpers (Dekker/Knuth error-free transformations on FP32):
+// (hi, lo) += a * x with a = ah + al, x = xh + xl
+__device__ __forceinline__ void ff_mac(float &hi, float &lo, float ah, float al, float xh,
+                                       float xl) {
+  const float p = ah * xh;
+  const float e = fmaf(ah, xh, -p) + fmaf(ah, xl, al * xh);
+  const float s = hi + p;
+  const float bb = s - hi;
+  lo += ((hi - (s - bb)) + (p - bb)) + e;
+  hi = s;
+}
+
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float h2, float l2) {
+  const float s = hi + h2;
+  const float bb = s - hi;
+  lo = lo + l2 + ((hi - (s - bb)) + (h2 - bb));
+  hi = s;
+}
+
+__global__ void k_split_ff(long long n, const double2 *__restrict__ a, float4 *__restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 v = a[i];
+  const float rh = __double2float_rn(v.x), ih = __double2float_rn(v.y);
+  out[i] = make_float4(rh, __double2float_rn(v.x - (double)rh), ih,
+                       __double2float_rn(v.y - (double)ih));
+}
+
+// r = y - (A w - sigma B w): warp per block row, lane (r, c) = 5 r + c
+// accumulates the row's blocks in float-float; B (block diagonal) in FP64.
+__global__ void __launch_bounds__(32 * kRowsPerCta)
+    k_residual_ff(int nrows, const int *__restrict__ row_ptr, const int *__restrict__ col,
+                  const float4 *__restrict__ aff, const double2 *__restrict__ B,
+                  const float4 *__restrict__ wff, const double2 *__restrict__ w,
+                  const double2 *__restrict__ y, double sr, double si, double2 *__restrict__ r) {
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * kRowsPerCta + (threadIdx.x >> 5);
+  if (row >= nrows) return;
+  const int c = lane % 5;
+  const bool active = lane < 25;
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+  const int k0 = row_ptr[row], k1 = row_ptr[row + 1];
+  for (int k = k0; k < k1; k += 4) {
+    float4 a[4], xv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const bool ok = active && k + u < k1;
+      a[u] = ok ? __ldcs(aff + (size_t)(k + u) * 25 + lane) : make_float4(0.f, 0.f, 0.f, 0.f);
+      xv[u] = ok ? wff[(size_t)col[k + u] * 5 + c] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      // (ar + i ai)(xr + i xi), every part a float-float pair
+      ff_mac(rh, rl, a[u].x, a[u].y, xv[u].x, xv[u].y);
+      ff_mac(rh, rl, -a[u].z, -a[u].w, xv[u].z, xv[u].w);
+      ff_mac(ih, il, a[u].x, a[u].y, xv[u].z, xv[u].w);
+      ff_mac(ih, il, a[u].z, a[u].w, xv[u].x, xv[u].y);
+    }
+  }
+  // the five column lanes of block row rr = lane / 5
+#pragma unroll
+  for (int d = 1; d < 5; ++d) {
+    const float h1 = __shfl_down_sync(0xffffffffu, rh, d), l1 = __shfl_down_sync(0xffffffffu, rl, d);
+    const float h2 = __shfl_down_sync(0xffffffffu, ih, d), l2 = __shfl_down_sync(0xffffffffu, il, d);
+    if (c == 0 && d < 5) {
+      ff_add(rh, rl, h1, l1);
+      ff_add(ih, il, h2, l2);
+    }
+  }
+  // lanes 5 rr carry row rr's sums (shuffles above read lanes 5 rr + d, all in the same row)
+  if (active && c == 0) {
+    const int rr = lane / 5;
+    const size_t i = (size_t)row * 5 + rr;
+    double bx = 0.0, by = 0.0;
+    const double2 *Bb = B + (size_t)row * 25 + rr * 5;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      const double2 b = Bb[q], v = w[(size_t)row * 5 + q];
+      bx = fma(b.x, v.x, bx);
+      bx = fma(-b.y, v.y, bx);
+      by = fma(b.x, v.y, by);
+      by = fma(b.y, v.x, by);
+    }
+    const double ax = (double)rh + (double)rl, ay = (double)ih + (double)il;
+    const double2 yy = y[i];
+    r[i] = make_double2(yy.x - (ax - (sr * bx - si * by)), yy.y - (ay - (sr * by + si * bx)));
+  }
+}
+
+}  // namespace
+
+int residual_ff(tlr_ctx *ctx, const double2 *y, const double2 *w, double sr, double si,
+                double2 *r) {
+  const long long nv = ctx->nnzb * 25;
+  if (!ctx->aff) TLR_CUDA(ctx, cudaMalloc(&ctx->aff, (size_t)nv * sizeof(float4)));
+  const long long n = 5LL * ctx->nn;
+  if (!ctx->wff) TLR_CUDA(ctx, cudaMalloc(&ctx->wff, (size_t)n * sizeof(float4)));
+  if (!ctx->aff_valid) {
+    { k_split_ff<<<blocks_for(nv, 256), 256, 0, ctx->stream>>>(nv, ctx->A, ctx->aff); count_launches(); }
+    ctx->aff_valid = true;
+  }
+  { k_split_ff<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, w, ctx->wff); count_launches(); }
+  { k_residual_ff<<<blocks_for(ctx->nn, kRowsPerCta), 32 * kRowsPerCta, 0, ctx->stream>>>(
+      ctx->nn, ctx->row_ptr, ctx->col, ctx->aff, ctx->B, ctx->wff, w, y, sr, si, r); count_launches(); }
+  TLR_CUDA(ctx, cudaGetLastError());
+  return TLR_OK;
+}
+
 int frobenius(tlr_ctx *ctx, const double2 *v, long long count, double *out) {
   const int blocks = ctx->partial_blocks;
   { k_sq2_partial<<<blocks, 256, 0, ctx->stream>>>(count, v, ctx->partial); count_launches(); }
