@@ -124,6 +124,43 @@ def one_pass(prob, api, precision):
     return good, sol, op
 
 
+# batched alpha-sweep: 64 instances, grids (60,32), (100,50), (150,64) drawn
+# 2:1:1, alpha uniform on [0.5, 4], Re 1000, Mach 0.5, nev 8, tol 1e-10
+C3_GRIDS = [(60, 32), (100, 50), (150, 64)]
+
+
+def c3_sweep_inputs(npoints=64, seed=2026):
+    from tailor_gb300.case import Physics, make_case
+    ph = Physics(alpha=1.0, omega=0j, nev=8, tol=1e-10)
+    cases = [make_case(ny, nz, amplitude=0.05, physics=ph) for ny, nz in C3_GRIDS]
+    rng = np.random.default_rng(seed)
+    cls = rng.choice([0, 0, 1, 2], size=npoints)
+    alphas = rng.uniform(0.5, 4.0, size=npoints)
+    return cases, [(int(c), float(a)) for c, a in zip(cls, alphas)]
+
+
+def run_c3(api, npoints=64):
+    """The sweep in the plain FP64 form (one instance at a time, CUDA-core
+    FP64 fronts) and in the mixed + batched form (complex64 fronts with
+    tensor-core Schur updates and FP64 refinement, six concurrent instances,
+    autotuned kernels): eigenpairs at resid <= 1e-10 per wall second."""
+    cases, points = c3_sweep_inputs(npoints)
+    out = {}
+    for name, kw in (("plain_fp64", dict(precision=0, workers=1, autotune=False)),
+                     ("mixed_batched", dict(precision=1, workers=6, autotune=True))):
+        t = time.perf_counter()
+        r = api.sweep(cases, points, nev=8, ncv=32, raise_on_error=False, **kw)
+        wall = time.perf_counter() - t
+        good = int(np.sum((r.residual >= 0) & (r.residual <= 1e-10)))
+        out[name] = {"value": good / wall, "unit": UNIT, "wall_s": wall, "eigenpairs": good,
+                     "failed_points": r.diag["failed"], "workers": r.diag["workers"],
+                     "solve_block": r.diag["solve_block"],
+                     "tensor_core_schur": [1 - c for c in r.diag["cuda_core_schur"]]}
+    out["points"] = npoints
+    out["grids"] = C3_GRIDS
+    return out
+
+
 def cpu_reference_sample(steps=1, threads=None):
     """The CPU path on a bounded sample (60 x 32 grid, C2 physics)."""
     from oracle.oracle import Oracle, boundary_rows, eigen_oracle, to_complex_blocks
@@ -176,6 +213,7 @@ def main():
     ap.add_argument("--precision", type=int, default=1, help="1 mixed (default), 0 FP64")
     ap.add_argument("--plain", action="store_true", help="also time the plain FP64 form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the 64-instance sweep")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -254,6 +292,10 @@ def main():
         plain = {"value": good / (time.perf_counter() - t), "factor_ms": sol.diag["factor_ms"],
                  "krylov_ms": sol.diag["krylov_ms"], "eigenpairs": good}
 
+    sweep = None
+    if rank == 0 and not args.no_sweep:
+        sweep = run_c3(api)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         g, times, c = cpu_reference_sample(steps=1)
@@ -303,6 +345,7 @@ def main():
                                        "trisolve_ms", "trisolves")},
         "cpu_baseline": cpu,
         "plain_fp64": plain,
+        "sweep_c3": sweep,
     }
     if rank == 0:
         print(json.dumps(line))

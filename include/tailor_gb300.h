@@ -195,6 +195,8 @@ typedef struct {
   int cuda_core_schur;    /* mixed form: 0 (default) Schur updates on the
                              tensor cores (tcgen05, 3xTF32); 1 on the CUDA
                              cores (FP32 FMA)                                */
+  int solve_block;        /* mixed form: diagonal-block size of the
+                             triangular solves, 128 or 256 (0: 256)          */
 } tlr_solve_opts;
 
 typedef struct {
@@ -257,6 +259,53 @@ int tlr_frobenius_noalloc(const double *values, size_t count, double *result,
 /* The context's CUDA stream (cudaStream_t) -- all device work of the
  * context is ordered on it; callers time or synchronise against it. */
 void *tlr_stream(tlr_ctx *ctx);
+
+/* Batched alpha-sweep, no counterpart in the reference (which solves one
+ * recipe per run, Process.cpp:34-179): every point is a full pass (metrics,
+ * derivatives, assembly, boundary rows, shift-invert Krylov-Schur) of its
+ * grid class at its own alpha.  Grid classes share one symbolic analysis
+ * each; worker threads own one context per class and run their points
+ * concurrently on the GPU. */
+typedef struct {
+  const tlr_recipe *recipe;   /* physics; alpha is taken from each point       */
+  const tlr_rule *xi, *eta;
+  int ny, nz;
+  double spanwise_period;
+  const double *grid;         /* natural-order fields, as for tlr_load_fields */
+  const double *baseflow;
+} tlr_grid_class;
+
+typedef struct {
+  int grid_class;
+  double alpha_re, alpha_im;
+  const double *start;        /* optional complex [5N] start vector (NULL)    */
+} tlr_sweep_point;
+
+typedef struct {
+  tlr_solve_opts solve;       /* shared solve options (start is ignored)      */
+  int workers;                /* concurrent instances (0: 6)                  */
+  int autotune;               /* mixed form: time both Schur-update kernels
+                                 and both solve block sizes on each class's
+                                 first point and keep the fastest             */
+  int device;
+} tlr_sweep_opts;
+
+typedef struct {
+  double wall_ms;
+  int points, failed, workers;
+  int converged_pairs;        /* pairs with relative residual <= tol          */
+  int cuda_core_schur[16];    /* per grid class: chosen Schur kernel          */
+  int solve_block[16];        /* per grid class: chosen diagonal-block size   */
+  double tune_factor_ms[16][2];   /* tensor cores, CUDA cores                 */
+  double tune_trisolve_ms[16][2]; /* block 256, block 128                     */
+} tlr_sweep_diag;
+
+/* lambda [npoints][nev] complex, residual [npoints][nev] (-1: not solved),
+ * status [npoints]; point_diag [npoints] optional.  Returns the first
+ * failing point's status (its message in tlr_last_error(NULL)). */
+int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sweep_point *points,
+              int npoints, const tlr_sweep_opts *opts, double *lambda, double *residual,
+              int *status, tlr_eig_diag *point_diag, tlr_sweep_diag *diag);
 
 /* Test hook, no counterpart in the reference: one Schur-complement update
  * F22 -= L21 U12 of a single dense complex64 front (m x m, column-major,

@@ -74,7 +74,8 @@ class SolveOpts(ctypes.Structure):
                 ("tol", ctypes.c_double), ("max_it", ctypes.c_int),
                 ("precision", ctypes.c_int), ("sigma_re", ctypes.c_double),
                 ("sigma_im", ctypes.c_double), ("use_sigma", ctypes.c_int),
-                ("start", ctypes.c_void_p), ("cuda_core_schur", ctypes.c_int)]
+                ("start", ctypes.c_void_p), ("cuda_core_schur", ctypes.c_int),
+                ("solve_block", ctypes.c_int)]
 
 
 class EigDiag(ctypes.Structure):
@@ -90,6 +91,32 @@ class EigDiag(ctypes.Structure):
                 ("trisolve_ms", ctypes.c_double), ("trisolves", ctypes.c_int),
                 ("ortho_ms", ctypes.c_double), ("dense_ms", ctypes.c_double),
                 ("residual_ms", ctypes.c_double)]
+
+
+class GridClass(ctypes.Structure):
+    _fields_ = [("recipe", ctypes.c_void_p), ("xi", ctypes.c_void_p), ("eta", ctypes.c_void_p),
+                ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("spanwise_period", ctypes.c_double), ("grid", ctypes.c_void_p),
+                ("baseflow", ctypes.c_void_p)]
+
+
+class SweepPoint(ctypes.Structure):
+    _fields_ = [("grid_class", ctypes.c_int), ("alpha_re", ctypes.c_double),
+                ("alpha_im", ctypes.c_double), ("start", ctypes.c_void_p)]
+
+
+class SweepOpts(ctypes.Structure):
+    _fields_ = [("solve", SolveOpts), ("workers", ctypes.c_int), ("autotune", ctypes.c_int),
+                ("device", ctypes.c_int)]
+
+
+class SweepDiag(ctypes.Structure):
+    _fields_ = [("wall_ms", ctypes.c_double), ("points", ctypes.c_int),
+                ("failed", ctypes.c_int), ("workers", ctypes.c_int),
+                ("converged_pairs", ctypes.c_int),
+                ("cuda_core_schur", ctypes.c_int * 16), ("solve_block", ctypes.c_int * 16),
+                ("tune_factor_ms", (ctypes.c_double * 2) * 16),
+                ("tune_trisolve_ms", (ctypes.c_double * 2) * 16)]
 
 
 # Exported symbols and their signatures (argtypes, restype).
@@ -114,6 +141,7 @@ SIGNATURES = {
     "tlr_solve": ([_P, _P, _P, _P, _P, _P], _I),
     "tlr_stream": ([_P], ctypes.c_void_p),
     "tlr_kernel_launches": ([], ctypes.c_longlong),
+    "tlr_sweep": ([_P, _I, _P, _I, _P, _P, _P, _P, _P, _P], _I),
     "tlr_schur_update_c64": ([_P, _I, _I, _I, _I, ctypes.c_uint, ctypes.c_uint, _P], _I),
     "tlr_frobenius_noalloc": ([_P, ctypes.c_size_t, _P, _P], _I),
     "tlr_mlp_create": ([_I, _I, _I, _I, ctypes.c_ulonglong, _P], _I),

@@ -238,6 +238,66 @@ class EigenSolver:
         return EigenSolution(lam_c, res[:nconv], vec_c, _diag_dict(d))
 
 
+@dataclass
+class SweepResult:
+    lam: np.ndarray        # [points][nev] complex (0 where not converged)
+    residual: np.ndarray   # [points][nev] (-1 where not solved)
+    status: np.ndarray     # [points] tlr status
+    diag: dict             # sweep diagnostics
+    point_diag: list       # per point solve diagnostics
+
+
+def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
+          autotune: bool = True, tol: float = 0.0, ncv: int = 0, max_it: int = 0,
+          starts=None, device: int = 0, raise_on_error: bool = True) -> SweepResult:
+    """Batched alpha-sweep (tlr_sweep): points are (class index, alpha); each
+    class is a Case (grid, base flow, physics) whose alpha is overridden."""
+    lib = L.load()
+    keep = []
+    holder = Problem.__new__(Problem)  # reuse the rule marshalling
+    holder._keep = keep
+    gcs = (L.GridClass * len(cases))()
+    for c, case in enumerate(cases):
+        r = make_recipe(case)
+        xi, eta = holder._rule(case.xi), holder._rule(case.eta)
+        g = np.ascontiguousarray(case.grid, dtype=np.float64)
+        b = np.ascontiguousarray(case.baseflow, dtype=np.float64)
+        keep += [r, xi, eta, g, b]
+        gcs[c] = L.GridClass(ctypes.addressof(r), ctypes.addressof(xi), ctypes.addressof(eta),
+                             case.ny, case.nz, case.spanwise_period, _ptr(g), _ptr(b))
+    npts = len(points)
+    pts = (L.SweepPoint * max(npts, 1))()
+    for i, (c, a) in enumerate(points):
+        s = None
+        if starts is not None and starts[i] is not None:
+            v = np.ascontiguousarray(np.stack([starts[i].real, starts[i].imag], -1),
+                                     dtype=np.float64)
+            keep.append(v)
+            s = v.ctypes.data
+        pts[i] = L.SweepPoint(int(c), complex(a).real, complex(a).imag, s)
+    k = nev or cases[0].physics.nev
+    opts = L.SweepOpts(L.SolveOpts(k, ncv, tol, max_it, precision, 0.0, 0.0, 0, None, 0, 0),
+                       workers, int(bool(autotune)), device)
+    lam = np.zeros((max(npts, 1), k, 2))
+    res = np.zeros((max(npts, 1), k))
+    st = np.zeros(max(npts, 1), dtype=np.int32)
+    pd = (L.EigDiag * max(npts, 1))()
+    d = L.SweepDiag()
+    rc = lib.tlr_sweep(gcs, len(cases), pts, npts, ctypes.byref(opts), _ptr(lam), _ptr(res),
+                       st.ctypes.data, pd, ctypes.byref(d))
+    if rc and raise_on_error:
+        raise TailorError(rc, lib.tlr_last_error(None).decode())
+    nc = len(cases)
+    diag = {"wall_ms": d.wall_ms, "points": d.points, "failed": d.failed,
+            "workers": d.workers, "converged_pairs": d.converged_pairs,
+            "cuda_core_schur": list(d.cuda_core_schur[:nc]),
+            "solve_block": list(d.solve_block[:nc]),
+            "tune_factor_ms": [list(d.tune_factor_ms[c]) for c in range(nc)],
+            "tune_trisolve_ms": [list(d.tune_trisolve_ms[c]) for c in range(nc)]}
+    return SweepResult(lam[:npts, :, 0] + 1j * lam[:npts, :, 1], res[:npts], st[:npts], diag,
+                       [_diag_dict(pd[i]) for i in range(npts)])
+
+
 def lns_points(case_or_physics, q: np.ndarray, qy: int = 10, qz: int = 6):
     """Pointwise LNS blocks on the GPU: q [np][10][5] -> [np][11][5][5]."""
     lib = L.load()

@@ -253,6 +253,8 @@ void tlr_ctx_destroy(tlr_ctx *ctx) {
   if (!ctx) return;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_factor(ctx);
+  free_workspace(ctx);
+  free_blas(ctx);
   free_rule(ctx->xi);
   free_rule(ctx->eta);
   cudaFree(ctx->grid_c); cudaFree(ctx->base_c); cudaFree(ctx->base);

@@ -76,7 +76,8 @@ struct DevRule {
   int *order = nullptr;  // [n][s] slots sorted by wrapped index
 };
 
-struct Factor;  // sparse LU state (tlr_lu.cu)
+struct Factor;    // sparse LU state (tlr_lu.cu)
+struct Symbolic;  // elimination structure (tlr_symbolic.h)
 
 }  // namespace tlr
 
@@ -99,6 +100,9 @@ struct tlr_ctx {
   // A_bc split into FP32 hi/lo pairs (re_hi, re_lo, im_hi, im_lo) for the
   // float-float refinement residual; rebuilt when the operator changes
   float4 *aff = nullptr, *wff = nullptr;  // wff: the iterate split the same way
+  const tlr::Symbolic *shared_sym = nullptr;  // set by a sweep: reuse this analysis
+  void *blas = nullptr;                         // cuBLAS handle, created on first solve
+  void *kws = nullptr;                          // Krylov workspace (tlr_krylov.cu)
   bool aff_valid = false;
   int *status = nullptr;     // [ST_COUNT]
   double *red = nullptr;     // [RD_COUNT]
@@ -140,6 +144,10 @@ int residual_ff(tlr_ctx *ctx, const double2 *y, const double2 *w, double sr, dou
 int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
               double *residual, double *modes, tlr_eig_diag *diag);
 void free_factor(tlr_ctx *ctx);
+void free_blas(tlr_ctx *ctx);
+void free_workspace(tlr_ctx *ctx);
+// Message returned by tlr_last_error(NULL) on the calling thread.
+void set_global_error(const std::string &msg);
 // Keep the symbolic analysis and device buffers, drop the numeric factor.
 void invalidate_factor(tlr_ctx *ctx);
 

@@ -65,6 +65,14 @@ __global__ void k_axmy(long long n, const double2 *__restrict__ a, const double2
   }
 }
 
+struct Workspace {  // device buffers of the Krylov driver, owned by the context
+  long long n = 0;
+  int ncv = 0;
+  double2 *V = nullptr, *w = nullptr, *y = nullptr, *r = nullptr, *aw = nullptr,
+          *bw = nullptr, *hv = nullptr, *tmp = nullptr;
+  float2 *x32 = nullptr;
+};
+
 struct Solver {
   tlr_ctx *ctx;
   Factor *F;
@@ -78,11 +86,6 @@ struct Solver {
   double refine_tol = 1e-12;
   int max_refine = 30;
 
-  ~Solver() {
-    cudaFree(V); cudaFree(w); cudaFree(y); cudaFree(r); cudaFree(aw); cudaFree(bw);
-    cudaFree(hv); cudaFree(tmp); cudaFree(x32);
-    if (h) cublasDestroy(h);
-  }
 
   double nrm(const double2 *v) {
     double out = 0.0;
@@ -185,6 +188,23 @@ void invalidate_factor(tlr_ctx *ctx) {
   if (ctx && ctx->factor) ctx->factor->factored = false;
 }
 
+void free_workspace(tlr_ctx *ctx) {
+  if (ctx && ctx->kws) {
+    Workspace *ws = static_cast<Workspace *>(ctx->kws);
+    cudaFree(ws->V); cudaFree(ws->w); cudaFree(ws->y); cudaFree(ws->r); cudaFree(ws->aw);
+    cudaFree(ws->bw); cudaFree(ws->hv); cudaFree(ws->tmp); cudaFree(ws->x32);
+    delete ws;
+    ctx->kws = nullptr;
+  }
+}
+
+void free_blas(tlr_ctx *ctx) {
+  if (ctx && ctx->blas) {
+    cublasDestroy(static_cast<cublasHandle_t>(ctx->blas));
+    ctx->blas = nullptr;
+  }
+}
+
 void free_factor(tlr_ctx *ctx) {
   if (ctx && ctx->factor) {
     ctx->factor->release();
@@ -213,12 +233,13 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   const cd sigma = o.use_sigma ? cd(o.sigma_re, o.sigma_im) : target;
   const int prec = o.precision == 1 ? 1 : 0;
   const bool tc = prec == 1 && !o.cuda_core_schur;
+  const int sblock = prec == 1 && o.solve_block == 128 ? 128 : (prec == 1 ? 256 : 128);
 
   // factorisation (reused when sigma, precision and Schur kernel are unchanged)
   Factor *F = ctx->factor;
   if (F && (F->prec != prec || F->sigma_re != sigma.real() || F->sigma_im != sigma.imag() ||
-            F->tensor_cores != tc || !F->factored)) {
-    if (F->prec != prec) {
+            F->tensor_cores != tc || F->sw != sblock || !F->factored)) {
+    if (F->prec != prec || F->sw != sblock) {
       free_factor(ctx);
       F = nullptr;
     } else {
@@ -230,7 +251,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   if (!F) {
     F = new Factor();
     ctx->factor = F;
-    int rc = F->setup(ctx, prec, 48);
+    int rc = F->setup(ctx, prec, 48, sblock);
     if (rc) {
       free_factor(ctx);
       return rc;
@@ -263,19 +284,46 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   S.n = n;
   S.sr = sigma.real();
   S.si = sigma.imag();
-  if (cublasCreate(&S.h) != CUBLAS_STATUS_SUCCESS)
-    return fail(ctx, TLR_ERR_CUDA, "cublasCreate failed");
+  if (!ctx->blas) {
+    cublasHandle_t hb = nullptr;
+    if (cublasCreate(&hb) != CUBLAS_STATUS_SUCCESS)
+      return fail(ctx, TLR_ERR_CUDA, "cublasCreate failed");
+    ctx->blas = hb;
+  }
+  S.h = static_cast<cublasHandle_t>(ctx->blas);
   cublasSetStream(S.h, ctx->stream);
   const size_t vb = n * sizeof(double2);
-  TLR_CUDA(ctx, cudaMalloc(&S.V, vb * (ncv + 1)));
-  TLR_CUDA(ctx, cudaMalloc(&S.w, vb));
-  TLR_CUDA(ctx, cudaMalloc(&S.y, vb));
-  TLR_CUDA(ctx, cudaMalloc(&S.r, vb));
-  TLR_CUDA(ctx, cudaMalloc(&S.aw, vb));
-  TLR_CUDA(ctx, cudaMalloc(&S.bw, vb));
-  TLR_CUDA(ctx, cudaMalloc(&S.hv, sizeof(double2) * (ncv + 1) * (ncv + 1)));
-  TLR_CUDA(ctx, cudaMalloc(&S.tmp, vb * ncv));
-  if (prec == 1) TLR_CUDA(ctx, cudaMalloc(&S.x32, n * sizeof(float2)));
+  // Krylov workspace kept in the context: cudaFree synchronises the whole
+  // device, which would serialise contexts that run concurrently
+  Workspace *ws = static_cast<Workspace *>(ctx->kws);
+  if (ws && (ws->n != n || ws->ncv < ncv)) {
+    free_workspace(ctx);
+    ws = nullptr;
+  }
+  if (!ws) {
+    ws = new Workspace();
+    ctx->kws = ws;
+    ws->n = n;
+    ws->ncv = ncv;
+    TLR_CUDA(ctx, cudaMalloc(&ws->V, vb * (ncv + 1)));
+    TLR_CUDA(ctx, cudaMalloc(&ws->w, vb));
+    TLR_CUDA(ctx, cudaMalloc(&ws->y, vb));
+    TLR_CUDA(ctx, cudaMalloc(&ws->r, vb));
+    TLR_CUDA(ctx, cudaMalloc(&ws->aw, vb));
+    TLR_CUDA(ctx, cudaMalloc(&ws->bw, vb));
+    TLR_CUDA(ctx, cudaMalloc(&ws->hv, sizeof(double2) * (ncv + 1) * (ncv + 1)));
+    TLR_CUDA(ctx, cudaMalloc(&ws->tmp, vb * ncv));
+    TLR_CUDA(ctx, cudaMalloc(&ws->x32, n * sizeof(float2)));
+  }
+  S.V = ws->V;
+  S.w = ws->w;
+  S.y = ws->y;
+  S.r = ws->r;
+  S.aw = ws->aw;
+  S.bw = ws->bw;
+  S.hv = ws->hv;
+  S.tmp = ws->tmp;
+  S.x32 = ws->x32;
 
   std::vector<double2> v0(n);
   if (o.start) {

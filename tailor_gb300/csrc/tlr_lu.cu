@@ -766,21 +766,26 @@ __global__ void __launch_bounds__(256)
 
 // ------------------------------------------------------------------- host
 
-int Factor::setup(tlr_ctx *ctx, int precision, int leaf) {
+int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block) {
   prec = precision;
   w = precision == 0 ? 32 : 64;
-  sw = precision == 0 ? 128 : 256;
-  std::vector<int> rp(ctx->nn + 1), cl((size_t)ctx->nnzb);
-  TLR_CUDA(ctx, cudaMemcpy(rp.data(), ctx->row_ptr, rp.size() * sizeof(int),
-                           cudaMemcpyDeviceToHost));
-  TLR_CUDA(ctx, cudaMemcpy(cl.data(), ctx->col, cl.size() * sizeof(int),
-                           cudaMemcpyDeviceToHost));
-  int rc = build_symbolic(ctx->ny, ctx->nz, ctx->h_xi_idx, ctx->sx, ctx->h_eta_off,
-                          ctx->se, rp, cl, leaf, sym);
-  if (rc) {
-    char buf[96];
-    snprintf(buf, sizeof(buf), "symbolic analysis failed (code %d)", rc);
-    return fail(ctx, TLR_ERR_ARG, buf);
+  sw = precision == 0 ? 128 : (solve_block == 128 ? 128 : 256);
+  int rc;
+  if (ctx->shared_sym) {
+    sym = *ctx->shared_sym;  // analysis shared by every context of the grid class
+  } else {
+    std::vector<int> rp(ctx->nn + 1), cl((size_t)ctx->nnzb);
+    TLR_CUDA(ctx, cudaMemcpy(rp.data(), ctx->row_ptr, rp.size() * sizeof(int),
+                             cudaMemcpyDeviceToHost));
+    TLR_CUDA(ctx, cudaMemcpy(cl.data(), ctx->col, cl.size() * sizeof(int),
+                             cudaMemcpyDeviceToHost));
+    rc = build_symbolic(ctx->ny, ctx->nz, ctx->h_xi_idx, ctx->sx, ctx->h_eta_off, ctx->se, rp,
+                        cl, leaf, sym);
+    if (rc) {
+      char buf[96];
+      snprintf(buf, sizeof(buf), "symbolic analysis failed (code %d)", rc);
+      return fail(ctx, TLR_ERR_ARG, buf);
+    }
   }
   const int nf = (int)sym.fronts.size();
   std::vector<DevFront> df(nf);
