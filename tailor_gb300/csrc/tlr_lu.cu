@@ -207,60 +207,85 @@ __global__ void k_swap(const int *__restrict__ fl, int s, int w, C *__restrict__
   }
 }
 
-// L21 = F21 U_kk^-1 on the border rows p..m-1 of the panel columns.
+// L21 = F21 U_kk^-1 on the border rows p..m-1 of the panel columns.  CTA =
+// 32 border rows x all ww columns staged in shared memory; column-oriented
+// substitution with all 256 threads: x_c = t_c / U_cc, then t_c' -= x_c U_cc'
+// for every later column c' (one barrier per step).
 template <class C>
-__global__ void k_trsm_border(const int *__restrict__ fl, int s, int w, C *__restrict__ pool,
-                              const DevFront *__restrict__ fr) {
+__global__ void __launch_bounds__(256)
+    k_trsm_border(const int *__restrict__ fl, int s, int w, C *__restrict__ pool,
+                  const DevFront *__restrict__ fr) {
   extern __shared__ __align__(16) unsigned char sm[];
-  C *U = reinterpret_cast<C *>(sm);          // ww x ww, column-major
-  C *dinv = U + w * w;
+  C *U = reinterpret_cast<C *>(sm);  // ww x ww, column-major U[c * w + r]
+  C *T = U + w * w;                  // [ww][33]: T[c * 33 + rr]
   const DevFront f = fr[fl[blockIdx.y]];
   const int k0 = s * w, ww = min(w, f.p - k0);
   const int m = f.m;
+  const int r0 = f.p + blockIdx.x * 32;
+  if (r0 >= m) return;
+  const int nr = min(32, m - r0);
   C *F = pool + f.off;
   for (int x = threadIdx.x; x < ww * ww; x += blockDim.x) {
     const int r = x % ww, c = x / ww;
     U[c * w + r] = F[(long long)(k0 + c) * m + k0 + r];
   }
+  for (int x = threadIdx.x; x < ww * 32; x += blockDim.x) {
+    const int rr = x & 31, c = x >> 5;
+    T[c * 33 + rr] = rr < nr ? F[(long long)(k0 + c) * m + r0 + rr] : czero<C>();
+  }
   __syncthreads();
-  for (int c = threadIdx.x; c < ww; c += blockDim.x) dinv[c] = cinv(U[c * w + c]);
-  __syncthreads();
-  const int r = f.p + blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= m) return;
-  C x[64];
-#pragma unroll 1
   for (int c = 0; c < ww; ++c) {
-    C v = F[(long long)(k0 + c) * m + r];
-    for (int cp = 0; cp < c; ++cp) v = cfms(v, x[cp], U[c * w + cp]);
-    x[c] = cmul(v, dinv[c]);
-    F[(long long)(k0 + c) * m + r] = x[c];
+    if (threadIdx.x < 32) T[c * 33 + threadIdx.x] = cmul(T[c * 33 + threadIdx.x], cinv(U[c * w + c]));
+    __syncthreads();
+    for (int x = threadIdx.x; x < (ww - 1 - c) * 32; x += blockDim.x) {
+      const int cp = c + 1 + (x >> 5), rr = x & 31;
+      T[cp * 33 + rr] = cfms(T[cp * 33 + rr], T[c * 33 + rr], U[cp * w + c]);
+    }
+    __syncthreads();
+  }
+  for (int x = threadIdx.x; x < ww * 32; x += blockDim.x) {
+    const int rr = x & 31, c = x >> 5;
+    if (rr < nr) F[(long long)(k0 + c) * m + r0 + rr] = T[c * 33 + rr];
   }
 }
 
-// U12 = L_kk^-1 F12 for columns k0+ww..m-1 (unit lower L_kk).
+// U12 = L_kk^-1 F12 for columns k0+ww..m-1 (unit lower L_kk).  CTA = 32
+// columns x all ww rows staged in shared memory; column-oriented forward
+// substitution with all 256 threads: row q final, then t_r -= L_rq t_q for
+// r > q (one barrier per step).
 template <class C>
-__global__ void k_trsm_urow(const int *__restrict__ fl, int s, int w, C *__restrict__ pool,
-                            const DevFront *__restrict__ fr) {
+__global__ void __launch_bounds__(256)
+    k_trsm_urow(const int *__restrict__ fl, int s, int w, C *__restrict__ pool,
+                const DevFront *__restrict__ fr) {
   extern __shared__ __align__(16) unsigned char sm[];
-  C *Lk = reinterpret_cast<C *>(sm);
+  C *Lk = reinterpret_cast<C *>(sm);  // ww x ww, column-major Lk[c * w + r]
+  C *T = Lk + w * w;                  // [ww][33]: T[q * 33 + cc]
   const DevFront f = fr[fl[blockIdx.y]];
   const int k0 = s * w, ww = min(w, f.p - k0);
   const int m = f.m;
+  const int c0 = k0 + ww + blockIdx.x * 32;
+  if (c0 >= m) return;
+  const int nc = min(32, m - c0);
   C *F = pool + f.off;
   for (int x = threadIdx.x; x < ww * ww; x += blockDim.x) {
     const int r = x % ww, c = x / ww;
     Lk[c * w + r] = F[(long long)(k0 + c) * m + k0 + r];
   }
+  for (int x = threadIdx.x; x < ww * 32; x += blockDim.x) {
+    const int q = x % ww, cc = x / ww;
+    T[q * 33 + cc] = cc < nc ? F[(long long)(c0 + cc) * m + k0 + q] : czero<C>();
+  }
   __syncthreads();
-  const int c = k0 + ww + blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= m) return;
-  C *col = F + (long long)c * m + k0;
-  C x[64];
-  for (int r = 0; r < ww; ++r) {
-    C v = col[r];
-    for (int rp = 0; rp < r; ++rp) v = cfms(v, Lk[rp * w + r], x[rp]);
-    x[r] = v;
-    col[r] = v;
+  for (int q = 0; q + 1 < ww; ++q) {
+    for (int x = threadIdx.x; x < (ww - 1 - q) * 32; x += blockDim.x) {
+      const int r = q + 1 + (x >> 5), cc = x & 31;
+      T[r * 33 + cc] = cfms(T[r * 33 + cc], Lk[q * w + r], T[q * 33 + cc]);
+    }
+    __syncthreads();
+  }
+  for (int x = threadIdx.x; x < ww * 32; x += blockDim.x) {
+    const int q = x % ww, cc = x / ww;
+    if (cc < nc) F[(long long)(c0 + cc) * m + k0 + q] = T[q * 33 + cc];
   }
 }
 
@@ -1027,7 +1052,7 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
   C *P = static_cast<C *>(pool);
   TLR_CUDA(ctx, cudaMemsetAsync(d_pert, 0, sizeof(int), st));
   TLR_CUDA(ctx, cudaMemsetAsync(d_tc_err, 0, sizeof(int), st));
-  const size_t tsm = sizeof(C) * (size_t)(w * w + w);
+  const size_t tsm = sizeof(C) * (size_t)(w * w + w * 33);
   TLR_CUDA(ctx, cudaFuncSetAttribute(k_trsm_border<C>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
   TLR_CUDA(ctx, cudaFuncSetAttribute(k_trsm_urow<C>,
@@ -1054,10 +1079,10 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
       { k_swap<C><<<dim3(blocks_for(S.max_m, 128), S.nf), 128, 0, st>>>(fl, s, w, P, d_fronts,
                                                                        d_ipiv); count_launches(); }
       if (S.max_b > 0)
-        { k_trsm_border<C><<<dim3(blocks_for(S.max_b, 128), S.nf), 128, tsm, st>>>(fl, s, w, P,
+        { k_trsm_border<C><<<dim3(blocks_for(S.max_b, 32), S.nf), 256, tsm, st>>>(fl, s, w, P,
                                                                                  d_fronts); count_launches(); }
       if (S.max_ext > 0) {
-        { k_trsm_urow<C><<<dim3(blocks_for(S.max_ext, 128), S.nf), 128, tsm, st>>>(fl, s, w, P,
+        { k_trsm_urow<C><<<dim3(blocks_for(S.max_ext, 32), S.nf), 256, tsm, st>>>(fl, s, w, P,
                                                                                  d_fronts); count_launches(); }
         if (S.tiles > 0) {
           if constexpr (sizeof(C) == sizeof(float2)) {
