@@ -459,7 +459,7 @@ int run_assemble(tlr_ctx *ctx, tlr_operator_diag *diag) {
   p.a2_im = ar * ai + ai * ar;
   p.alpha_finite = std::isfinite(ar) && std::isfinite(ai);
   TLR_CUDA(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int) * ST_COUNT, ctx->stream));
-  { k_coefficients<<<blocks_for(ctx->nn, 128), 128, 0, ctx->stream>>>(
+  { k_coefficients<<<blocks_for(ctx->nn, 32), 32, 0, ctx->stream>>>(
       p, ctx->base_c, ctx->derivs, ctx->metrics, ctx->coef, ctx->status); count_launches(); }
   TLR_CUDA(ctx, cudaGetLastError());
   int st[ST_COUNT];

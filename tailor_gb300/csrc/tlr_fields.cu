@@ -14,6 +14,9 @@
 namespace tlr {
 namespace {
 
+// one warp per CTA: node counts of a few thousand still spread over every SM
+constexpr int kNodeThreads = 32;
+
 constexpr double kEps = DBL_EPSILON;
 
 __device__ inline bool finite(double v) { return isfinite(v); }
@@ -324,7 +327,7 @@ int run_metrics(tlr_ctx *ctx, tlr_metric_diag *diag) {
   if (rc) return rc;
   TLR_CUDA(ctx, cudaMemsetAsync(ctx->metrics, 0, sizeof(double) * 10 * nn,
                                 ctx->stream));
-  { k_metrics_first<<<blocks_for(nn, 128), 128, 0, ctx->stream>>>(
+  { k_metrics_first<<<blocks_for(nn, kNodeThreads), kNodeThreads, 0, ctx->stream>>>(
       ctx->ny, ctx->nz, ctx->span, ctx->xi, ctx->eta, ctx->grid_c,
       ctx->metrics, ctx->status, ctx->red); count_launches(); }
   int st[ST_COUNT];
@@ -355,7 +358,7 @@ int run_metrics(tlr_ctx *ctx, tlr_metric_diag *diag) {
              "is %.16g", d.max_grid_imaginary);
     return fail(ctx, TLR_ERR_COMPLEX, buf);
   }
-  { k_metrics_second<<<blocks_for(nn, 128), 128, 0, ctx->stream>>>(
+  { k_metrics_second<<<blocks_for(nn, kNodeThreads), kNodeThreads, 0, ctx->stream>>>(
       ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->metrics, ctx->status); count_launches(); }
   if ((rc = read_status(ctx, st, red))) return rc;
   if (st[ST_SECOND])
@@ -372,9 +375,9 @@ int run_derivatives(tlr_ctx *ctx, tlr_deriv_diag *diag) {
   if (rc) return rc;
   TLR_CUDA(ctx, cudaMemsetAsync(ctx->derivs, 0, sizeof(double) * 25 * nn,
                                 ctx->stream));
-  { k_baseflow_prep<<<blocks_for(nn, 128), 128, 0, ctx->stream>>>(
+  { k_baseflow_prep<<<blocks_for(nn, kNodeThreads), kNodeThreads, 0, ctx->stream>>>(
       nn, ctx->base_c, ctx->base, ctx->status, ctx->red); count_launches(); }
-  { k_derivatives<<<blocks_for(nn, 128), 128, 0, ctx->stream>>>(
+  { k_derivatives<<<blocks_for(nn, kNodeThreads), kNodeThreads, 0, ctx->stream>>>(
       ctx->ny, ctx->nz, ctx->xi, ctx->eta, ctx->base, ctx->metrics,
       ctx->derivs, ctx->status); count_launches(); }
   int st[ST_COUNT];
