@@ -212,13 +212,14 @@ class EigenSolver:
     def solve(self, nev: int = 0, ncv: int = 0, tol: float = 0.0,
               max_it: int = 0, precision: int = 0, sigma: complex | None = None,
               start: np.ndarray | None = None, modes: bool = False,
-              cuda_core_schur: bool = False) -> EigenSolution:
+              cuda_core_schur: bool = False, persistent_solve: bool = False) -> EigenSolution:
         ph = self.p.case.physics
         k = nev or ph.nev
         opts = L.SolveOpts(nev, ncv, tol, max_it, precision,
                            0.0 if sigma is None else complex(sigma).real,
                            0.0 if sigma is None else complex(sigma).imag,
-                           0 if sigma is None else 1, None, int(bool(cuda_core_schur)))
+                           0 if sigma is None else 1, None, int(bool(cuda_core_schur)), 0,
+                           int(bool(persistent_solve)))
         if start is not None:
             s = np.ascontiguousarray(np.stack([start.real, start.imag], -1),
                                      dtype=np.float64)
@@ -276,7 +277,7 @@ def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
             s = v.ctypes.data
         pts[i] = L.SweepPoint(int(c), complex(a).real, complex(a).imag, s)
     k = nev or cases[0].physics.nev
-    opts = L.SweepOpts(L.SolveOpts(k, ncv, tol, max_it, precision, 0.0, 0.0, 0, None, 0, 0),
+    opts = L.SweepOpts(L.SolveOpts(k, ncv, tol, max_it, precision, 0.0, 0.0, 0, None, 0, 0, 0),
                        workers, int(bool(autotune)), device)
     lam = np.zeros((max(npts, 1), k, 2))
     res = np.zeros((max(npts, 1), k))

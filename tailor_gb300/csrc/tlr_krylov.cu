@@ -258,6 +258,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     }
   }
   F->tensor_cores = tc;
+  F->persistent = o.persistent_solve != 0;
   if (!F->factored) {
     double anorm = 0.0;
     int rc = frobenius(ctx, ctx->A, ctx->nnzb * 25, &anorm);
@@ -516,6 +517,10 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
                                     cudaMemcpyDeviceToHost, ctx->stream));
   TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   const auto t3 = clock::now();
+  {
+    const int erc = F->take_solve_error(ctx);
+    if (erc) return erc;
+  }
   if (diag) {
     tlr_eig_diag d{};
     d.requested = nev;

@@ -787,6 +787,213 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---- persistent solve ------------------------------------------------------
+// The whole triangular solve as one cooperative launch: every phase of the
+// graph above (gather of a level, one block step, border product, backward
+// start) becomes a list of CTA work items that the resident CTAs stride
+// through, with a grid barrier between dependent phases.  Data written by
+// other CTAs in earlier phases is read past L1 (__ldcg).  The barrier spins
+// with a bound: on timeout it raises the solve's error flag and goes on (the
+// host rejects the solve).
+
+enum PhaseType : int { kPhGather = 0, kPhFwd = 1, kPhBorder = 2, kPhBwdStart = 3, kPhBwd = 4 };
+
+constexpr unsigned kBarrierLimit = 1u << 22;
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void grid_barrier(unsigned *count, unsigned target, int *err) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(count, 1u);
+    unsigned it = 0;
+    while (ld_acquire(count) < target)
+      if (++it > kBarrierLimit) {
+        atomicExch(err, 1);
+        break;
+      }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+template <class C>
+__device__ void ps_gather(const int *fl, const DevFront *fr, const int *nodes, const int *perm,
+                          const int2 *cinv, const C *b, C *work, int bx, int by) {
+  const DevFront f = fr[fl[by]];
+  const int i = bx * blockDim.x + threadIdx.x;
+  if (i >= f.m) return;
+  C v = czero<C>();
+  if (i < f.p) {
+    const int q = perm[f.toff + i];
+    v = __ldcg(b + (long long)nodes[f.node_off + q / 5] * 5 + q % 5);
+  }
+  const int2 c = cinv[f.toff + i];
+  if (c.x >= 0) v = cadd(v, __ldcg(work + c.x));
+  if (c.y >= 0) v = cadd(v, __ldcg(work + c.y));
+  work[f.toff + i] = v;
+}
+
+template <class C, int SW>
+__device__ void ps_step(const int *fl, int b, int backward, const C *pool, const DevFront *fr,
+                        C *work, const int *nodes, C *x, int bx, int by, C *vs, C (*red)[32]) {
+  const DevFront f = fr[fl[by]];
+  const int b0 = b * SW, b1 = min(f.p, b0 + SW), nb = b1 - b0;
+  const int lo = backward ? 0 : b1, hi = backward ? b0 : f.m;
+  const int r0 = lo + bx * 32;
+  if (nb <= 0 || r0 >= hi) return;
+  C *t = work + f.toff;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int r = r0 + lane;
+  const C *F = pool + f.off + (long long)b0 * f.m;
+  constexpr int kQ = SW / 8;
+  const int q0 = wp * kQ;
+  C fv[kQ];
+#pragma unroll
+  for (int k = 0; k < kQ; ++k)
+    fv[k] = (r < hi && q0 + k < nb) ? F[(long long)(q0 + k) * f.m + r] : czero<C>();
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) vs[q] = __ldcg(t + b0 + q);
+  __syncthreads();
+  C acc = czero<C>();
+#pragma unroll
+  for (int k = 0; k < kQ; ++k)
+    if (q0 + k < nb) acc = cfma(acc, fv[k], vs[q0 + k]);
+  red[wp][lane] = acc;
+  __syncthreads();
+  if (wp == 0 && r < hi) {
+    C v = __ldcg(t + r);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v = csub(v, red[k][lane]);
+    t[r] = v;
+    if (backward && r >= b0 - SW) x[(long long)nodes[f.node_off + r / 5] * 5 + r % 5] = v;
+  }
+  __syncthreads();  // vs and red are reused by the next item
+}
+
+template <class C>
+__device__ void ps_border(const int *fl, const C *pool, const DevFront *fr, const int *nodes,
+                          const C *x, double2 *partial, int nck, int pmax, int bx, int by, int bz,
+                          C *xs, C (*red)[32]) {
+  const DevFront f = fr[fl[bz]];
+  const int r0 = bx * 32;
+  const int c0 = f.p + by * kBC;
+  if (r0 >= f.p || c0 >= f.m) return;
+  const int nc = min(kBC, f.m - c0);
+  for (int k = threadIdx.x; k < nc; k += blockDim.x) {
+    const int c = c0 + k;
+    xs[k] = __ldcg(x + (long long)nodes[f.node_off + c / 5] * 5 + c % 5);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int r = r0 + lane;
+  C acc = czero<C>();
+  if (r < f.p) {
+    const int ka = wp * (kBC / 8), kb = min(nc, ka + kBC / 8);
+    const C *F = pool + f.off + (long long)c0 * f.m + r;
+#pragma unroll 8
+    for (int k = ka; k < kb; ++k) acc = cfma(acc, F[(long long)k * f.m], xs[k]);
+  }
+  red[wp][lane] = acc;
+  __syncthreads();
+  if (wp == 0 && r < f.p) {
+    C v = czero<C>();
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v = cadd(v, red[k][lane]);
+    partial[((long long)bz * nck + by) * pmax + r] = to64(v);
+  }
+  __syncthreads();
+}
+
+template <class C, int SW>
+__device__ void ps_bwd_start(const int *fl, const DevFront *fr, const long long *inv_off,
+                             const C *dmat, const C *work, C *work2, const double2 *partial,
+                             int nck, int pmax, const int *nodes, C *x, int bx, int by, C *zs,
+                             C (*red)[32]) {
+  const int fid = fl[by];
+  const DevFront f = fr[fid];
+  const int blk = bx / (SW / 32), quarter = bx % (SW / 32);
+  const int b0 = blk * SW, nb = min(SW, f.p - b0);
+  const int rr0 = quarter * 32;
+  if (nb <= 0 || rr0 >= nb) return;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int rr = rr0 + lane;
+  const C *Dm = dmat + inv_off[fid] + (long long)blk * SW * SW;
+  constexpr int kQ = SW / 8;
+  const int q0 = wp * kQ;
+  C dv[kQ];
+#pragma unroll
+  for (int k = 0; k < kQ; ++k)
+    dv[k] = (rr < nb && q0 + k < nb) ? Dm[(long long)(q0 + k) * nb + rr] : czero<C>();
+  const C *z = work + f.toff + b0;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) zs[q] = __ldcg(z + q);
+  __syncthreads();
+  C acc = czero<C>();
+#pragma unroll
+  for (int k = 0; k < kQ; ++k)
+    if (q0 + k < nb) acc = cfma(acc, dv[k], zs[q0 + k]);
+  red[wp][lane] = acc;
+  __syncthreads();
+  if (wp == 0 && rr < nb) {
+    C w = czero<C>();
+#pragma unroll
+    for (int k = 0; k < 8; ++k) w = cadd(w, red[k][lane]);
+    const int r = b0 + rr;
+    const int nchf = f.m > f.p ? (f.m - f.p + kBC - 1) / kBC : 0;
+    double2 s = make_double2(0, 0);
+    for (int k = 0; k < nchf; ++k) {
+      const double2 pv = __ldcg(partial + ((long long)by * nck + k) * pmax + r);
+      s.x += pv.x;
+      s.y += pv.y;
+    }
+    w = csub(w, from64<C>(s));
+    work2[f.toff + r] = w;
+    if (b0 + SW >= f.p) x[(long long)nodes[f.node_off + r / 5] * 5 + r % 5] = w;
+  }
+  __syncthreads();
+}
+
+template <class C, int SW>
+__global__ void __launch_bounds__(256)
+    k_solve_persistent(const Phase *__restrict__ phases, int nphases, const int *__restrict__ sched,
+                       const C *__restrict__ pool, const DevFront *__restrict__ fr,
+                       const int *__restrict__ nodes, const int *__restrict__ perm,
+                       const int2 *__restrict__ cinv, const long long *__restrict__ inv_off,
+                       const C *__restrict__ dmat, C *work, C *work2, double2 *partial, C *x,
+                       unsigned *barrier, int *err) {
+  __shared__ C vec_s[SW > kBC ? SW : kBC];
+  __shared__ C red_s[8][32];
+  unsigned target = 0;
+  for (int ph = 0; ph < nphases; ++ph) {
+    const Phase P = phases[ph];
+    const int *fl = sched + P.fl_off;
+    const int nitems = P.nx * P.ny * P.nz;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+      const int bx = it % P.nx, rest = it / P.nx, by = rest % P.ny, bz = rest / P.ny;
+      switch (P.type) {
+        case kPhGather: ps_gather<C>(fl, fr, nodes, perm, cinv, x, work, bx, by); break;
+        case kPhFwd: ps_step<C, SW>(fl, P.b, 0, pool, fr, work, nodes, x, bx, by, vec_s, red_s); break;
+        case kPhBorder:
+          ps_border<C>(fl, pool, fr, nodes, x, partial, P.nck, P.pmax, bx, by, bz, vec_s, red_s);
+          break;
+        case kPhBwdStart:
+          ps_bwd_start<C, SW>(fl, fr, inv_off, dmat, work, work2, partial, P.nck, P.pmax, nodes, x,
+                              bx, by, vec_s, red_s);
+          break;
+        default: ps_step<C, SW>(fl, P.b, 1, pool, fr, work2, nodes, x, bx, by, vec_s, red_s); break;
+      }
+    }
+    if (ph + 1 < nphases) {
+      target += gridDim.x;
+      grid_barrier(barrier, target, err);
+    }
+  }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------- host
@@ -992,6 +1199,79 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block) {
                            cudaMemcpyHostToDevice));
   TLR_CUDA(ctx, cudaMemcpy(d_sched, sched.data(), sched.size() * sizeof(int),
                            cudaMemcpyHostToDevice));
+  return build_phases(ctx);
+}
+
+int Factor::build_phases(tlr_ctx *ctx) {
+  std::vector<Phase> ph;
+  for (size_t h = 0; h < levels.size(); ++h) {
+    const Level &L = levels[h];
+    ph.push_back({kPhGather, L.fronts_off, 0, blocks_for(L.max_m, 256), L.nfronts, 1, 0, 0});
+    for (int b = 0; b < (int)L.blk_nf.size(); ++b)
+      if (L.fwd_rows[b] > 0)
+        ph.push_back({kPhFwd, L.fronts_off, b, blocks_for(L.fwd_rows[b], 32), L.blk_nf[b], 1, 0, 0});
+  }
+  for (int h = (int)levels.size() - 1; h >= 0; --h) {
+    const Level &L = levels[h];
+    if (L.bmax > 0)
+      ph.push_back({kPhBorder, L.fronts_off, 0, blocks_for(L.pmax, 32), L.nck_b, L.nfronts,
+                    L.nck_b, L.pmax});
+    ph.push_back({kPhBwdStart, L.fronts_off, 0, (int)L.blk_nf.size() * (sw / 32), L.nfronts, 1,
+                  L.nck_b, L.pmax});
+    for (int b = (int)L.blk_nf.size() - 1; b >= 1; --b)
+      ph.push_back({kPhBwd, L.fronts_off, b, blocks_for(b * sw, 32), L.blk_nf[b], 1, 0, 0});
+  }
+  nphases = (int)ph.size();
+  cudaError_t e;
+  if ((e = cudaMalloc(&d_phases, std::max<size_t>(ph.size(), 1) * sizeof(Phase))) != cudaSuccess ||
+      (e = cudaMalloc(&d_barrier, sizeof(unsigned))) != cudaSuccess ||
+      (e = cudaMalloc(&d_solve_err, sizeof(int))) != cudaSuccess)
+    return fail(ctx, TLR_ERR_NOMEM, std::string("factor allocation failed: ") + cudaGetErrorString(e));
+  TLR_CUDA(ctx, cudaMemcpy(d_phases, ph.data(), ph.size() * sizeof(Phase), cudaMemcpyHostToDevice));
+  TLR_CUDA(ctx, cudaMemset(d_solve_err, 0, sizeof(int)));
+  return TLR_OK;
+}
+
+int Factor::take_solve_error(tlr_ctx *ctx) {
+  if (!d_solve_err) return TLR_OK;
+  int h = 0;
+  TLR_CUDA(ctx, cudaMemcpyAsync(&h, d_solve_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (!h) return TLR_OK;
+  TLR_CUDA(ctx, cudaMemsetAsync(d_solve_err, 0, sizeof(int), ctx->stream));
+  return fail(ctx, TLR_ERR_CUDA, "persistent solve: a grid barrier timed out");
+}
+
+template <class C, int SW>
+int Factor::solve_persistent(tlr_ctx *ctx) {
+  cudaStream_t st = ctx->stream;
+  int grid = persist_grid;
+  int dev = 0, sms = 0, occ = 0;
+  TLR_CUDA(ctx, cudaGetDevice(&dev));
+  TLR_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  TLR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solve_persistent<C, SW>,
+                                                               256, 0));
+  const int cap = sms * std::max(occ, 1);
+  if (grid <= 0) grid = 2 * sms;
+  grid = std::max(1, std::min(grid, cap));
+  const Phase *ph = d_phases;
+  int np = nphases;
+  const int *sc = d_sched;
+  const C *P = static_cast<const C *>(pool);
+  const DevFront *frp = d_fronts;
+  const int *nd = d_nodes, *pm = d_perm;
+  const int2 *ci = d_cinv;
+  const long long *io = d_inv_off;
+  const C *dm = static_cast<const C *>(dmat);
+  C *W = static_cast<C *>(work), *W2 = static_cast<C *>(work2), *X = static_cast<C *>(vec_a);
+  double2 *pa = d_partial;
+  unsigned *bar = d_barrier;
+  int *er = d_solve_err;
+  void *args[] = {&ph, &np, &sc, &P, &frp, &nd, &pm, &ci, &io, &dm, &W, &W2, &pa, &X, &bar, &er};
+  TLR_CUDA(ctx, cudaMemsetAsync(d_barrier, 0, sizeof(unsigned), st));
+  TLR_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)k_solve_persistent<C, SW>, dim3(grid),
+                                            dim3(256), args, 0, st));
+  count_launches(1);
   return TLR_OK;
 }
 
@@ -1016,6 +1296,10 @@ void Factor::release() {
   cudaFree(d_cinv); cudaFree(work2); cudaFree(d_sched); cudaFree(d_partial); cudaFree(d_pert); cudaFree(d_tc_err);
   cudaFree(vec_a); cudaFree(linv); cudaFree(uinv); cudaFree(dmat);
   cudaFree(d_inv_off); cudaFree(d_inv_blocks); cudaFree(d_ltiles); cudaFree(d_utiles);
+  cudaFree(d_phases); cudaFree(d_barrier); cudaFree(d_solve_err);
+  d_phases = nullptr;
+  d_barrier = nullptr;
+  d_solve_err = nullptr;
   linv = uinv = dmat = nullptr;
   d_ltiles = d_utiles = nullptr;
   d_inv_off = nullptr;
@@ -1212,6 +1496,24 @@ int Factor::solve(tlr_ctx *ctx, void *x) {
   const size_t bytes = (size_t)sym.nn * 5 * (prec == 0 ? sizeof(double2) : sizeof(float2));
   cudaStream_t st = ctx->stream;
   TLR_CUDA(ctx, cudaMemcpyAsync(vec_a, x, bytes, cudaMemcpyDeviceToDevice, st));
+  if (persistent) {
+    if (ev_used + 2 > ev_pool.size()) {
+      cudaEvent_t a, b;
+      TLR_CUDA(ctx, cudaEventCreate(&a));
+      TLR_CUDA(ctx, cudaEventCreate(&b));
+      ev_pool.push_back(a);
+      ev_pool.push_back(b);
+    }
+    TLR_CUDA(ctx, cudaEventRecord(ev_pool[ev_used], st));
+    const int rc = prec == 0 ? solve_persistent<double2, 128>(ctx)
+                             : (sw == 256 ? solve_persistent<float2, 256>(ctx)
+                                          : solve_persistent<float2, 128>(ctx));
+    if (rc) return rc;
+    TLR_CUDA(ctx, cudaEventRecord(ev_pool[ev_used + 1], st));
+    ev_used += 2;
+    TLR_CUDA(ctx, cudaMemcpyAsync(x, vec_a, bytes, cudaMemcpyDeviceToDevice, st));
+    return TLR_OK;
+  }
   if (!graph_exec) {
     TLR_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     int rc;

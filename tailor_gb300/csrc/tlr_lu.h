@@ -28,6 +28,13 @@ struct Level {
   std::vector<int> fwd_rows;  // rows below block b, largest over those fronts
 };
 
+// One phase of the persistent solve: a kind of work item over a level's
+// fronts (fl_off into the level schedule), block b, and an nx x ny x nz
+// item grid (the CTA grid of the equivalent separate launch).
+struct Phase {
+  int type, fl_off, b, nx, ny, nz, nck, pmax;
+};
+
 struct Factor {
   Symbolic sym;
   int prec = 0;  // 0: complex128 fronts, 1: complex64 fronts
@@ -51,6 +58,13 @@ struct Factor {
   int n_inv_blocks = 0;
   long long inv_elems = 0, n_ltiles = 0, n_utiles = 0;
   cudaGraphExec_t graph_exec = nullptr;  // captured solve, replayed per call
+  // persistent solve: one cooperative launch per solve over a phase table
+  bool persistent = false;
+  int persist_grid = 0;                  // CTAs (0: two per SM, capped by occupancy)
+  Phase *d_phases = nullptr;
+  int nphases = 0;
+  unsigned *d_barrier = nullptr;
+  int *d_solve_err = nullptr;
   long long graph_kernels = 0;           // kernel nodes of graph_exec
   double2 *d_partial = nullptr;
   int perturbed = 0;
@@ -71,6 +85,11 @@ struct Factor {
   template <class C> int factor_impl(tlr_ctx *ctx, double sr, double si, double tiny);
   template <class C, int SW> int solve_impl(tlr_ctx *ctx, void *x);
   template <class C, int SW> int rewrite_factors(tlr_ctx *ctx);
+  template <class C, int SW> int solve_persistent(tlr_ctx *ctx);
+  int build_phases(tlr_ctx *ctx);
+  // error raised inside a persistent solve since the last call (a grid
+  // barrier that gave up); resets the flag
+  int take_solve_error(tlr_ctx *ctx);
 };
 
 }  // namespace tlr

@@ -225,6 +225,9 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
         so.cuda_core_schur = cs[c].cuda_core_schur;
         so.solve_block = cs[c].solve_block;
         so.start = pt.start;
+        // concurrent contexts replay solve graphs: a cooperative grid per
+        // worker could not count on having the GPU's SMs to itself
+        if (workers > 1) so.persistent_solve = 0;
         st = tlr_solve(ctx, &so, lam, res, nullptr, &d);
       }
       if (st) {

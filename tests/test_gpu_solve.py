@@ -42,3 +42,20 @@ def test_eigen_parity(gpu_lib, oracle, precision, shape):
     # the nev eigenvalues nearest the target, like EPS_TARGET_MAGNITUDE
     dist = np.sort(np.abs(lam_ref - sigma))[:6]
     assert np.allclose(np.sort(np.abs(sol.lam - sigma)), dist, rtol=1e-8)
+
+
+@pytest.mark.parametrize("kw", [dict(persistent_solve=True), dict(cuda_core_schur=True),
+                                dict(precision=0, persistent_solve=True)],
+                         ids=["persistent", "cuda-core-schur", "fp64-persistent"])
+def test_solver_variants_agree(gpu_lib, kw):
+    """The persistent (cooperative, grid-barrier) triangular solve and the
+    CUDA-core Schur update give the default path's eigenvalues."""
+    case = make_case(60, 32, physics=Physics(alpha=1.2, omega=complex(0.3, 0.01), nev=6))
+    prec = kw.pop("precision", 1)
+    with api.Problem(case) as prob:
+        api.run_pipeline(prob)
+        ref = api.EigenSolver(prob).solve(precision=prec)
+        alt = api.EigenSolver(prob).solve(precision=prec, **kw)
+    assert np.all(alt.residual <= 1e-10)
+    for lam in alt.lam:
+        assert np.min(np.abs(ref.lam - lam)) <= 1e-8 * abs(lam)
