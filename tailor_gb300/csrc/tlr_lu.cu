@@ -443,6 +443,15 @@ __global__ void __launch_bounds__(256)
 
 // ------------------------------------------------------------------ solves
 
+// Programmatic dependent launch: a solve kernel lets the next one launch
+// right away (launch_dependents) and waits for its predecessor's results
+// only where it reads them (wait); loads of factor data go out before the
+// wait.  Both are no-ops for a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Forward gather of one level: t[i] = b[unknown of front row perm[i]] for
 // pivot rows (0 for border rows), plus the children's updated border rows
 // that map to row i (cinv: absolute work index per child slot, -1: none),
@@ -452,6 +461,8 @@ __global__ void k_sgather(const int *__restrict__ fl, const DevFront *__restrict
                           const int *__restrict__ nodes, const int *__restrict__ perm,
                           const int2 *__restrict__ cinv, const C *__restrict__ b,
                           C *__restrict__ work) {
+  pdl_launch_dependents();
+  pdl_wait();
   const DevFront f = fr[fl[blockIdx.y]];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= f.m) return;
@@ -656,6 +667,7 @@ __global__ void __launch_bounds__(256)
                  const int *__restrict__ nodes, C *__restrict__ x) {
   __shared__ C vs[SW];
   __shared__ C red[8][32];
+  pdl_launch_dependents();
   const DevFront f = fr[fl[blockIdx.y]];
   const int b0 = b * SW, b1 = min(f.p, b0 + SW), nb = b1 - b0;
   const int lo = backward ? 0 : b1, hi = backward ? b0 : f.m;
@@ -672,6 +684,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
   for (int k = 0; k < kQ; ++k)
     fv[k] = (r < hi && q0 + k < nb) ? F[(long long)(q0 + k) * f.m + r] : czero<C>();
+  pdl_wait();
   for (int q = threadIdx.x; q < nb; q += blockDim.x) vs[q] = t[b0 + q];
   __syncthreads();
   C acc = czero<C>();
@@ -702,6 +715,8 @@ __global__ void __launch_bounds__(256)
                   const C *__restrict__ x, double2 *__restrict__ partial, int nck, int pmax) {
   __shared__ C xs[kBC];
   __shared__ C red[8][32];
+  pdl_launch_dependents();
+  pdl_wait();
   const int fq = blockIdx.z;
   const DevFront f = fr[fl[fq]];
   const int r0 = blockIdx.x * 32;
@@ -745,6 +760,7 @@ __global__ void __launch_bounds__(256)
                 const int *__restrict__ nodes, C *__restrict__ x) {
   __shared__ C zs[SW];
   __shared__ C red[8][32];
+  pdl_launch_dependents();
   const int fq = blockIdx.y, fid = fl[fq];
   const DevFront f = fr[fid];
   const int blk = blockIdx.x / (SW / 32), quarter = blockIdx.x % (SW / 32);
@@ -760,6 +776,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
   for (int k = 0; k < kQ; ++k)
     dv[k] = (rr < nb && q0 + k < nb) ? Dm[(long long)(q0 + k) * nb + rr] : czero<C>();
+  pdl_wait();
   const C *z = work + f.toff + b0;
   for (int q = threadIdx.x; q < nb; q += blockDim.x) zs[q] = z[q];
   __syncthreads();
@@ -992,6 +1009,24 @@ __global__ void __launch_bounds__(256)
       grid_barrier(barrier, target, err);
     }
   }
+}
+
+// launch, with programmatic stream serialisation when pdl (captured into
+// the graph as a programmatic dependency on the previous kernel)
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st,
+                       Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
 }  // namespace
@@ -1459,6 +1494,9 @@ int Factor::factor(tlr_ctx *ctx, double sr, double si, double tiny) {
 template <class C, int SW>
 int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
   cudaStream_t st = ctx->stream;
+  // programmatic dependent launch pays for the complex64 solve (about 7% at
+  // 200 x 128) but not for the register-heavier complex128 kernels
+  const bool pdl = sizeof(C) == sizeof(float2);
   const C *P = static_cast<const C *>(pool);
   C *W = static_cast<C *>(work);
   C *W2 = static_cast<C *>(work2);
@@ -1466,27 +1504,42 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
   for (size_t h = 0; h < levels.size(); ++h) {
     const Level &L = levels[h];
     const int *fl = d_sched + L.fronts_off;
-    { k_sgather<C><<<dim3(blocks_for(L.max_m, 128), L.nfronts), 128, 0, st>>>(
-        fl, d_fronts, d_nodes, d_perm, d_cinv, x, W); count_launches(); }
+    TLR_CUDA(ctx, launch_pdl(pdl, k_sgather<C>, dim3(blocks_for(L.max_m, 128), L.nfronts), dim3(128),
+                             st, fl, (const DevFront *)d_fronts, (const int *)d_nodes,
+                             (const int *)d_perm, (const int2 *)d_cinv, (const C *)x, W));
+    count_launches();
     for (int b = 0; b < (int)L.blk_nf.size(); ++b) {
       const int rows = L.fwd_rows[b];
-      if (rows > 0)
-        { k_blk_update<C, SW><<<dim3(blocks_for(rows, 32), L.blk_nf[b]), 256, 0, st>>>(
-            fl, b, 0, P, d_fronts, W, d_nodes, x); count_launches(); }
+      if (rows > 0) {
+        TLR_CUDA(ctx, launch_pdl(pdl, k_blk_update<C, SW>, dim3(blocks_for(rows, 32), L.blk_nf[b]),
+                                 dim3(256), st, fl, b, 0, P, (const DevFront *)d_fronts, W,
+                                 (const int *)d_nodes, x));
+        count_launches();
+      }
     }
   }
   for (int h = (int)levels.size() - 1; h >= 0; --h) {
     const Level &L = levels[h];
     const int *fl = d_sched + L.fronts_off;
-    if (L.bmax > 0)
-      { k_border_gemv<C><<<dim3(blocks_for(L.pmax, 32), L.nck_b, L.nfronts), 256, 0, st>>>(
-          fl, P, d_fronts, d_nodes, x, d_partial, L.nck_b, L.pmax); count_launches(); }
-    { k_bwd_start<C, SW><<<dim3((unsigned)L.blk_nf.size() * (SW / 32), L.nfronts), 256, 0, st>>>(
-        fl, d_fronts, d_inv_off, static_cast<const C *>(dmat), W, W2, d_partial, L.nck_b,
-        L.pmax, d_nodes, x); count_launches(); }
-    for (int b = (int)L.blk_nf.size() - 1; b >= 1; --b)
-      { k_blk_update<C, SW><<<dim3(blocks_for(b * SW, 32), L.blk_nf[b]), 256, 0, st>>>(
-          fl, b, 1, P, d_fronts, W2, d_nodes, x); count_launches(); }
+    if (L.bmax > 0) {
+      TLR_CUDA(ctx, launch_pdl(pdl, k_border_gemv<C>, dim3(blocks_for(L.pmax, 32), L.nck_b, L.nfronts),
+                               dim3(256), st, fl, P, (const DevFront *)d_fronts,
+                               (const int *)d_nodes, (const C *)x, d_partial, L.nck_b, L.pmax));
+      count_launches();
+    }
+    TLR_CUDA(ctx, launch_pdl(pdl, k_bwd_start<C, SW>,
+                             dim3((unsigned)L.blk_nf.size() * (SW / 32), L.nfronts), dim3(256), st,
+                             fl, (const DevFront *)d_fronts, (const long long *)d_inv_off,
+                             static_cast<const C *>(dmat), (const C *)W, W2,
+                             (const double2 *)d_partial, L.nck_b, L.pmax, (const int *)d_nodes,
+                             x));
+    count_launches();
+    for (int b = (int)L.blk_nf.size() - 1; b >= 1; --b) {
+      TLR_CUDA(ctx, launch_pdl(pdl, k_blk_update<C, SW>, dim3(blocks_for(b * SW, 32), L.blk_nf[b]),
+                               dim3(256), st, fl, b, 1, P, (const DevFront *)d_fronts, W2,
+                               (const int *)d_nodes, x));
+      count_launches();
+    }
   }
   TLR_CUDA(ctx, cudaGetLastError());
   return TLR_OK;
