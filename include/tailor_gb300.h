@@ -284,6 +284,9 @@ typedef struct {
   int grid_class;
   double alpha_re, alpha_im;
   const double *start;        /* optional complex [5N] start vector (NULL)    */
+  double reynolds;            /* > 0: overrides the class recipe's Reynolds
+                                 number (Mach stays a class property: the
+                                 base flow depends on it)                      */
 } tlr_sweep_point;
 
 typedef struct {

@@ -102,7 +102,8 @@ class GridClass(ctypes.Structure):
 
 class SweepPoint(ctypes.Structure):
     _fields_ = [("grid_class", ctypes.c_int), ("alpha_re", ctypes.c_double),
-                ("alpha_im", ctypes.c_double), ("start", ctypes.c_void_p)]
+                ("alpha_im", ctypes.c_double), ("start", ctypes.c_void_p),
+                ("reynolds", ctypes.c_double)]
 
 
 class SweepOpts(ctypes.Structure):

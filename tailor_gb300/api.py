@@ -16,7 +16,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib as L
-from .case import Case, target_lambda
+from .case import Case, rebuild_baseflow, target_lambda
 
 TLR_MAT_M, TLR_MAT_L, TLR_MAT_A, TLR_MAT_B = 0, 1, 2, 3
 (OUT_METRICS, OUT_DERIVS, OUT_ROW_PTR, OUT_COL, OUT_M, OUT_L, OUT_A,
@@ -116,8 +116,14 @@ class Problem:
                                           complex(omega).imag))
 
     def set_physics(self, physics) -> None:
-        """New Re / Mach / alpha / target on the same grid (re-assemble after)."""
+        """New Re / Mach / alpha / target on the same grid (re-run the stages
+        after).  The synthetic base flow depends on Mach (Crocco-Busemann
+        temperature), so a new Mach reloads it."""
+        mach_changed = physics.mach != self.case.physics.mach
         self.case.physics = physics
+        if mach_changed:
+            self.case.baseflow = rebuild_baseflow(self.case)
+            self.load_fields(self.case.grid, self.case.baseflow)
         r = make_recipe(self.case)
         self.check(self.lib.tlr_set_physics(self.ctx, ctypes.byref(r)))
 
@@ -251,8 +257,9 @@ class SweepResult:
 def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
           autotune: bool = True, tol: float = 0.0, ncv: int = 0, max_it: int = 0,
           starts=None, device: int = 0, raise_on_error: bool = True) -> SweepResult:
-    """Batched alpha-sweep (tlr_sweep): points are (class index, alpha); each
-    class is a Case (grid, base flow, physics) whose alpha is overridden."""
+    """Batched alpha-sweep (tlr_sweep): points are (class index, alpha) or
+    (class index, alpha, Re); each class is a Case (grid, base flow,
+    physics) whose alpha (and Re when given) is overridden."""
     lib = L.load()
     keep = []
     holder = Problem.__new__(Problem)  # reuse the rule marshalling
@@ -268,14 +275,16 @@ def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
                              case.ny, case.nz, case.spanwise_period, _ptr(g), _ptr(b))
     npts = len(points)
     pts = (L.SweepPoint * max(npts, 1))()
-    for i, (c, a) in enumerate(points):
+    for i, pt in enumerate(points):
+        c, a = pt[0], pt[1]
+        re_ov = float(pt[2]) if len(pt) > 2 else 0.0
         s = None
         if starts is not None and starts[i] is not None:
             v = np.ascontiguousarray(np.stack([starts[i].real, starts[i].imag], -1),
                                      dtype=np.float64)
             keep.append(v)
             s = v.ctypes.data
-        pts[i] = L.SweepPoint(int(c), complex(a).real, complex(a).imag, s)
+        pts[i] = L.SweepPoint(int(c), complex(a).real, complex(a).imag, s, re_ov)
     k = nev or cases[0].physics.nev
     opts = L.SweepOpts(L.SolveOpts(k, ncv, tol, max_it, precision, 0.0, 0.0, 0, None, 0, 0, 0),
                        workers, int(bool(autotune)), device)

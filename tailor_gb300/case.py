@@ -76,20 +76,34 @@ def make_case(ny: int, nz: int, qy: int = 10, qz: int = 6, amplitude=0.05,
     yw = amplitude * np.cos(beta * z + phase)
     ydist = 20.0 * np.sinh(3.0 * i / (ny - 1)) / math.sinh(3.0)
     y = yw[:, None] + ydist[None, :]                       # [nz, ny]
-    d = y - yw[:, None]
-    u = np.tanh(1.7 * d) * (1.0 + 0.1 * np.cos(beta * z)[:, None] *
-                            np.exp(-d * d / 4.0))
-    r = math.sqrt(physics.prandtl)
-    t = 1.0 + r * (physics.gamma - 1.0) / 2.0 * physics.mach ** 2 * (1.0 - u * u)
-    rho = 1.0 / t
     grid = np.zeros((nz * ny, 3, 2))
     grid[:, 1, 0] = y.reshape(-1)
     grid[:, 2, 0] = np.broadcast_to(z[:, None], (nz, ny)).reshape(-1)
+    base = _baseflow(y, yw, z, beta, physics)
+    return Case(ny, nz, qy, qz, xi, eta, lz, grid, base, physics)
+
+
+def _baseflow(y, yw, z, beta, physics) -> np.ndarray:
+    """U = tanh(1.7 d)(1 + 0.1 cos(beta z) exp(-d^2/4)), V = W = 0, Crocco-Busemann
+    T with T_w = T_aw, rho = 1/T; d = y - y_w.  Arrays [nz, ny] -> [N][5][2]."""
+    nz, ny = y.shape
+    d = y - yw[:, None]
+    u = np.tanh(1.7 * d) * (1.0 + 0.1 * np.cos(beta * z)[:, None] * np.exp(-d * d / 4.0))
+    r = math.sqrt(physics.prandtl)
+    t = 1.0 + r * (physics.gamma - 1.0) / 2.0 * physics.mach ** 2 * (1.0 - u * u)
     base = np.zeros((nz * ny, 5, 2))
-    base[:, 0, 0] = rho.reshape(-1)
+    base[:, 0, 0] = (1.0 / t).reshape(-1)
     base[:, 1, 0] = u.reshape(-1)
     base[:, 4, 0] = t.reshape(-1)
-    return Case(ny, nz, qy, qz, xi, eta, lz, grid, base, physics)
+    return base
+
+
+def rebuild_baseflow(case: Case) -> np.ndarray:
+    """The synthetic base flow of case's grid for case.physics (after a Mach
+    change); the wall y_w(z) is the grid's first wall-normal line."""
+    y = case.grid[:, 1, 0].reshape(case.nz, case.ny)
+    z = case.grid[:, 2, 0].reshape(case.nz, case.ny)[:, 0]
+    return _baseflow(y, y[:, 0].copy(), z, 2.0 * math.pi / case.spanwise_period, case.physics)
 
 
 def target_lambda(omega: complex) -> complex:

@@ -54,9 +54,16 @@ int make_context(const tlr_grid_class &gc, int device, tlr_ctx **out) {
   return TLR_OK;
 }
 
-int stage_point(tlr_ctx *ctx, const tlr_sweep_point &pt) {
-  int rc = tlr_set_alpha(ctx, pt.alpha_re, pt.alpha_im, ctx->recipe.omega_re,
-                         ctx->recipe.omega_im);
+int stage_point(tlr_ctx *ctx, const tlr_grid_class &gc, const tlr_sweep_point &pt) {
+  int rc = TLR_OK;
+  const double re = pt.reynolds > 0 ? pt.reynolds : gc.recipe->reynolds;
+  if (re != ctx->recipe.reynolds) {
+    tlr_recipe r = ctx->recipe;
+    r.reynolds = re;
+    rc = tlr_set_physics(ctx, &r);
+  }
+  if (!rc)
+    rc = tlr_set_alpha(ctx, pt.alpha_re, pt.alpha_im, ctx->recipe.omega_re, ctx->recipe.omega_im);
   tlr_operator_diag od;
   tlr_bc_diag bd;
   if (!rc) rc = tlr_assemble(ctx, &od);
@@ -167,7 +174,7 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
       break;
     }
     tlr_ctx *ctx = ctxs[0][c];
-    if ((rc = stage_point(ctx, points[first[c]]))) {
+    if ((rc = stage_point(ctx, classes[c], points[first[c]]))) {
       err = ctx->last_error;
       break;
     }
@@ -213,7 +220,7 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
         st = make_context(classes[c], opts->device, &ctx);
         if (!st) ctx->shared_sym = cs[c].sym.get();
       }
-      if (!st) st = stage_point(ctx, pt);
+      if (!st) st = stage_point(ctx, classes[c], pt);
       double *lam = lambda + (size_t)i * nev * 2;
       double *res = residual + (size_t)i * nev;
       std::fill(lam, lam + 2 * nev, 0.0);

@@ -56,3 +56,34 @@ def test_no_product_import_of_oracle():
     for p in (ROOT / "tailor_gb300").rglob("*.py"):
         txt = p.read_text()
         assert "import oracle" not in txt and "from oracle" not in txt, p
+
+
+def test_sweep_argument_checks_without_gpu():
+    """tlr_sweep rejects malformed sweeps before touching the device."""
+    import ctypes
+    from tailor_gb300 import _lib as L
+    tb.build()
+    lib = L.load()
+    gcs = (L.GridClass * 1)()
+    pts = (L.SweepPoint * 2)(L.SweepPoint(0, 1.0, 0.0, None, 0.0),
+                             L.SweepPoint(3, 2.0, 0.0, None, 0.0))
+    opts = L.SweepOpts()
+    lam = np.zeros(64)
+    res = np.zeros(32)
+    st = np.zeros(2, dtype=np.int32)
+    rc = lib.tlr_sweep(gcs, 1, pts, 2, ctypes.byref(opts), lam.ctypes.data, res.ctypes.data,
+                       st.ctypes.data, None, None)
+    assert rc == 1 and b"invalid grid class" in lib.tlr_last_error(None)
+    rc = lib.tlr_sweep(gcs, 0, pts, 2, ctypes.byref(opts), lam.ctypes.data, res.ctypes.data,
+                       st.ctypes.data, None, None)
+    assert rc == 1 and b"invalid sweep arguments" in lib.tlr_last_error(None)
+
+
+def test_rebuilt_baseflow_matches_synthetic_case():
+    """Mach changes reload the Crocco-Busemann base flow (api.Problem.set_physics)."""
+    from tailor_gb300.case import Physics, make_case, rebuild_baseflow
+    c = make_case(24, 16, physics=Physics(mach=0.5), amplitude=0.08)
+    assert np.array_equal(rebuild_baseflow(c), c.baseflow)
+    c.physics = Physics(mach=0.85)
+    assert np.array_equal(rebuild_baseflow(c),
+                          make_case(24, 16, physics=Physics(mach=0.85), amplitude=0.08).baseflow)
