@@ -196,7 +196,7 @@ typedef struct {
                              tensor cores (tcgen05, 3xTF32); 1 on the CUDA
                              cores (FP32 FMA)                                */
   int solve_block;        /* mixed form: diagonal-block size of the
-                             triangular solves, 128 or 256 (0: 256)          */
+                             triangular solves, 128, 256 or 512 (0: 256)     */
   int persistent_solve;   /* 0 (default): each triangular solve replays a
                              CUDA graph of per-step launches; 1: one
                              persistent cooperative launch with grid

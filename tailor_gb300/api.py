@@ -218,14 +218,15 @@ class EigenSolver:
     def solve(self, nev: int = 0, ncv: int = 0, tol: float = 0.0,
               max_it: int = 0, precision: int = 0, sigma: complex | None = None,
               start: np.ndarray | None = None, modes: bool = False,
-              cuda_core_schur: bool = False, persistent_solve: bool = False) -> EigenSolution:
+              cuda_core_schur: bool = False, persistent_solve: bool = False,
+              solve_block: int = 0) -> EigenSolution:
         ph = self.p.case.physics
         k = nev or ph.nev
         opts = L.SolveOpts(nev, ncv, tol, max_it, precision,
                            0.0 if sigma is None else complex(sigma).real,
                            0.0 if sigma is None else complex(sigma).imag,
-                           0 if sigma is None else 1, None, int(bool(cuda_core_schur)), 0,
-                           int(bool(persistent_solve)))
+                           0 if sigma is None else 1, None, int(bool(cuda_core_schur)),
+                           int(solve_block), int(bool(persistent_solve)))
         if start is not None:
             s = np.ascontiguousarray(np.stack([start.real, start.imag], -1),
                                      dtype=np.float64)

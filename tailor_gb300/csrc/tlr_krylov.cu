@@ -233,7 +233,8 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   const cd sigma = o.use_sigma ? cd(o.sigma_re, o.sigma_im) : target;
   const int prec = o.precision == 1 ? 1 : 0;
   const bool tc = prec == 1 && !o.cuda_core_schur;
-  const int sblock = prec == 1 && o.solve_block == 128 ? 128 : (prec == 1 ? 256 : 128);
+  const int sblock = prec == 0 ? 128
+                     : (o.solve_block == 128 || o.solve_block == 512 ? o.solve_block : 256);
 
   // factorisation (reused when sigma, precision and Schur kernel are unchanged)
   Factor *F = ctx->factor;

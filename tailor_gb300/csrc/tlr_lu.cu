@@ -600,12 +600,13 @@ __global__ void __launch_bounds__(256)
 }
 
 // Left product by inv(U_bb), in place over a tile of 32 columns (staged in
-// shared memory before any write); thread (row i, group h of the 256 / SW
-// groups) forms columns h, h + 256 / SW, ... of row i.  tiles: {front, block b, first column, kind}:
+// shared memory before any write); max(SW, 256) threads, thread (row i,
+// group h of the 256 / SW groups when SW < 256) forms columns h, h + H, ...
+// of row i.  tiles: {front, block b, first column, kind}:
 //   kind 0: U'(b rows, cols) = inv(U_bb) U(b rows, cols) inside the front;
 //   kind 1: D_b(:, cols) = inv(U_bb) inv(L_bb)(:, cols) into dmat.
 template <class C, int SW>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(SW > 256 ? SW : 256)
     k_scale_u(const int4 *__restrict__ tiles, C *__restrict__ pool,
               const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
               const C *__restrict__ Linv, const C *__restrict__ Uinv, C *__restrict__ dmat) {
@@ -636,8 +637,8 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   const C *Ui = Uinv + io;  // (i, q) at q nb + i, upper triangular
-  constexpr int H = 256 / SW;  // column groups over the 256 threads
-  const int i = threadIdx.x & (SW - 1), h = threadIdx.x / SW;
+  constexpr int H = SW >= 256 ? 1 : 256 / SW;  // column groups (max(SW, 256) threads)
+  const int i = threadIdx.x % SW, h = threadIdx.x / SW;
   C acc[kRT / H];
 #pragma unroll
   for (int k = 0; k < kRT / H; ++k) acc[k] = czero<C>();
@@ -1036,7 +1037,7 @@ cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block
 int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block) {
   prec = precision;
   w = precision == 0 ? 32 : 64;
-  sw = precision == 0 ? 128 : (solve_block == 128 ? 128 : 256);
+  sw = precision == 0 ? 128 : (solve_block == 128 || solve_block == 512 ? solve_block : 256);
   int rc;
   if (ctx->shared_sym) {
     sym = *ctx->shared_sym;  // analysis shared by every context of the grid class
@@ -1357,7 +1358,7 @@ int Factor::rewrite_factors(tlr_ctx *ctx) {
   TLR_CUDA(ctx, cudaFuncSetAttribute(k_scale_l<C, SW>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
   if (n_utiles > 0)
-    { k_scale_u<C, SW><<<(unsigned)n_utiles, 256, ssm, st>>>(d_utiles, P, d_fronts, d_inv_off, Li,
+    { k_scale_u<C, SW><<<(unsigned)n_utiles, SW > 256 ? SW : 256, ssm, st>>>(d_utiles, P, d_fronts, d_inv_off, Li,
                                                             Ui, static_cast<C *>(dmat)); count_launches(); }
   if (n_ltiles > 0)
     { k_scale_l<C, SW><<<(unsigned)n_ltiles, 256, ssm, st>>>(d_ltiles, P, d_fronts, d_inv_off,
@@ -1424,7 +1425,9 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
   if (n_inv_blocks > 0) {
     int rc;
     if constexpr (sizeof(C) == sizeof(float2))
-      rc = sw == 256 ? rewrite_factors<C, 256>(ctx) : rewrite_factors<C, 128>(ctx);
+      rc = sw == 512   ? rewrite_factors<C, 512>(ctx)
+           : sw == 256 ? rewrite_factors<C, 256>(ctx)
+                       : rewrite_factors<C, 128>(ctx);
     else
       rc = rewrite_factors<C, 128>(ctx);
     if (rc) return rc;
@@ -1559,8 +1562,9 @@ int Factor::solve(tlr_ctx *ctx, void *x) {
     }
     TLR_CUDA(ctx, cudaEventRecord(ev_pool[ev_used], st));
     const int rc = prec == 0 ? solve_persistent<double2, 128>(ctx)
-                             : (sw == 256 ? solve_persistent<float2, 256>(ctx)
-                                          : solve_persistent<float2, 128>(ctx));
+                             : (sw == 512   ? solve_persistent<float2, 512>(ctx)
+                                : sw == 256 ? solve_persistent<float2, 256>(ctx)
+                                            : solve_persistent<float2, 128>(ctx));
     if (rc) return rc;
     TLR_CUDA(ctx, cudaEventRecord(ev_pool[ev_used + 1], st));
     ev_used += 2;
@@ -1573,8 +1577,9 @@ int Factor::solve(tlr_ctx *ctx, void *x) {
     {
       CaptureScope cs;
       rc = prec == 0 ? solve_impl<double2, 128>(ctx, vec_a)
-                     : (sw == 256 ? solve_impl<float2, 256>(ctx, vec_a)
-                                  : solve_impl<float2, 128>(ctx, vec_a));
+                     : (sw == 512   ? solve_impl<float2, 512>(ctx, vec_a)
+                        : sw == 256 ? solve_impl<float2, 256>(ctx, vec_a)
+                                    : solve_impl<float2, 128>(ctx, vec_a));
     }
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(st, &g);

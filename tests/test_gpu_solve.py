@@ -45,11 +45,14 @@ def test_eigen_parity(gpu_lib, oracle, precision, shape):
 
 
 @pytest.mark.parametrize("kw", [dict(persistent_solve=True), dict(cuda_core_schur=True),
-                                dict(precision=0, persistent_solve=True)],
-                         ids=["persistent", "cuda-core-schur", "fp64-persistent"])
+                                dict(precision=0, persistent_solve=True), dict(solve_block=512),
+                                dict(solve_block=128)],
+                         ids=["persistent", "cuda-core-schur", "fp64-persistent", "block512",
+                              "block128"])
 def test_solver_variants_agree(gpu_lib, kw):
-    """The persistent (cooperative, grid-barrier) triangular solve and the
-    CUDA-core Schur update give the default path's eigenvalues."""
+    """The persistent (cooperative, grid-barrier) triangular solve, the
+    CUDA-core Schur update and the other diagonal-block sizes give the
+    default path's eigenvalues."""
     case = make_case(60, 32, physics=Physics(alpha=1.2, omega=complex(0.3, 0.01), nev=6))
     prec = kw.pop("precision", 1)
     with api.Problem(case) as prob:
