@@ -197,6 +197,11 @@ typedef struct {
                              cores (FP32 FMA)                                */
   int solve_block;        /* mixed form: diagonal-block size of the
                              triangular solves, 128, 256 or 512 (0: 256)     */
+  int refinement;         /* mixed form: 0 (default) classic iterative
+                             refinement; 1 FP64 GMRES-based refinement
+                             (right-preconditioned GMRES(4) with the
+                             complex64 LU: the same two inner solves per
+                             application here, and 9% slower)               */
   int persistent_solve;   /* 0 (default): each triangular solve replays a
                              CUDA graph of per-step launches; 1: one
                              persistent cooperative launch with grid

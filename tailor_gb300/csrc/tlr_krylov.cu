@@ -65,12 +65,16 @@ __global__ void k_axmy(long long n, const double2 *__restrict__ a, const double2
   }
 }
 
+constexpr int kGmresM = 4;  // inner iterations per GMRES-IR cycle
+
 struct Workspace {  // device buffers of the Krylov driver, owned by the context
   long long n = 0;
   int ncv = 0;
   double2 *V = nullptr, *w = nullptr, *y = nullptr, *r = nullptr, *aw = nullptr,
           *bw = nullptr, *hv = nullptr, *tmp = nullptr;
   float2 *x32 = nullptr;
+  double2 *gv = nullptr;    // GMRES-IR: kGmresM + 1 basis vectors, kGmresM preconditioned
+  double2 *zero = nullptr;  // a zero vector
 };
 
 struct Solver {
@@ -82,6 +86,8 @@ struct Solver {
   double2 *V = nullptr, *w = nullptr, *y = nullptr, *r = nullptr, *aw = nullptr,
           *bw = nullptr, *hv = nullptr, *tmp = nullptr;
   float2 *x32 = nullptr;
+  double2 *gv = nullptr, *zero = nullptr;
+  bool gmres = false;  // GMRES-IR, or classic iterative refinement (default)
   int solves = 0, refine = 0;
   double refine_tol = 1e-12;
   int max_refine = 30;
@@ -116,6 +122,114 @@ struct Solver {
     return TLR_OK;
   }
 
+  // z = M^-1 v through the complex64 factor (z, v FP64)
+  int precondition(const double2 *v, double2 *z) {
+    cudaStream_t st = ctx->stream;
+    const int blocks = blocks_for(n, 256);
+    { k_to32<<<blocks, 256, 0, st>>>(n, v, x32); count_launches(); }
+    int rc = F->solve(ctx, x32);
+    if (rc) return rc;
+    ++solves;
+    TLR_CUDA(ctx, cudaMemsetAsync(z, 0, n * sizeof(double2), st));
+    { k_add32<<<blocks, 256, 0, st>>>(n, x32, z); count_launches(); }
+    return TLR_OK;
+  }
+
+  // GMRES-based iterative refinement: right-preconditioned GMRES(kGmresM)
+  // in FP64 on K d = r with the complex64 LU as preconditioner, products
+  // K z in float-float, restarted from the updated iterate; the acceptance
+  // test is an FP64 residual ||y - K x|| <= 1e-12 ||y||.
+  int refine_gmres(const double2 *in, double2 *out, double ny) {
+    cudaStream_t st = ctx->stream;
+    double2 *Vg = gv, *Zg = gv + (size_t)(kGmresM + 1) * n;
+    auto Vj = [&](int j) { return reinterpret_cast<cuDoubleComplex *>(Vg + (size_t)j * n); };
+    auto Zj = [&](int j) { return Zg + (size_t)j * n; };
+    const cuDoubleComplex one = {1.0, 0.0}, zero1 = {0.0, 0.0}, mone = {-1.0, 0.0};
+    int rc;
+    int inner = 0;
+    for (int cycle = 0; inner < max_refine; ++cycle) {
+      // residual of the current iterate: float-float, confirmed in FP64
+      if ((rc = residual_ff(ctx, in, out, sr, si, r))) return rc;
+      double beta = nrm(r);
+      if (beta <= refine_tol * ny) {
+        if ((rc = residual64(in, out))) return rc;
+        beta = nrm(r);
+        if (beta <= refine_tol * ny) return TLR_OK;
+      }
+      const double inv = 1.0 / beta;
+      TLR_CUDA(ctx, cudaMemcpyAsync(Vg, r, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+      cublasZdscal(h, (int)n, &inv, Vj(0), 1);
+      std::vector<cd> H((kGmresM + 1) * kGmresM, 0.0), g(kGmresM + 1, 0.0);
+      std::vector<cd> cs(kGmresM), sn(kGmresM);
+      g[0] = beta;
+      int k = 0;
+      for (; k < kGmresM && inner < max_refine; ++k, ++inner) {
+        if ((rc = precondition(Vg + (size_t)k * n, Zj(k)))) return rc;
+        ++refine;
+        // kz = K z_k  (residual_ff with y = 0 gives -K z_k); out is the
+        // caller's vector, so the product lives in aw
+        double2 *kz = aw;
+        if ((rc = residual_ff(ctx, zero, Zj(k), sr, si, kz))) return rc;
+        cublasZdscal(h, (int)n, &mone.x, reinterpret_cast<cuDoubleComplex *>(kz), 1);
+        // two passes of classical Gram-Schmidt against V_0..V_k
+        std::vector<double2> hc(k + 1), hc2(k + 1);
+        for (int pass = 0; pass < 2; ++pass) {
+          cublasZgemv(h, CUBLAS_OP_C, (int)n, k + 1, &one, Vj(0), (int)n,
+                      reinterpret_cast<cuDoubleComplex *>(kz), 1, &zero1,
+                      reinterpret_cast<cuDoubleComplex *>(hv), 1);
+          cublasZgemv(h, CUBLAS_OP_N, (int)n, k + 1, &mone, Vj(0), (int)n,
+                      reinterpret_cast<cuDoubleComplex *>(hv), 1, &one,
+                      reinterpret_cast<cuDoubleComplex *>(kz), 1);
+          TLR_CUDA(ctx, cudaMemcpyAsync(pass ? hc2.data() : hc.data(), hv,
+                                        sizeof(double2) * (k + 1), cudaMemcpyDeviceToHost, st));
+        }
+        const double hn = nrm(kz);
+        TLR_CUDA(ctx, cudaStreamSynchronize(st));
+        for (int i = 0; i <= k; ++i)
+          H[i * kGmresM + k] = cd(hc[i].x + hc2[i].x, hc[i].y + hc2[i].y);
+        H[(k + 1) * kGmresM + k] = hn;
+        // previous rotations, then a new one zeroing H(k+1, k)
+        for (int i = 0; i < k; ++i) {
+          const cd a = H[i * kGmresM + k], b = H[(i + 1) * kGmresM + k];
+          H[i * kGmresM + k] = std::conj(cs[i]) * a + std::conj(sn[i]) * b;
+          H[(i + 1) * kGmresM + k] = -sn[i] * a + cs[i] * b;
+        }
+        const cd a = H[k * kGmresM + k], b = H[(k + 1) * kGmresM + k];
+        const double den = std::sqrt(std::norm(a) + std::norm(b));
+        cs[k] = den > 0 ? a / den : cd(1.0);
+        sn[k] = den > 0 ? b / den : cd(0.0);
+        H[k * kGmresM + k] = den;
+        H[(k + 1) * kGmresM + k] = 0.0;
+        g[k + 1] = -sn[k] * g[k];
+        g[k] = std::conj(cs[k]) * g[k];
+        if (!(hn > 0) || std::abs(g[k + 1]) <= 0.5 * refine_tol * ny) {
+          ++k;
+          ++inner;
+          break;
+        }
+        const double hinv = 1.0 / hn;
+        TLR_CUDA(ctx, cudaMemcpyAsync(Vg + (size_t)(k + 1) * n, kz, n * sizeof(double2),
+                                      cudaMemcpyDeviceToDevice, st));
+        cublasZdscal(h, (int)n, &hinv, Vj(k + 1), 1);
+      }
+      // x += Z y with H(0:k, 0:k) y = g(0:k)
+      std::vector<cd> yk(k);
+      for (int i = k - 1; i >= 0; --i) {
+        cd v = g[i];
+        for (int j = i + 1; j < k; ++j) v -= H[i * kGmresM + j] * yk[j];
+        yk[i] = v / H[i * kGmresM + i];
+      }
+      for (int i = 0; i < k; ++i) {
+        const cuDoubleComplex c = {yk[i].real(), yk[i].imag()};
+        cublasZaxpy(h, (int)n, &c, reinterpret_cast<cuDoubleComplex *>(Zj(i)), 1,
+                    reinterpret_cast<cuDoubleComplex *>(out), 1);
+      }
+    }
+    // out of iterations: report the final FP64 residual through the caller's
+    // explicit eigen residual checks
+    return TLR_OK;
+  }
+
   int apply_inverse_impl(const double2 *in, double2 *out) {
     cudaStream_t st = ctx->stream;
     const int blocks = blocks_for(n, 256);
@@ -133,6 +247,7 @@ struct Solver {
     TLR_CUDA(ctx, cudaMemsetAsync(out, 0, n * sizeof(double2), st));
     { k_add32<<<blocks, 256, 0, st>>>(n, x32, out); count_launches(); }
     const double ny = nrm(in);
+    if (gmres) return refine_gmres(in, out, ny);
     // Residuals in float-float (FP32 pipe) drive the corrections; the
     // acceptance test is always an FP64 residual.  If the float-float
     // residual stops decreasing (its rounding floor), switch to FP64.
@@ -193,6 +308,7 @@ void free_workspace(tlr_ctx *ctx) {
     Workspace *ws = static_cast<Workspace *>(ctx->kws);
     cudaFree(ws->V); cudaFree(ws->w); cudaFree(ws->y); cudaFree(ws->r); cudaFree(ws->aw);
     cudaFree(ws->bw); cudaFree(ws->hv); cudaFree(ws->tmp); cudaFree(ws->x32);
+    cudaFree(ws->gv); cudaFree(ws->zero);
     delete ws;
     ctx->kws = nullptr;
   }
@@ -316,6 +432,9 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     TLR_CUDA(ctx, cudaMalloc(&ws->hv, sizeof(double2) * (ncv + 1) * (ncv + 1)));
     TLR_CUDA(ctx, cudaMalloc(&ws->tmp, vb * ncv));
     TLR_CUDA(ctx, cudaMalloc(&ws->x32, n * sizeof(float2)));
+    TLR_CUDA(ctx, cudaMalloc(&ws->gv, vb * (2 * kGmresM + 1)));
+    TLR_CUDA(ctx, cudaMalloc(&ws->zero, vb));
+    TLR_CUDA(ctx, cudaMemset(ws->zero, 0, vb));
   }
   S.V = ws->V;
   S.w = ws->w;
@@ -326,6 +445,9 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   S.hv = ws->hv;
   S.tmp = ws->tmp;
   S.x32 = ws->x32;
+  S.gv = ws->gv;
+  S.zero = ws->zero;
+  S.gmres = o.refinement == 1;
 
   std::vector<double2> v0(n);
   if (o.start) {

@@ -46,9 +46,9 @@ def test_eigen_parity(gpu_lib, oracle, precision, shape):
 
 @pytest.mark.parametrize("kw", [dict(persistent_solve=True), dict(cuda_core_schur=True),
                                 dict(precision=0, persistent_solve=True), dict(solve_block=512),
-                                dict(solve_block=128)],
+                                dict(solve_block=128), dict(refinement="gmres")],
                          ids=["persistent", "cuda-core-schur", "fp64-persistent", "block512",
-                              "block128"])
+                              "block128", "gmres-ir"])
 def test_solver_variants_agree(gpu_lib, kw):
     """The persistent (cooperative, grid-barrier) triangular solve, the
     CUDA-core Schur update and the other diagonal-block sizes give the
