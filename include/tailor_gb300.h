@@ -224,6 +224,8 @@ typedef struct {
   double ortho_ms;        /* Gram-Schmidt of the Arnoldi steps (host clock) */
   double dense_ms;        /* projected Schur problem on the host            */
   double residual_ms;     /* Ritz vectors and explicit residuals            */
+  double refine_res[3];   /* mixed form: largest ||r|| / ||y|| seen after the
+                             first solve, the first and the second correction */
 } tlr_eig_diag;
 
 /* lambda [nev] complex, residual [nev]; modes [nev][5N] complex or NULL. */

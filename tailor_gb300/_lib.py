@@ -91,7 +91,7 @@ class EigDiag(ctypes.Structure):
                 ("solve_ms", ctypes.c_double), ("factor_bytes", ctypes.c_double),
                 ("trisolve_ms", ctypes.c_double), ("trisolves", ctypes.c_int),
                 ("ortho_ms", ctypes.c_double), ("dense_ms", ctypes.c_double),
-                ("residual_ms", ctypes.c_double)]
+                ("residual_ms", ctypes.c_double), ("refine_res", ctypes.c_double * 3)]
 
 
 class GridClass(ctypes.Structure):

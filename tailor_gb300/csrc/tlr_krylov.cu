@@ -89,6 +89,7 @@ struct Solver {
   double2 *gv = nullptr, *zero = nullptr;
   bool gmres = false;  // GMRES-IR, or classic iterative refinement (default)
   int solves = 0, refine = 0;
+  double refine_res[3] = {0, 0, 0};  // largest ||r|| / ||y|| after solve 1, 2, 3
   double refine_tol = 1e-12;
   int max_refine = 30;
 
@@ -100,15 +101,108 @@ struct Solver {
   }
 
   double solve_ms = 0.0;
+  // CUDA events around every K^-1 application (no host synchronisation on
+  // the hot path); summed into solve_ms by collect_solve_ms()
+  std::vector<cudaEvent_t> evs;
+  size_t ev_n = 0;
 
   // out = K^-1 in (FP64 vectors); in may alias nothing else
   int apply_inverse(const double2 *in, double2 *out) {
-    TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    const auto t0 = std::chrono::steady_clock::now();
+    if (ev_n + 2 > evs.size()) {
+      cudaEvent_t a, b;
+      TLR_CUDA(ctx, cudaEventCreate(&a));
+      TLR_CUDA(ctx, cudaEventCreate(&b));
+      evs.push_back(a);
+      evs.push_back(b);
+    }
+    TLR_CUDA(ctx, cudaEventRecord(evs[ev_n], ctx->stream));
     const int rc = apply_inverse_impl(in, out);
-    TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    solve_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    TLR_CUDA(ctx, cudaEventRecord(evs[ev_n + 1], ctx->stream));
+    ev_n += 2;
     return rc;
+  }
+
+  void collect_solve_ms() {
+    if (ev_n) cudaEventSynchronize(evs[ev_n - 1]);
+    for (size_t i = 0; i + 1 < ev_n; i += 2) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, evs[i], evs[i + 1]) == cudaSuccess) solve_ms += ms;
+    }
+    ev_n = 0;
+  }
+
+  // Refinement graph: the fixed sequence solve - correction - correction -
+  // FP64 residual captured once per (in, out) pair and replayed; the host
+  // synchronises once per application, for the acceptance norm.  Every
+  // application so far needed exactly two corrections; when the accepted
+  // residual is still too large, the dynamic loop continues.
+  bool use_ref_graph = true;
+  cudaGraphExec_t ref_exec = nullptr;
+  long long ref_kernels = 0;
+  const double2 *ref_in = nullptr;
+  double2 *ref_out = nullptr;
+  cudaEvent_t rev[6] = {};
+  double tri_ms = 0.0;
+  int tri_n = 0;
+
+  ~Solver() {
+    for (cudaEvent_t e : evs) cudaEventDestroy(e);
+    for (cudaEvent_t e : rev)
+      if (e) cudaEventDestroy(e);
+    if (ref_exec) cudaGraphExecDestroy(ref_exec);
+  }
+
+  int build_ref_graph(const double2 *in, double2 *out) {
+    cudaStream_t st = ctx->stream;
+    const int blocks = blocks_for(n, 256);
+    int rc = prepare_ff(ctx);
+    if (rc) return rc;
+    for (auto &e : rev)
+      if (!e) TLR_CUDA(ctx, cudaEventCreate(&e));
+    if (ref_exec) {
+      cudaGraphExecDestroy(ref_exec);
+      ref_exec = nullptr;
+    }
+    TLR_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    {
+      CaptureScope cs;
+      k_to32<<<blocks, 256, 0, st>>>(n, in, x32);
+      rc = F->enqueue_solve(ctx, x32, rev[0], rev[1]);
+      if (!rc) rc = cudaMemsetAsync(out, 0, n * sizeof(double2), st) == cudaSuccess ? 0 : TLR_ERR_CUDA;
+      if (!rc) k_add32<<<blocks, 256, 0, st>>>(n, x32, out);
+      for (int q = 1; q < 3 && !rc; ++q) {
+        rc = residual_ff(ctx, in, out, sr, si, r);
+        if (rc) break;
+        k_to32<<<blocks, 256, 0, st>>>(n, r, x32);
+        rc = F->enqueue_solve(ctx, x32, rev[2 * q], rev[2 * q + 1]);
+        if (!rc) k_add32<<<blocks, 256, 0, st>>>(n, x32, out);
+      }
+      if (!rc) rc = residual64(in, out);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture (refinement)");
+    size_t nn = 0;
+    ref_kernels = 0;
+    if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn > 0) {
+      std::vector<cudaGraphNode_t> nodes(nn);
+      if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+        for (size_t i = 0; i < nn; ++i) {
+          cudaGraphNodeType t;
+          if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+            ++ref_kernels;
+        }
+    }
+    const cudaError_t e2 = cudaGraphInstantiate(&ref_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaGraphInstantiate (refinement)");
+    ref_in = in;
+    ref_out = out;
+    return TLR_OK;
   }
 
   bool use_ff = true;  // float-float residuals between FP64 acceptance tests
@@ -240,6 +334,28 @@ struct Solver {
       return rc;
     }
     // FP32 factor + FP64 iterative refinement
+    if (!gmres && use_ref_graph && !F->persistent) {
+      int rc;
+      if (!ref_exec || in != ref_in || out != ref_out)
+        if ((rc = build_ref_graph(in, out))) return rc;
+      TLR_CUDA(ctx, cudaGraphLaunch(ref_exec, st));
+      count_launches(ref_kernels);
+      solves += 3;
+      refine += 2;
+      const double nr = nrm(r), ny = nrm(in);  // synchronises
+      for (int q = 0; q < 3; ++q) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, rev[2 * q], rev[2 * q + 1]) == cudaSuccess) {
+          tri_ms += ms;
+          ++tri_n;
+        } else {
+          cudaGetLastError();  // not a failure of the solve: no timing this time
+        }
+      }
+      refine_res[2] = std::max(refine_res[2], nr / ny);
+      if (nr <= refine_tol * ny) return TLR_OK;
+      return refine_loop(in, out, ny);
+    }
     { k_to32<<<blocks, 256, 0, st>>>(n, in, x32); count_launches(); }
     int rc = F->solve(ctx, x32);
     if (rc) return rc;
@@ -248,6 +364,14 @@ struct Solver {
     { k_add32<<<blocks, 256, 0, st>>>(n, x32, out); count_launches(); }
     const double ny = nrm(in);
     if (gmres) return refine_gmres(in, out, ny);
+    return refine_loop(in, out, ny);
+  }
+
+  // classic refinement from the iterate in out until ||y - K out|| <= tol ||y||
+  int refine_loop(const double2 *in, double2 *out, double ny) {
+    cudaStream_t st = ctx->stream;
+    const int blocks = blocks_for(n, 256);
+    int rc;
     // Residuals in float-float (FP32 pipe) drive the corrections; the
     // acceptance test is always an FP64 residual.  If the float-float
     // residual stops decreasing (its rounding floor), switch to FP64.
@@ -268,6 +392,7 @@ struct Solver {
         if ((rc = residual64(in, out))) return rc;
         nr = nrm(r);
       }
+      if (it < 3) refine_res[it] = std::max(refine_res[it], nr / ny);
       if (nr <= refine_tol * ny) break;
       { k_to32<<<blocks, 256, 0, st>>>(n, r, x32); count_launches(); }
       if ((rc = F->solve(ctx, x32))) return rc;
@@ -331,6 +456,7 @@ void free_factor(tlr_ctx *ctx) {
 
 int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
               double *residual, double *modes, tlr_eig_diag *diag) {
+  cudaGetLastError();  // a stale, non-sticky error of an earlier failed call
   using clock = std::chrono::steady_clock;
   const auto t0 = clock::now();
   tlr_solve_opts o{};
@@ -660,12 +786,15 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     d.krylov_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
     d.total_ms = std::chrono::duration<double, std::milli>(t3 - t0).count();
     d.factor_flops = F->sym.flops;
+    S.collect_solve_ms();
     d.solve_ms = S.solve_ms;
     d.factor_bytes = (double)F->sym.factor_elems * (prec == 0 ? 16.0 : 8.0);
-    d.trisolve_ms = F->take_solve_time(&d.trisolves);
+    d.trisolve_ms = F->take_solve_time(&d.trisolves) + S.tri_ms;
+    d.trisolves += S.tri_n;
     d.ortho_ms = ortho_ms;
     d.dense_ms = dense_ms;
     d.residual_ms = residual_ms;
+    for (int q = 0; q < 3; ++q) d.refine_res[q] = S.refine_res[q];
     *diag = d;
   }
   if (reason != 1) {

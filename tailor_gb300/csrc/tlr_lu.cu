@@ -1507,7 +1507,9 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
   for (size_t h = 0; h < levels.size(); ++h) {
     const Level &L = levels[h];
     const int *fl = d_sched + L.fronts_off;
-    TLR_CUDA(ctx, launch_pdl(pdl, k_sgather<C>, dim3(blocks_for(L.max_m, 128), L.nfronts), dim3(128),
+    // the first kernel follows a copy (or an event) node, not a kernel: no
+    // programmatic edge for it
+    TLR_CUDA(ctx, launch_pdl(pdl && h > 0, k_sgather<C>, dim3(blocks_for(L.max_m, 128), L.nfronts), dim3(128),
                              st, fl, (const DevFront *)d_fronts, (const int *)d_nodes,
                              (const int *)d_perm, (const int2 *)d_cinv, (const C *)x, W));
     count_launches();
@@ -1545,6 +1547,23 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
     }
   }
   TLR_CUDA(ctx, cudaGetLastError());
+  return TLR_OK;
+}
+
+int Factor::enqueue_solve(tlr_ctx *ctx, void *x, cudaEvent_t a, cudaEvent_t b) {
+  const size_t bytes = (size_t)sym.nn * 5 * (prec == 0 ? sizeof(double2) : sizeof(float2));
+  cudaStream_t st = ctx->stream;
+  TLR_CUDA(ctx, cudaMemcpyAsync(vec_a, x, bytes, cudaMemcpyDeviceToDevice, st));
+  // external event nodes: the events are recorded (with time stamps) on
+  // every replay of the caller's graph
+  if (a) TLR_CUDA(ctx, cudaEventRecordWithFlags(a, st, cudaEventRecordExternal));
+  const int rc = prec == 0 ? solve_impl<double2, 128>(ctx, vec_a)
+                           : (sw == 512   ? solve_impl<float2, 512>(ctx, vec_a)
+                              : sw == 256 ? solve_impl<float2, 256>(ctx, vec_a)
+                                          : solve_impl<float2, 128>(ctx, vec_a));
+  if (rc) return rc;
+  if (b) TLR_CUDA(ctx, cudaEventRecordWithFlags(b, st, cudaEventRecordExternal));
+  TLR_CUDA(ctx, cudaMemcpyAsync(x, vec_a, bytes, cudaMemcpyDeviceToDevice, st));
   return TLR_OK;
 }
 

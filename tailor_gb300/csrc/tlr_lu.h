@@ -81,6 +81,10 @@ struct Factor {
   int factor(tlr_ctx *ctx, double sr, double si, double tiny);
   // In-place x <- K^-1 x on a device vector in the factor's precision.
   int solve(tlr_ctx *ctx, void *x);
+  // Enqueue one solve's kernels on the context stream without a graph
+  // (for capture into a caller's graph); events a/b, when given, bracket
+  // the triangular solve.
+  int enqueue_solve(tlr_ctx *ctx, void *x, cudaEvent_t a, cudaEvent_t b);
 
   template <class C> int factor_impl(tlr_ctx *ctx, double sr, double si, double tiny);
   template <class C, int SW> int solve_impl(tlr_ctx *ctx, void *x);

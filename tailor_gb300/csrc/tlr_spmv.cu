@@ -208,8 +208,7 @@ __global__ void __launch_bounds__(32 * kRowsPerCta)
 
 }  // namespace
 
-int residual_ff(tlr_ctx *ctx, const double2 *y, const double2 *w, double sr, double si,
-                double2 *r) {
+int prepare_ff(tlr_ctx *ctx) {
   const long long nv = ctx->nnzb * 25;
   if (!ctx->aff) TLR_CUDA(ctx, cudaMalloc(&ctx->aff, (size_t)nv * sizeof(float4)));
   const long long n = 5LL * ctx->nn;
@@ -218,6 +217,14 @@ int residual_ff(tlr_ctx *ctx, const double2 *y, const double2 *w, double sr, dou
     { k_split_ff<<<blocks_for(nv, 256), 256, 0, ctx->stream>>>(nv, ctx->A, ctx->aff); count_launches(); }
     ctx->aff_valid = true;
   }
+  return TLR_OK;
+}
+
+int residual_ff(tlr_ctx *ctx, const double2 *y, const double2 *w, double sr, double si,
+                double2 *r) {
+  int rc = prepare_ff(ctx);
+  if (rc) return rc;
+  const long long n = 5LL * ctx->nn;
   { k_split_ff<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, w, ctx->wff); count_launches(); }
   { k_residual_ff<<<blocks_for(ctx->nn, kRowsPerCta), 32 * kRowsPerCta, 0, ctx->stream>>>(
       ctx->nn, ctx->row_ptr, ctx->col, ctx->aff, ctx->B, ctx->wff, w, y, sr, si, r); count_launches(); }
