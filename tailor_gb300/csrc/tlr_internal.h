@@ -141,6 +141,10 @@ int frobenius(tlr_ctx *ctx, const double2 *v, long long count, double *out);
 // FP32 pipe (about 48-bit significands); builds ctx->aff on first use.
 int residual_ff(tlr_ctx *ctx, const double2 *y, const double2 *w, double sr, double si,
                 double2 *r);
+// ||v||_2 into device memory out (scratch: ctx->partial_blocks doubles),
+// stream-ordered, no host synchronisation (capturable).
+int vec_norm_async(tlr_ctx *ctx, const double2 *v, long long count, double *scratch,
+                   double *out);
 // Allocate and fill ctx->aff / ctx->wff if needed (outside stream capture).
 int prepare_ff(tlr_ctx *ctx);
 int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,

@@ -75,6 +75,8 @@ struct Workspace {  // device buffers of the Krylov driver, owned by the context
   float2 *x32 = nullptr;
   double2 *gv = nullptr;    // GMRES-IR: kGmresM + 1 basis vectors, kGmresM preconditioned
   double2 *zero = nullptr;  // a zero vector
+  double *nscratch = nullptr;  // two norm reductions: 2 x (blocks + 1) doubles
+  double *hnorm = nullptr;     // pinned host copy of the two norms
 };
 
 struct Solver {
@@ -87,6 +89,7 @@ struct Solver {
           *bw = nullptr, *hv = nullptr, *tmp = nullptr;
   float2 *x32 = nullptr;
   double2 *gv = nullptr, *zero = nullptr;
+  double *nscratch = nullptr, *hnorm = nullptr;
   bool gmres = false;  // GMRES-IR, or classic iterative refinement (default)
   int solves = 0, refine = 0;
   double refine_res[3] = {0, 0, 0};  // largest ||r|| / ||y|| after solve 1, 2, 3
@@ -178,6 +181,15 @@ struct Solver {
         if (!rc) k_add32<<<blocks, 256, 0, st>>>(n, x32, out);
       }
       if (!rc) rc = residual64(in, out);
+      // ||r|| and ||in|| to pinned host memory: one synchronisation per application
+      const int nb = ctx->partial_blocks;
+      double *s0 = nscratch, *s1 = nscratch + nb + 1;
+      if (!rc) rc = vec_norm_async(ctx, r, n, s0, s0 + nb);
+      if (!rc) rc = vec_norm_async(ctx, in, n, s1, s1 + nb);
+      if (!rc && cudaMemcpyAsync(hnorm, s0 + nb, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        rc = TLR_ERR_CUDA;
+      if (!rc && cudaMemcpyAsync(hnorm + 1, s1 + nb, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        rc = TLR_ERR_CUDA;
     }
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(st, &g);
@@ -342,7 +354,8 @@ struct Solver {
       count_launches(ref_kernels);
       solves += 3;
       refine += 2;
-      const double nr = nrm(r), ny = nrm(in);  // synchronises
+      TLR_CUDA(ctx, cudaStreamSynchronize(st));
+      const double nr = hnorm[0], ny = hnorm[1];
       for (int q = 0; q < 3; ++q) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, rev[2 * q], rev[2 * q + 1]) == cudaSuccess) {
@@ -433,7 +446,7 @@ void free_workspace(tlr_ctx *ctx) {
     Workspace *ws = static_cast<Workspace *>(ctx->kws);
     cudaFree(ws->V); cudaFree(ws->w); cudaFree(ws->y); cudaFree(ws->r); cudaFree(ws->aw);
     cudaFree(ws->bw); cudaFree(ws->hv); cudaFree(ws->tmp); cudaFree(ws->x32);
-    cudaFree(ws->gv); cudaFree(ws->zero);
+    cudaFree(ws->gv); cudaFree(ws->zero); cudaFree(ws->nscratch); cudaFreeHost(ws->hnorm);
     delete ws;
     ctx->kws = nullptr;
   }
@@ -561,6 +574,8 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     TLR_CUDA(ctx, cudaMalloc(&ws->gv, vb * (2 * kGmresM + 1)));
     TLR_CUDA(ctx, cudaMalloc(&ws->zero, vb));
     TLR_CUDA(ctx, cudaMemset(ws->zero, 0, vb));
+    TLR_CUDA(ctx, cudaMalloc(&ws->nscratch, sizeof(double) * 2 * (ctx->partial_blocks + 1)));
+    TLR_CUDA(ctx, cudaHostAlloc(&ws->hnorm, 2 * sizeof(double), cudaHostAllocDefault));
   }
   S.V = ws->V;
   S.w = ws->w;
@@ -573,6 +588,8 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   S.x32 = ws->x32;
   S.gv = ws->gv;
   S.zero = ws->zero;
+  S.nscratch = ws->nscratch;
+  S.hnorm = ws->hnorm;
   S.gmres = o.refinement == 1;
 
   std::vector<double2> v0(n);

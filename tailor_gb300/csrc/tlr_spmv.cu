@@ -232,6 +232,14 @@ int residual_ff(tlr_ctx *ctx, const double2 *y, const double2 *w, double sr, dou
   return TLR_OK;
 }
 
+int vec_norm_async(tlr_ctx *ctx, const double2 *v, long long count, double *scratch,
+                   double *out) {
+  const int blocks = ctx->partial_blocks;
+  { k_sq2_partial<<<blocks, 256, 0, ctx->stream>>>(count, v, scratch); count_launches(); }
+  { k_sum_sqrt<<<1, 32, 0, ctx->stream>>>(blocks, scratch, out); count_launches(); }
+  return TLR_OK;
+}
+
 int frobenius(tlr_ctx *ctx, const double2 *v, long long count, double *out) {
   const int blocks = ctx->partial_blocks;
   { k_sq2_partial<<<blocks, 256, 0, ctx->stream>>>(count, v, ctx->partial); count_launches(); }
