@@ -147,7 +147,7 @@ def run_c3(api, npoints=64):
     cases, points = c3_sweep_inputs(npoints)
     out = {}
     for name, kw in (("plain_fp64", dict(precision=0, workers=1, autotune=False)),
-                     ("mixed_batched", dict(precision=1, workers=6, autotune=True))):
+                     ("mixed_batched", dict(precision=1, workers=8, autotune=True))):
         t = time.perf_counter()
         r = api.sweep(cases, points, nev=8, ncv=32, raise_on_error=False, **kw)
         wall = time.perf_counter() - t

@@ -298,7 +298,7 @@ typedef struct {
 
 typedef struct {
   tlr_solve_opts solve;       /* shared solve options (start is ignored)      */
-  int workers;                /* concurrent instances (0: 6)                  */
+  int workers;                /* concurrent instances (0: 8)                  */
   int autotune;               /* mixed form: time both Schur-update kernels
                                  and both solve block sizes on each class's
                                  first point and keep the fastest             */

@@ -77,6 +77,8 @@ struct Workspace {  // device buffers of the Krylov driver, owned by the context
   double2 *zero = nullptr;  // a zero vector
   double *nscratch = nullptr;  // two norm reductions: 2 x (blocks + 1) doubles
   double *hnorm = nullptr;     // pinned host copy of the two norms
+  double2 *hpin = nullptr;     // pinned: Gram-Schmidt coefficients (2 passes) and beta
+  double *ascratch = nullptr;  // norm reduction of the Arnoldi vector
 };
 
 struct Solver {
@@ -447,6 +449,7 @@ void free_workspace(tlr_ctx *ctx) {
     cudaFree(ws->V); cudaFree(ws->w); cudaFree(ws->y); cudaFree(ws->r); cudaFree(ws->aw);
     cudaFree(ws->bw); cudaFree(ws->hv); cudaFree(ws->tmp); cudaFree(ws->x32);
     cudaFree(ws->gv); cudaFree(ws->zero); cudaFree(ws->nscratch); cudaFreeHost(ws->hnorm);
+    cudaFreeHost(ws->hpin); cudaFree(ws->ascratch);
     delete ws;
     ctx->kws = nullptr;
   }
@@ -576,6 +579,9 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     TLR_CUDA(ctx, cudaMemset(ws->zero, 0, vb));
     TLR_CUDA(ctx, cudaMalloc(&ws->nscratch, sizeof(double) * 2 * (ctx->partial_blocks + 1)));
     TLR_CUDA(ctx, cudaHostAlloc(&ws->hnorm, 2 * sizeof(double), cudaHostAllocDefault));
+    TLR_CUDA(ctx, cudaHostAlloc(&ws->hpin, sizeof(double2) * (2 * (ncv + 1) + 1),
+                                cudaHostAllocDefault));
+    TLR_CUDA(ctx, cudaMalloc(&ws->ascratch, sizeof(double) * (ctx->partial_blocks + 1)));
   }
   S.V = ws->V;
   S.w = ws->w;
@@ -670,6 +676,9 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
       int rc = S.op(S.V + (size_t)j * n, S.w);
       if (rc) return rc;
       const auto to = clock::now();
+      // two passes of classical Gram-Schmidt; coefficients and ||w|| land in
+      // pinned memory and the host waits once
+      double2 *h1 = ws->hpin, *h2 = ws->hpin + (ncv + 1), *hb = ws->hpin + 2 * (ncv + 1);
       for (int pass = 0; pass < 2; ++pass) {
         cublasZgemv(S.h, CUBLAS_OP_C, (int)n, j + 1, &one, Vc(0), (int)n,
                     reinterpret_cast<cuDoubleComplex *>(S.w), 1, &zero,
@@ -677,13 +686,19 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
         cublasZgemv(S.h, CUBLAS_OP_N, (int)n, j + 1, &mone, Vc(0), (int)n,
                     reinterpret_cast<cuDoubleComplex *>(S.hv), 1, &one,
                     reinterpret_cast<cuDoubleComplex *>(S.w), 1);
-        TLR_CUDA(ctx, cudaMemcpyAsync(pass ? hcol2.data() : hcol.data(), S.hv,
-                                      sizeof(double2) * (j + 1), cudaMemcpyDeviceToHost,
-                                      ctx->stream));
+        TLR_CUDA(ctx, cudaMemcpyAsync(pass ? h2 : h1, S.hv, sizeof(double2) * (j + 1),
+                                      cudaMemcpyDeviceToHost, ctx->stream));
       }
-      const double beta = S.nrm(S.w);
+      {
+        const int nb = ctx->partial_blocks;
+        int rc2 = vec_norm_async(ctx, S.w, n, ws->ascratch, ws->ascratch + nb);
+        if (rc2) return rc2;
+        TLR_CUDA(ctx, cudaMemcpyAsync(&hb->x, ws->ascratch + nb, sizeof(double),
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+      }
       TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-      for (int i = 0; i <= j; ++i) H(i, j) = hcol[i] + hcol2[i];
+      const double beta = hb->x;
+      for (int i = 0; i <= j; ++i) H(i, j) = cd(h1[i].x + h2[i].x, h1[i].y + h2[i].y);
       H(j + 1, j) = beta;
       if (!(beta > 0)) return fail(ctx, TLR_ERR_NOT_CONVERGED, "Arnoldi breakdown");
       const double inv = 1.0 / beta;

@@ -153,7 +153,7 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
   const auto t0 = clock::now();
   const tlr_solve_opts base = opts->solve;
   const int nev = base.nev > 0 ? base.nev : classes[0].recipe->nev;
-  const int workers = std::max(1, std::min(opts->workers > 0 ? opts->workers : 6,
+  const int workers = std::max(1, std::min(opts->workers > 0 ? opts->workers : 8,
                                            std::max(npoints, 1)));
   std::vector<ClassState> cs(nclass);
   std::vector<std::vector<tlr_ctx *>> ctxs(workers, std::vector<tlr_ctx *>(nclass, nullptr));
