@@ -202,6 +202,8 @@ typedef struct {
                              (right-preconditioned GMRES(4) with the
                              complex64 LU: the same two inner solves per
                              application here, and 9% slower)               */
+  int panel_width;        /* panel columns of the factorisation: 32, 64 or
+                             128 (0: 32 for complex128, 64 for complex64)    */
   int persistent_solve;   /* 0 (default): each triangular solve replays a
                              CUDA graph of per-step launches; 1: one
                              persistent cooperative launch with grid

@@ -493,12 +493,16 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   const bool tc = prec == 1 && !o.cuda_core_schur;
   const int sblock = prec == 0 ? 128
                      : (o.solve_block == 128 || o.solve_block == 512 ? o.solve_block : 256);
+  const int pwidth =
+      o.panel_width == 32 || o.panel_width == 64 || (o.panel_width == 128 && prec == 1)
+          ? o.panel_width
+          : (prec == 0 ? 32 : 64);
 
   // factorisation (reused when sigma, precision and Schur kernel are unchanged)
   Factor *F = ctx->factor;
   if (F && (F->prec != prec || F->sigma_re != sigma.real() || F->sigma_im != sigma.imag() ||
-            F->tensor_cores != tc || F->sw != sblock || !F->factored)) {
-    if (F->prec != prec || F->sw != sblock) {
+            F->tensor_cores != tc || F->sw != sblock || F->w != pwidth || !F->factored)) {
+    if (F->prec != prec || F->sw != sblock || F->w != pwidth) {
       free_factor(ctx);
       F = nullptr;
     } else {
@@ -510,7 +514,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   if (!F) {
     F = new Factor();
     ctx->factor = F;
-    int rc = F->setup(ctx, prec, 48, sblock);
+    int rc = F->setup(ctx, prec, 48, sblock, pwidth);
     if (rc) {
       free_factor(ctx);
       return rc;

@@ -31,9 +31,6 @@ namespace {
 
 constexpr int kTile = 64;
 
-// widest panel per precision (FP64 fronts use w = 32, FP32 fronts w = 64)
-template <class C> struct MaxW { static constexpr int v = 64; };
-template <> struct MaxW<double2> { static constexpr int v = 32; };
 
 // ------------------------------------------------------------ factorization
 
@@ -1034,9 +1031,13 @@ cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block
 
 // ------------------------------------------------------------------- host
 
-int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block) {
+int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int panel_width) {
   prec = precision;
-  w = precision == 0 ? 32 : 64;
+  // complex128 panels stop at 64 columns: the TRSM tiles (w x w + w x 33
+  // values) must fit in shared memory
+  w = panel_width == 32 || panel_width == 64 || (panel_width == 128 && precision == 1)
+          ? panel_width
+          : (precision == 0 ? 32 : 64);
   sw = precision == 0 ? 128 : (solve_block == 128 || solve_block == 512 ? solve_block : 256);
   int rc;
   if (ctx->shared_sym) {

@@ -76,7 +76,7 @@ struct Factor {
   bool factored = false;
   double sigma_re = 0.0, sigma_im = 0.0;
 
-  int setup(tlr_ctx *ctx, int precision, int leaf, int solve_block = 0);
+  int setup(tlr_ctx *ctx, int precision, int leaf, int solve_block = 0, int panel_width = 0);
   void release();
   int factor(tlr_ctx *ctx, double sr, double si, double tiny);
   // In-place x <- K^-1 x on a device vector in the factor's precision.
