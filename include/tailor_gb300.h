@@ -204,6 +204,11 @@ typedef struct {
                              application here, and 9% slower)               */
   int panel_width;        /* panel columns of the factorisation: 32, 64 or
                              128 (0: 32 for complex128, 64 for complex64)    */
+  int cluster_panel;      /* 1: pivoting panel over an 8-CTA thread-block
+                             cluster per front (candidates exchanged through
+                             distributed shared memory) instead of one CTA;
+                             same pivots and factors; slower here (47 vs 41
+                             ms at 100 x 50, 266 vs 270 ms at 200 x 128)    */
   int persistent_solve;   /* 0 (default): each triangular solve replays a
                              CUDA graph of per-step launches; 1: one
                              persistent cooperative launch with grid

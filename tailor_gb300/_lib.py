@@ -76,7 +76,8 @@ class SolveOpts(ctypes.Structure):
                 ("sigma_im", ctypes.c_double), ("use_sigma", ctypes.c_int),
                 ("start", ctypes.c_void_p), ("cuda_core_schur", ctypes.c_int),
                 ("solve_block", ctypes.c_int), ("refinement", ctypes.c_int),
-                ("panel_width", ctypes.c_int), ("persistent_solve", ctypes.c_int)]
+                ("panel_width", ctypes.c_int), ("cluster_panel", ctypes.c_int),
+                ("persistent_solve", ctypes.c_int)]
 
 
 class EigDiag(ctypes.Structure):

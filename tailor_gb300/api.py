@@ -220,7 +220,7 @@ class EigenSolver:
               start: np.ndarray | None = None, modes: bool = False,
               cuda_core_schur: bool = False, persistent_solve: bool = False,
               solve_block: int = 0, refinement: str = "ir",
-              panel_width: int = 0) -> EigenSolution:
+              panel_width: int = 0, cluster_panel: bool = False) -> EigenSolution:
         ph = self.p.case.physics
         k = nev or ph.nev
         opts = L.SolveOpts(nev, ncv, tol, max_it, precision,
@@ -228,7 +228,8 @@ class EigenSolver:
                            0.0 if sigma is None else complex(sigma).imag,
                            0 if sigma is None else 1, None, int(bool(cuda_core_schur)),
                            int(solve_block), 1 if refinement == "gmres" else 0,
-                           int(panel_width), int(bool(persistent_solve)))
+                           int(panel_width), int(bool(cluster_panel)),
+                           int(bool(persistent_solve)))
         if start is not None:
             s = np.ascontiguousarray(np.stack([start.real, start.imag], -1),
                                      dtype=np.float64)
@@ -289,7 +290,8 @@ def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
             s = v.ctypes.data
         pts[i] = L.SweepPoint(int(c), complex(a).real, complex(a).imag, s, re_ov)
     k = nev or cases[0].physics.nev
-    opts = L.SweepOpts(L.SolveOpts(k, ncv, tol, max_it, precision, 0.0, 0.0, 0, None, 0, 0, 0, 0, 0),
+    opts = L.SweepOpts(L.SolveOpts(k, ncv, tol, max_it, precision, 0.0, 0.0, 0, None, 0, 0, 0, 0,
+                                   0, 0),
                        workers, int(bool(autotune)), device)
     lam = np.zeros((max(npts, 1), k, 2))
     res = np.zeros((max(npts, 1), k))

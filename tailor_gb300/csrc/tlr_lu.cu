@@ -18,6 +18,8 @@
 // blocks are inverted explicitly (k_tri_inv), so each solve step is a
 // parallel GEMV plus one small dense product instead of a serial
 // substitution; the solves walk the same levels.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cstdio>
 #include <vector>
@@ -183,6 +185,153 @@ __global__ void __launch_bounds__(512)
     }
     __syncthreads();
   }
+}
+
+// The same panel factorisation spread over a thread-block cluster of
+// kPanelCluster CTAs (one cluster per front): CTA 0 owns the panel's top ww
+// rows (where pivots land, and the U rows of every sub-panel), CTAs 1..7
+// split the remaining fully summed rows.  Per column each CTA finds its
+// local pivot candidate, the candidates are exchanged through distributed
+// shared memory after a cluster barrier (every CTA picks the same winner:
+// largest |a|, then the smallest row), CTA 0 swaps the rows, and after a
+// second barrier every CTA scales and updates its own rows.  Pivots and
+// arithmetic are those of k_panel, so the factors are identical.  Panel
+// data written by other CTAs is read past L1.
+constexpr int kPanelCluster = 8;
+
+template <class C>
+__global__ void __cluster_dims__(kPanelCluster, 1, 1) __launch_bounds__(256)
+    k_panel_cluster(const int *__restrict__ fl, int s, int w, C *__restrict__ pool,
+                    const DevFront *__restrict__ fr, int *__restrict__ ipiv,
+                    int *__restrict__ pert, double tiny) {
+  namespace cg = cooperative_groups;
+  using T = typename Real<C>::T;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int q = (int)cluster.block_rank();
+  __shared__ T sval[256];
+  __shared__ int sidx[256];
+  __shared__ T cval;
+  __shared__ int cidx;
+  __shared__ C lsub[kSB][kSB];
+  const DevFront f = fr[fl[blockIdx.x / kPanelCluster]];
+  C *F = pool + f.off;
+  const int m = f.m, p = f.p;
+  const int k0 = s * w, ww = min(w, p - k0);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // rows of this CTA: CTA 0 the top rows, CTAs 1.. contiguous chunks of the rest
+  const int top_end = k0 + ww;
+  const int rest = p - top_end;
+  const int chunk = (rest + kPanelCluster - 2) / (kPanelCluster - 1);
+  const int ra = q == 0 ? k0 : min(p, top_end + (q - 1) * chunk);
+  const int rb = q == 0 ? top_end : min(p, ra + chunk);
+  for (int jb = 0; jb < ww; jb += kSB) {
+    const int nb = min(kSB, ww - jb);
+    const int c0 = k0 + jb, c1 = c0 + nb;
+    for (int col = c0; col < c1; ++col) {
+      // local candidate over owned rows >= col
+      T best = -1;
+      int bi = p;
+      for (int r = max(ra, col) + tid; r < rb; r += nt) {
+        const T a = cabs1(__ldcg(F + (long long)col * m + r));
+        if (a > best) { best = a; bi = r; }
+      }
+      sval[tid] = best;
+      sidx[tid] = bi;
+      __syncthreads();
+      for (int o = nt / 2; o > 0; o >>= 1) {
+        if (tid < o) {
+          const T a = sval[tid + o];
+          const int ia = sidx[tid + o];
+          if (a > sval[tid] || (a == sval[tid] && ia < sidx[tid])) {
+            sval[tid] = a;
+            sidx[tid] = ia;
+          }
+        }
+        __syncthreads();
+      }
+      if (tid == 0) {
+        cval = sval[0];
+        cidx = sidx[0];
+      }
+      cluster.sync();
+      // every CTA reads the kPanelCluster candidates and picks the same pivot
+      T gb = -1;
+      int gi = p;
+      for (int k = 0; k < kPanelCluster; ++k) {
+        const T a = *cluster.map_shared_rank(&cval, k);
+        const int ia = *cluster.map_shared_rank(&cidx, k);
+        if (a > gb || (a == gb && ia < gi)) {
+          gb = a;
+          gi = ia;
+        }
+      }
+      const int pr = gi < p ? gi : col;
+      if (q == 0) {
+        if (tid == 0) ipiv[f.toff + col] = pr;
+        if (pr != col)
+          for (int c = k0 + tid; c < k0 + ww; c += nt) {
+            const C t = __ldcg(F + (long long)c * m + col);
+            F[(long long)c * m + col] = __ldcg(F + (long long)c * m + pr);
+            F[(long long)c * m + pr] = t;
+          }
+        __syncthreads();  // the pivot's own column may have been swapped by another thread
+        if (tid == 0 && cabs1(__ldcg(F + (long long)col * m + col)) == T(0)) {
+          F[(long long)col * m + col] = cmake<C>((T)tiny, 0);
+          atomicAdd(pert, 1);
+        }
+      }
+      __threadfence();
+      cluster.sync();
+      const C inv = cinv(__ldcg(F + (long long)col * m + col));
+      const int r0 = max(ra, col + 1);
+      for (int r = r0 + tid; r < rb; r += nt)
+        F[(long long)col * m + r] = cmul(__ldcg(F + (long long)col * m + r), inv);
+      __syncthreads();
+      const int nr = rb - r0, nc = c1 - col - 1;
+      for (int x = tid; x < nr * nc; x += nt) {
+        const int r = r0 + x % nr, c = col + 1 + x / nr;
+        F[(long long)c * m + r] = cfms(__ldcg(F + (long long)c * m + r),
+                                       __ldcg(F + (long long)col * m + r),
+                                       __ldcg(F + (long long)c * m + col));
+      }
+      __syncthreads();
+    }
+    if (c1 >= k0 + ww) break;
+    // CTA 0: U rows of the sub-panel for the remaining panel columns
+    if (q == 0) {
+      for (int x = tid; x < nb * nb; x += nt)
+        lsub[x / nb][x % nb] = __ldcg(F + (long long)(c0 + x % nb) * m + c0 + x / nb);
+      __syncthreads();
+      for (int c = c1 + tid; c < k0 + ww; c += nt) {
+        C xr[kSB];
+#pragma unroll
+        for (int r = 0; r < kSB; ++r) {
+          if (r >= nb) break;
+          C v = __ldcg(F + (long long)c * m + c0 + r);
+          for (int rp = 0; rp < r; ++rp) v = cfms(v, lsub[r][rp], xr[rp]);
+          xr[r] = v;
+          F[(long long)c * m + c0 + r] = v;
+        }
+      }
+    }
+    __threadfence();
+    cluster.sync();
+    // rank-nb update of the owned rows below the sub-panel
+    const int r0 = max(ra, c1);
+    const int nr = rb - r0, nc = k0 + ww - c1;
+    for (int x = tid; x < nr * nc; x += nt) {
+      const int r = r0 + x % nr, c = c1 + x / nr;
+      C v = __ldcg(F + (long long)c * m + r);
+#pragma unroll
+      for (int t = 0; t < kSB; ++t)
+        if (t < nb)
+          v = cfms(v, __ldcg(F + (long long)(c0 + t) * m + r),
+                   __ldcg(F + (long long)c * m + c0 + t));
+      F[(long long)c * m + r] = v;
+    }
+    __syncthreads();
+  }
+  cluster.sync();  // no CTA leaves while others may still read its candidates
 }
 
 template <class C>
@@ -1396,7 +1545,10 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
     const int *fl = d_sched + L.fronts_off;
     for (int s = 0; s < (int)L.steps.size(); ++s) {
       const Step &S = L.steps[s];
-      { k_panel<C><<<S.nf, 512, 0, st>>>(fl, s, w, P, d_fronts, d_ipiv, d_pert, tiny); count_launches(); }
+      if (cluster_panel)
+        { k_panel_cluster<C><<<S.nf * kPanelCluster, 256, 0, st>>>(fl, s, w, P, d_fronts, d_ipiv, d_pert, tiny); count_launches(); }
+      else
+        { k_panel<C><<<S.nf, 512, 0, st>>>(fl, s, w, P, d_fronts, d_ipiv, d_pert, tiny); count_launches(); }
       { k_swap<C><<<dim3(blocks_for(S.max_m, 128), S.nf), 128, 0, st>>>(fl, s, w, P, d_fronts,
                                                                        d_ipiv); count_launches(); }
       if (S.max_b > 0)

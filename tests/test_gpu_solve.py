@@ -62,3 +62,15 @@ def test_solver_variants_agree(gpu_lib, kw):
     assert np.all(alt.residual <= 1e-10)
     for lam in alt.lam:
         assert np.min(np.abs(ref.lam - lam)) <= 1e-8 * abs(lam)
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_cluster_panel_is_bitwise_the_single_cta_panel(gpu_lib, precision):
+    """The 8-CTA cluster panel picks the same pivots and does the same
+    arithmetic as the one-CTA panel: identical eigenvalues to the bit."""
+    case = make_case(60, 32, physics=Physics(alpha=1.2, omega=complex(0.3, 0.01), nev=6))
+    with api.Problem(case) as prob:
+        api.run_pipeline(prob)
+        a = api.EigenSolver(prob).solve(precision=precision)
+        b = api.EigenSolver(prob).solve(precision=precision, cluster_panel=True)
+    assert np.array_equal(a.lam, b.lam)
