@@ -76,6 +76,49 @@ __global__ void k_extend(const int *__restrict__ kids, const DevFront *__restric
   }
 }
 
+// Block-wide argmax of (value, row) pairs: largest value, ties to the
+// smaller row; warp shuffles, then one warp over the warp winners.  The
+// result is returned to every thread.
+template <class T>
+__device__ __forceinline__ void block_argmax(T &best, int &bi, T *wval, int *widx) {
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const T a = __shfl_down_sync(0xffffffffu, best, o);
+    const int ia = __shfl_down_sync(0xffffffffu, bi, o);
+    if (a > best || (a == best && ia < bi)) {
+      best = a;
+      bi = ia;
+    }
+  }
+  if (lane == 0) {
+    wval[wp] = best;
+    widx[wp] = bi;
+  }
+  __syncthreads();
+  if (wp == 0) {
+    best = lane < nw ? wval[lane] : T(-2);
+    bi = lane < nw ? widx[lane] : 0x7fffffff;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const T a = __shfl_down_sync(0xffffffffu, best, o);
+      const int ia = __shfl_down_sync(0xffffffffu, bi, o);
+      if (a > best || (a == best && ia < bi)) {
+        best = a;
+        bi = ia;
+      }
+    }
+    if (lane == 0) {
+      wval[0] = best;
+      widx[0] = bi;
+    }
+  }
+  __syncthreads();
+  best = wval[0];
+  bi = widx[0];
+  __syncthreads();  // wval/widx are reused by the next call
+}
+
 // Panel factorisation of step s for one front per CTA: columns k0..k0+ww,
 // partial pivoting over the fully summed rows k0..p-1.  The panel is
 // processed in sub-panels of kSB columns: pivoting, scaling and rank-1
@@ -91,9 +134,8 @@ __global__ void __launch_bounds__(512)
             const DevFront *__restrict__ fr, int *__restrict__ ipiv,
             int *__restrict__ pert, double tiny) {
   using T = typename Real<C>::T;
-  __shared__ T sval[512];
-  __shared__ int sidx[512];
-  __shared__ int piv_sh;
+  __shared__ T sval[32];
+  __shared__ int sidx[32];
   __shared__ C lsub[kSB][kSB];
   const DevFront f = fr[fl[blockIdx.x]];
   C *F = pool + f.off;
@@ -110,26 +152,9 @@ __global__ void __launch_bounds__(512)
         const T a = cabs1(F[(long long)col * m + r]);
         if (a > best) { best = a; bi = r; }
       }
-      sval[tid] = best;
-      sidx[tid] = bi;
-      __syncthreads();
-      for (int o = nt / 2; o > 0; o >>= 1) {
-        if (tid < o) {
-          const T a = sval[tid + o];
-          const int ia = sidx[tid + o];
-          if (a > sval[tid] || (a == sval[tid] && ia < sidx[tid])) {
-            sval[tid] = a;
-            sidx[tid] = ia;
-          }
-        }
-        __syncthreads();
-      }
-      if (tid == 0) {
-        piv_sh = sidx[0];
-        ipiv[f.toff + col] = sidx[0];
-      }
-      __syncthreads();
-      const int pr = piv_sh;
+      block_argmax(best, bi, sval, sidx);
+      if (tid == 0) ipiv[f.toff + col] = bi;
+      const int pr = bi;
       if (pr != col)
         for (int c = k0 + tid; c < k0 + ww; c += nt) {
           const C t = F[(long long)c * m + col];
@@ -208,8 +233,8 @@ __global__ void __cluster_dims__(kPanelCluster, 1, 1) __launch_bounds__(256)
   using T = typename Real<C>::T;
   cg::cluster_group cluster = cg::this_cluster();
   const int q = (int)cluster.block_rank();
-  __shared__ T sval[256];
-  __shared__ int sidx[256];
+  __shared__ T sval[32];
+  __shared__ int sidx[32];
   __shared__ T cval;
   __shared__ int cidx;
   __shared__ C lsub[kSB][kSB];
@@ -235,23 +260,10 @@ __global__ void __cluster_dims__(kPanelCluster, 1, 1) __launch_bounds__(256)
         const T a = cabs1(__ldcg(F + (long long)col * m + r));
         if (a > best) { best = a; bi = r; }
       }
-      sval[tid] = best;
-      sidx[tid] = bi;
-      __syncthreads();
-      for (int o = nt / 2; o > 0; o >>= 1) {
-        if (tid < o) {
-          const T a = sval[tid + o];
-          const int ia = sidx[tid + o];
-          if (a > sval[tid] || (a == sval[tid] && ia < sidx[tid])) {
-            sval[tid] = a;
-            sidx[tid] = ia;
-          }
-        }
-        __syncthreads();
-      }
+      block_argmax(best, bi, sval, sidx);
       if (tid == 0) {
-        cval = sval[0];
-        cidx = sidx[0];
+        cval = best;
+        cidx = bi;
       }
       cluster.sync();
       // every CTA reads the kPanelCluster candidates and picks the same pivot
