@@ -159,16 +159,18 @@ __global__ void __launch_bounds__(32 * kRowsPerCta)
   const bool active = lane < 25;
   float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
   const int k0 = row_ptr[row], k1 = row_ptr[row + 1];
-  for (int k = k0; k < k1; k += 4) {
-    float4 a[4], xv[4];
+  // eight blocks in flight per lane: the kernel is load-latency bound
+  constexpr int kU = 8;
+  for (int k = k0; k < k1; k += kU) {
+    float4 a[kU], xv[kU];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < kU; ++u) {
       const bool ok = active && k + u < k1;
       a[u] = ok ? __ldcs(aff + (size_t)(k + u) * 25 + lane) : make_float4(0.f, 0.f, 0.f, 0.f);
       xv[u] = ok ? wff[(size_t)col[k + u] * 5 + c] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < kU; ++u) {
       // (ar + i ai)(xr + i xi), every part a float-float pair
       ff_mac(rh, rl, a[u].x, a[u].y, xv[u].x, xv[u].y);
       ff_mac(rh, rl, -a[u].z, -a[u].w, xv[u].z, xv[u].w);
