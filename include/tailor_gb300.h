@@ -339,6 +339,14 @@ int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sweep_point *
 int tlr_schur_update_c64(const float *front, int m, int p, int k0, int w, unsigned lbo,
                          unsigned sbo, float *out);
 
+/* Test hook, no counterpart in the reference: failure detection without a
+ * GPU fault.  which = 0: the tensor-core kernel's bounded mbarrier wait on
+ * a barrier that nothing completes; which = 1: the persistent solve's
+ * bounded grid barrier waiting for a CTA that does not exist.  limit is the
+ * poll count; *timed_out = 1 when the wait gave up and reported it (the
+ * context stays usable). */
+int tlr_wait_selftest(int which, unsigned limit, int *timed_out);
+
 /* Kernels of this library launched by the process so far (every kernel
  * node of a replayed CUDA graph counts once per replay; cuBLAS kernels are
  * not counted).  No counterpart in the reference: it lets a caller check

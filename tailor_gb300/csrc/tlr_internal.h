@@ -145,6 +145,9 @@ int residual_ff(tlr_ctx *ctx, const double2 *y, const double2 *w, double sr, dou
 // stream-ordered, no host synchronisation (capturable).
 int vec_norm_async(tlr_ctx *ctx, const double2 *v, long long count, double *scratch,
                    double *out);
+// Launch the persistent solve's grid barrier on one CTA with a target it
+// cannot reach (bounded-wait self test).
+int grid_barrier_probe(unsigned *count, unsigned limit, int *err);
 // Allocate and fill ctx->aff / ctx->wff if needed (outside stream capture).
 int prepare_ff(tlr_ctx *ctx);
 int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,

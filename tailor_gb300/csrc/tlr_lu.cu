@@ -982,20 +982,26 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   return v;
 }
 
-__device__ __forceinline__ void grid_barrier(unsigned *count, unsigned target, int *err) {
+__device__ __forceinline__ void grid_barrier(unsigned *count, unsigned target, int *err,
+                                             unsigned limit = kBarrierLimit) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
     atomicAdd(count, 1u);
     unsigned it = 0;
     while (ld_acquire(count) < target)
-      if (++it > kBarrierLimit) {
+      if (++it > limit) {
         atomicExch(err, 1);
         break;
       }
     __threadfence();
   }
   __syncthreads();
+}
+
+// one CTA waits at a grid barrier for a second arrival that never comes
+__global__ void k_grid_barrier_probe(unsigned *count, unsigned limit, int *err) {
+  grid_barrier(count, 2u, err, limit);
 }
 
 template <class C>
@@ -1428,6 +1434,11 @@ int Factor::build_phases(tlr_ctx *ctx) {
   TLR_CUDA(ctx, cudaMemcpy(d_phases, ph.data(), ph.size() * sizeof(Phase), cudaMemcpyHostToDevice));
   TLR_CUDA(ctx, cudaMemset(d_solve_err, 0, sizeof(int)));
   return TLR_OK;
+}
+
+int grid_barrier_probe(unsigned *count, unsigned limit, int *err) {
+  { k_grid_barrier_probe<<<1, 32>>>(count, limit, err); count_launches(); }
+  return cudaGetLastError() == cudaSuccess ? TLR_OK : TLR_ERR_CUDA;
 }
 
 int Factor::take_solve_error(tlr_ctx *ctx) {

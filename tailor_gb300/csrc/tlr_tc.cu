@@ -88,10 +88,23 @@ __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
 }
 
 // bounded wait; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (unsigned it = 0; it < kWaitLimit; ++it)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          unsigned limit = kWaitLimit) {
+  for (unsigned it = 0; it < limit; ++it)
     if (mbar_test(bar, parity)) return true;
   return false;
+}
+
+// Bounded-wait check: one thread waits on an mbarrier that nothing will
+// complete, with a short poll limit, and reports the timeout.
+__global__ void k_mbar_timeout_probe(unsigned limit, int *err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && !mbar_wait(&bar, 0, limit)) atomicExch(err, 1);
 }
 
 #define TLR_TC_LD16(taddr, r)                                                                    \
@@ -299,6 +312,33 @@ int launch_gemm_tc(tlr_ctx *ctx, const int *fl, const int *prefix, int nf, int s
 }
 
 }  // namespace tlr
+
+// ---------------------------------------------------------------- test hooks
+// Failure detection without a fault: which = 0 runs the tensor-core
+// kernel's bounded mbarrier wait on a barrier nothing completes, which = 1
+// the persistent solve's bounded grid barrier waiting for a CTA that does
+// not exist; *timed_out = 1 when the wait gave up and reported it.
+extern "C" int tlr_wait_selftest(int which, unsigned limit, int *timed_out) {
+  using namespace tlr;
+  if (!timed_out || which < 0 || which > 1 || limit == 0) return TLR_ERR_ARG;
+  int *d = nullptr;  // err flag, then the barrier counter
+  if (cudaMalloc(&d, 2 * sizeof(int)) != cudaSuccess) return TLR_ERR_NOMEM;
+  int rc = TLR_OK;
+  if (cudaMemset(d, 0, 2 * sizeof(int)) != cudaSuccess) rc = TLR_ERR_CUDA;
+  if (!rc) {
+    if (which == 0)
+      { k_mbar_timeout_probe<<<1, 32>>>(limit, d); count_launches(); }
+    else
+      rc = grid_barrier_probe(reinterpret_cast<unsigned *>(d + 1), limit, d);
+  }
+  int h = 0;
+  if (!rc && (cudaDeviceSynchronize() != cudaSuccess ||
+              cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess))
+    rc = TLR_ERR_CUDA;
+  cudaFree(d);
+  *timed_out = h;
+  return rc;
+}
 
 // ---------------------------------------------------------------- test hook
 extern "C" int tlr_schur_update_c64(const float *front, int m, int p, int k0, int w,

@@ -73,3 +73,19 @@ def test_rule_validation(gpu_lib):
     with pytest.raises(api.TailorError) as e:
         api.Problem(case)
     assert e.value.status == 4
+
+
+@pytest.mark.parametrize("which", [0, 1], ids=["mbarrier", "grid-barrier"])
+def test_bounded_waits_report_timeouts(gpu_lib, which):
+    """The GPU's only waits (the tensor-core kernel's mbarrier wait, the
+    persistent solve's grid barrier) give up after their poll limit and set
+    an error flag the host reads; the context stays usable afterwards."""
+    import ctypes
+    t = ctypes.c_int(-1)
+    assert gpu_lib.tlr_wait_selftest(which, 200000, ctypes.byref(t)) == 0
+    assert t.value == 1
+    case = make_case(24, 16)
+    with api.Problem(case) as prob:
+        api.run_pipeline(prob)
+        sol = api.EigenSolver(prob).solve(nev=4, precision=1)
+    assert np.all(sol.residual <= 1e-10)
