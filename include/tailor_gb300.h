@@ -204,11 +204,12 @@ typedef struct {
                              application here, and 9% slower)               */
   int panel_width;        /* panel columns of the factorisation: 32, 64 or
                              128 (0: 32 for complex128, 64 for complex64)    */
-  int cluster_panel;      /* 1: pivoting panel over an 8-CTA thread-block
+  int cluster_panel;      /* pivoting panel over an 8-CTA thread-block
                              cluster per front (candidates exchanged through
-                             distributed shared memory) instead of one CTA;
-                             same pivots and factors; slower here (47 vs 41
-                             ms at 100 x 50, 266 vs 270 ms at 200 x 128)    */
+                             distributed shared memory) or one CTA; same
+                             pivots and factors.  0 (default): cluster for
+                             the steps with >= 4096 fully summed rows left;
+                             1: always; -1: never                           */
   int persistent_solve;   /* 0 (default): each triangular solve replays a
                              CUDA graph of per-step launches; 1: one
                              persistent cooperative launch with grid

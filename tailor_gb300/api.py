@@ -220,7 +220,7 @@ class EigenSolver:
               start: np.ndarray | None = None, modes: bool = False,
               cuda_core_schur: bool = False, persistent_solve: bool = False,
               solve_block: int = 0, refinement: str = "ir",
-              panel_width: int = 0, cluster_panel: bool = False) -> EigenSolution:
+              panel_width: int = 0, cluster_panel: int = 0) -> EigenSolution:
         ph = self.p.case.physics
         k = nev or ph.nev
         opts = L.SolveOpts(nev, ncv, tol, max_it, precision,
@@ -228,7 +228,7 @@ class EigenSolver:
                            0.0 if sigma is None else complex(sigma).imag,
                            0 if sigma is None else 1, None, int(bool(cuda_core_schur)),
                            int(solve_block), 1 if refinement == "gmres" else 0,
-                           int(panel_width), int(bool(cluster_panel)),
+                           int(panel_width), int(cluster_panel),
                            int(bool(persistent_solve)))
         if start is not None:
             s = np.ascontiguousarray(np.stack([start.real, start.imag], -1),

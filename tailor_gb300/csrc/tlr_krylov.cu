@@ -520,9 +520,10 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
       return rc;
     }
   }
-  if (F->cluster_panel != (o.cluster_panel != 0)) F->factored = false;
+  const int cpanel = o.cluster_panel > 0 ? 1 : (o.cluster_panel < 0 ? -1 : 0);
+  if (F->cluster_panel != cpanel) F->factored = false;
   F->tensor_cores = tc;
-  F->cluster_panel = o.cluster_panel != 0;
+  F->cluster_panel = cpanel;
   F->persistent = o.persistent_solve != 0;
   if (!F->factored) {
     double anorm = 0.0;

@@ -39,7 +39,7 @@ struct Factor {
   Symbolic sym;
   int prec = 0;  // 0: complex128 fronts, 1: complex64 fronts
   bool tensor_cores = true;  // complex64 Schur updates on tcgen05 (3xTF32)
-  bool cluster_panel = false; // panel factorisation over an 8-CTA cluster per front
+  int cluster_panel = 0;  // panel over an 8-CTA cluster: 1 always, -1 never, 0 for large fronts
   int *d_tc_err = nullptr;   // set by a tensor-core kernel whose wait timed out
   int w = 32;    // panel width
   int sw = 128;  // rows of a diagonal block of the solves (128 or 256)

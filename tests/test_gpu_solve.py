@@ -71,6 +71,6 @@ def test_cluster_panel_is_bitwise_the_single_cta_panel(gpu_lib, precision):
     case = make_case(60, 32, physics=Physics(alpha=1.2, omega=complex(0.3, 0.01), nev=6))
     with api.Problem(case) as prob:
         api.run_pipeline(prob)
-        a = api.EigenSolver(prob).solve(precision=precision)
-        b = api.EigenSolver(prob).solve(precision=precision, cluster_panel=True)
+        a = api.EigenSolver(prob).solve(precision=precision, cluster_panel=-1)
+        b = api.EigenSolver(prob).solve(precision=precision, cluster_panel=1)
     assert np.array_equal(a.lam, b.lam)
