@@ -54,7 +54,8 @@ typedef enum {
   TLR_ERR_NOMEM = 12,
   TLR_ERR_NOT_CONVERGED = 13,
   TLR_ERR_TIMEOUT = 14,     /* bounded device wait ran out                 */
-  TLR_ERR_SINGULAR = 15     /* zero pivot in the sparse factorisation      */
+  TLR_ERR_SINGULAR = 15,    /* zero pivot in the sparse factorisation      */
+  TLR_ERR_RULE = 16         /* FD-q rule generation or validation failed   */
 } tlr_status;
 
 /* Numerical part of the reference Recipe (Recipe.hpp:17-61). */
@@ -339,6 +340,22 @@ int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sweep_point *
  * Writes the updated front to out. */
 int tlr_schur_update_c64(const float *front, int m, int p, int k0, int w, unsigned lbo,
                          unsigned sbo, float *out);
+
+/* FD-q rule generation on the host (src/Python/fdq_nodes.py:280-353,
+ * calculate_fdq_rule and calculate_periodic_fdq_rule).  periodic = 0: the
+ * equal-error nodes on [-1, 1] with node_count - 1 intervals (period is
+ * ignored and taken as 2); periodic = 1: node_count uniform nodes on
+ * [-period/2, period/2) with centred stencils.  The caller provides
+ * nodes[node_count], stencil_indices and stencil_offsets
+ * [node_count][q+1] and weights [3][node_count][q+1] (d0, d1, d2), the
+ * layout of tlr_rule; log_error[node_count] (the equal-error amplitudes,
+ * zero for periodic rules) may be NULL.  Argument checks as the
+ * reference's (TLR_ERR_ARG); a node solve that does not converge or a
+ * rule that fails the reference's symmetry, equal-error or polynomial
+ * checks returns TLR_ERR_RULE. */
+int tlr_fdq_rule(int node_count, int q, int periodic, double period, double *nodes,
+                 int *stencil_indices, int *stencil_offsets, double *weights,
+                 double *log_error);
 
 /* Test hook, no counterpart in the reference: failure detection without a
  * GPU fault.  which = 0: the tensor-core kernel's bounded mbarrier wait on

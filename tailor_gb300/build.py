@@ -1,6 +1,7 @@
 """Build the CUDA library libtailor_gb300.so in-tree for sm_103a.
 
-Each translation unit is compiled in parallel with nvcc; the files that
+Each translation unit is compiled in parallel: CUDA sources with nvcc,
+host-only C++ sources (*.cpp) with the system compiler; the files that
 must reproduce the reference's arithmetic bit for bit are compiled with
 --fmad=false (no contraction of a*b+c into one fused operation).
 """
@@ -31,10 +32,18 @@ def nvcc() -> str:
 
 
 def sources() -> list[Path]:
-    return sorted(CSRC.glob("*.cu"))
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
 
 
 def _compile(src: Path, obj: Path, verbose: bool) -> str:
+    if src.suffix == ".cpp":  # host-only code: the system C++ compiler
+        cxx = shutil.which("g++") or "c++"
+        cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", str(src),
+               "-o", str(obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"{cxx} failed for {src.name}:\n{r.stderr}")
+        return r.stderr
     flags = list(COMMON)
     if src.name in EXACT:
         flags.append("--fmad=false")

@@ -150,6 +150,7 @@ const char *tlr_status_string(int status) {
     case TLR_ERR_NOT_CONVERGED: return "eigensolver did not converge";
     case TLR_ERR_TIMEOUT: return "device wait timed out";
     case TLR_ERR_SINGULAR: return "singular factorisation";
+    case TLR_ERR_RULE: return "FD-q rule generation failed";
   }
   return "unknown status";
 }

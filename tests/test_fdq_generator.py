@@ -1,0 +1,118 @@
+"""Host FD-q rule generator (tlr_fdq_rule) against the reference's rules.
+
+Golden data: the shipped tables and tests/golden/fdq_reference_rules.npz
+were produced by the reference's generator (fdq_nodes.py:280-353; the
+scripts are tailor_gb300/rules/make_rules.py and
+tests/golden/make_fdq_golden.py), and fdq_n100_q10_notebook.txt is the node
+vector the reference's own test pins (test_fdq_nodes.py:24-27, 70-76).
+The reference's node solve stops at a least-squares tolerance, so bounded
+nodes are compared to 1e-13 and weights relative to their row scale to
+1e-11; periodic rules have no solve and must match bit for bit.  No GPU.
+"""
+import re
+import time
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from tailor_gb300 import build as tb
+from tailor_gb300 import rules
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    tb.build()
+
+
+def _compare(g, nodes, idx, off, w, periodic):
+    assert np.array_equal(g.indices, idx) and np.array_equal(g.offsets, off)
+    if periodic:
+        assert np.array_equal(g.nodes, nodes) and np.array_equal(g.weights, w)
+        return
+    assert np.max(np.abs(g.nodes - nodes)) < 1e-13
+    for k in range(3):
+        scale = np.max(np.abs(w[k]), axis=1, keepdims=True)
+        assert np.max(np.abs(g.weights[k] - w[k]) / scale) < 1e-11, k
+
+
+@pytest.mark.parametrize("name", rules.available())
+def test_generated_matches_shipped_table(name):
+    m = re.match(r"N(\d+)_q(\d+)(p?)", name)
+    n, q, per = int(m.group(1)), int(m.group(2)), m.group(3) == "p"
+    nc = n if per else n + 1
+    r = rules.load_rule(nc, q, per)
+    g = rules.generate_rule(nc, q, per, r.period)
+    _compare(g, r.nodes, r.indices, r.offsets, r.weights, per)
+
+
+@pytest.mark.parametrize("name", ["N10_q4", "N8_q8", "N40_q6", "N10_q4p", "N24_q6p"])
+def test_generated_matches_reference_generator(name):
+    ref = np.load(GOLDEN / "fdq_reference_rules.npz")
+    m = re.match(r"N(\d+)_q(\d+)(p?)", name)
+    n, q, per = int(m.group(1)), int(m.group(2)), m.group(3) == "p"
+    g, le = rules.generate_rule(n if per else n + 1, q, per, with_log_error=True)
+    _compare(g, ref[f"{name}_nodes"], ref[f"{name}_stencil_indices"],
+             ref[f"{name}_stencil_offsets"], ref[f"{name}_weights"], per)
+    # equal-error amplitudes: flat, and at the reference's level
+    assert np.max(np.abs(np.diff(le))) < 1e-9
+    assert np.max(np.abs(le - ref[f"{name}_log_error"])) < 1e-9
+
+
+def test_notebook_nodes_n100_q10():
+    """The reference test's pinned N=100, q=10 nodes (atol 2e-9 there)."""
+    want = np.loadtxt(GOLDEN / "fdq_n100_q10_notebook.txt")
+    g = rules.generate_rule(101, 10, False)
+    assert np.max(np.abs(g.nodes - want)) < 2e-9
+
+
+def test_full_stencil_limit_is_cgl():
+    """q = N gives the Chebyshev-Gauss-Lobatto nodes (test_fdq_nodes.py:62-68)."""
+    for n in (4, 8, 12):
+        g = rules.generate_rule(n + 1, n, False)
+        cgl = -np.cos(np.arange(n + 1) * np.pi / n)
+        assert np.max(np.abs(g.nodes - cgl)) < 2e-11
+
+
+def test_bounded_shapes_and_invariants():
+    g, le = rules.generate_rule(11, 4, False, with_log_error=True)
+    assert g.nodes.shape == (11,) and g.indices.shape == (11, 5) and g.weights.shape == (3, 11, 5)
+    assert g.nodes[0] == -1.0 and g.nodes[-1] == 1.0 and np.all(np.diff(g.nodes) > 0)
+    assert np.max(np.abs(g.nodes + g.nodes[::-1])) < 5e-12
+    assert np.max(np.abs(np.diff(le))) < 1e-9
+
+
+def test_periodic_half_open_and_wraps():
+    g = rules.generate_rule(10, 4, True)
+    assert g.nodes[0] == -1.0 and g.nodes[-1] < 1.0
+    assert list(g.offsets[0]) == [-2, -1, 0, 1, 2]
+    assert list(g.indices[0]) == [8, 9, 0, 1, 2]
+
+
+def test_periodic_derivatives_converge():
+    errs = []
+    for nc in (24, 48):
+        g = rules.generate_rule(nc, 6, True)
+        v = np.sin(np.pi * g.nodes)
+        d = np.sum(g.weights[1] * v[g.indices], axis=1)
+        errs.append(np.max(np.abs(d - np.pi * np.cos(np.pi * g.nodes))))
+    assert errs[1] < errs[0] / 40.0
+
+
+@pytest.mark.parametrize("nc,q,per,period", [
+    (2, 2, False, 2.0), (5, 1, False, 2.0), (5, 5, False, 2.0),   # N < 2, q < 2, q > N
+    (2, 2, True, 2.0), (10, 3, True, 2.0), (10, 10, True, 2.0),   # n < 3, odd q, q >= n
+    (10, 4, True, 0.0), (10, 4, True, float("nan"))])
+def test_argument_checks(nc, q, per, period):
+    with pytest.raises(ValueError):
+        rules.generate_rule(nc, q, per, period)
+
+
+def test_unshipped_size_is_generated_on_demand():
+    assert "N40_q10" not in rules.available()
+    t = time.perf_counter()
+    r = rules.load_rule(41, 10, False)
+    assert time.perf_counter() - t < 5.0
+    assert r.n == 41 and r.nodes[0] == -1.0 and r.nodes[-1] == 1.0
