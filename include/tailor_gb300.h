@@ -208,9 +208,10 @@ typedef struct {
   int cluster_panel;      /* pivoting panel over an 8-CTA thread-block
                              cluster per front (candidates exchanged through
                              distributed shared memory) or one CTA; same
-                             pivots and factors.  0 (default): cluster for
-                             the steps with >= 4096 fully summed rows left;
-                             1: always; -1: never                           */
+                             pivots and factors.  A panel step uses the
+                             cluster when at least cluster_panel fully
+                             summed rows are left (1: always); 0 (default):
+                             4096; -1: never                                */
   int persistent_solve;   /* 0 (default): each triangular solve replays a
                              CUDA graph of per-step launches; 1: one
                              persistent cooperative launch with grid

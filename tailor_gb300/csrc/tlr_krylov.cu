@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -520,10 +521,11 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
       return rc;
     }
   }
-  const int cpanel = o.cluster_panel > 0 ? 1 : (o.cluster_panel < 0 ? -1 : 0);
-  if (F->cluster_panel != cpanel) F->factored = false;
+  const int crows = o.cluster_panel > 0 ? o.cluster_panel
+                    : (o.cluster_panel < 0 ? INT_MAX : kClusterPanelRows);
+  if (F->cluster_rows != crows) F->factored = false;
   F->tensor_cores = tc;
-  F->cluster_panel = cpanel;
+  F->cluster_rows = crows;
   F->persistent = o.persistent_solve != 0;
   if (!F->factored) {
     double anorm = 0.0;

@@ -223,7 +223,6 @@ __global__ void __launch_bounds__(512)
 // arithmetic are those of k_panel, so the factors are identical.  Panel
 // data written by other CTAs is read past L1.
 constexpr int kPanelCluster = 8;
-constexpr int kClusterPanelRows = 4096;  // automatic choice: rows still to pivot
 
 template <class C>
 __global__ void __cluster_dims__(kPanelCluster, 1, 1) __launch_bounds__(256)
@@ -1570,10 +1569,8 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
     for (int s = 0; s < (int)L.steps.size(); ++s) {
       const Step &S = L.steps[s];
       // the cluster panel pays off once the largest front still has many
-      // fully summed rows (measured: 678 vs 728 ms at 300 x 192, 44 vs 37
-      // ms at 100 x 50); both give the same pivots and factors
-      const bool cluster = cluster_panel > 0 ||
-                           (cluster_panel == 0 && L.pmax - s * w >= kClusterPanelRows);
+      // fully summed rows; both give the same pivots and factors
+      const bool cluster = L.pmax - s * w >= cluster_rows;
       if (cluster)
         { k_panel_cluster<C><<<S.nf * kPanelCluster, 256, 0, st>>>(fl, s, w, P, d_fronts, d_ipiv, d_pert, tiny); count_launches(); }
       else

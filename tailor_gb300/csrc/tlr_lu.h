@@ -14,6 +14,9 @@ struct DevFront {
 };
 
 
+// Default of Factor::cluster_rows (the automatic cluster-panel choice).
+constexpr int kClusterPanelRows = 4096;
+
 struct Step {  // one panel step of one level
   int nf, max_m, max_b, max_ext, prefix_off, tiles;
 };
@@ -39,7 +42,9 @@ struct Factor {
   Symbolic sym;
   int prec = 0;  // 0: complex128 fronts, 1: complex64 fronts
   bool tensor_cores = true;  // complex64 Schur updates on tcgen05 (3xTF32)
-  int cluster_panel = 0;  // panel over an 8-CTA cluster: 1 always, -1 never, 0 for large fronts
+  // panel steps with at least this many fully summed rows left run over an
+  // 8-CTA cluster (INT_MAX: never)
+  int cluster_rows = kClusterPanelRows;
   int *d_tc_err = nullptr;   // set by a tensor-core kernel whose wait timed out
   int w = 32;    // panel width
   int sw = 128;  // rows of a diagonal block of the solves (128 or 256)
