@@ -211,7 +211,7 @@ typedef struct {
                              pivots and factors.  A panel step uses the
                              cluster when at least cluster_panel fully
                              summed rows are left (1: always); 0 (default):
-                             4096; -1: never                                */
+                             1024; -1: never                                */
   int persistent_solve;   /* 0 (default): each triangular solve replays a
                              CUDA graph of per-step launches; 1: one
                              persistent cooperative launch with grid
