@@ -814,17 +814,44 @@ __global__ void __launch_bounds__(SW > 256 ? SW : 256)
   }
 }
 
+// sum over k < min(kQ, nv) of fv[k] v[k], in k order (v in shared memory,
+// 16-byte aligned; complex64 pairs are read 16 bytes at a time when all
+// kQ columns exist)
+template <class C, int kQ>
+__device__ __forceinline__ C dot_cols(const C (&fv)[kQ], const C *v, bool full, int nv) {
+  C acc = czero<C>();
+  if (full) {
+    if constexpr (sizeof(C) == sizeof(float2) && kQ % 2 == 0) {
+      const float4 *v4 = reinterpret_cast<const float4 *>(v);
+#pragma unroll
+      for (int k = 0; k < kQ; k += 2) {
+        const float4 pv = v4[k / 2];
+        acc = cfma(acc, fv[k], make_float2(pv.x, pv.y));
+        acc = cfma(acc, fv[k + 1], make_float2(pv.z, pv.w));
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < kQ; ++k) acc = cfma(acc, fv[k], v[k]);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kQ; ++k)
+      if (k < nv) acc = cfma(acc, fv[k], v[k]);
+  }
+  return acc;
+}
+
 // One solve step of every front of the level that owns block b: rows
 // [lo, hi) take t[r] -= F(r, b0:b1) t[b0:b1] (forward: lo = b1, hi = m;
 // backward: lo = 0, hi = b0).  CTA = 32 rows x 8 warps of SW/8 columns.
 // Backward steps run on the pivot-row vector of the backward pass; rows of
 // block b-1 are final after step b and are written to the solution x.
 template <class C, int SW>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, (SW <= 256 && sizeof(C) == 8) ? 3 : 1)
     k_blk_update(const int *__restrict__ fl, int b, int backward, const C *__restrict__ pool,
                  const DevFront *__restrict__ fr, C *__restrict__ work,
                  const int *__restrict__ nodes, C *__restrict__ x) {
-  __shared__ C vs[SW];
+  __shared__ __align__(16) C vs[SW];
   __shared__ C red[8][32];
   pdl_launch_dependents();
   const DevFront f = fr[fl[blockIdx.y]];
@@ -839,21 +866,31 @@ __global__ void __launch_bounds__(256)
   // the matrix loads go out before the vector is staged (independent)
   constexpr int kQ = SW / 8;
   const int q0 = wp * kQ;
+  const bool full = q0 + kQ <= nb;  // every column of this warp exists
   C fv[kQ];
+  if (full && r < hi) {  // unpredicated stream down the warp's columns
+    const C *Fp = F + (long long)q0 * f.m + r;
 #pragma unroll
-  for (int k = 0; k < kQ; ++k)
-    fv[k] = (r < hi && q0 + k < nb) ? F[(long long)(q0 + k) * f.m + r] : czero<C>();
+    for (int k = 0; k < kQ; ++k, Fp += f.m) fv[k] = *Fp;
+  } else {
+#pragma unroll
+    for (int k = 0; k < kQ; ++k)
+      fv[k] = (r < hi && q0 + k < nb) ? F[(long long)(q0 + k) * f.m + r] : czero<C>();
+  }
   pdl_wait();
+  // complex64: the row's own value goes out with the vector loads (only
+  // this CTA writes row r in this step, and no row of block b); the
+  // complex128 kernel keeps its registers for three CTAs per SM
+  C v = czero<C>();
+  if constexpr (sizeof(C) == sizeof(float2))
+    if (wp == 0 && r < hi) v = t[r];
   for (int q = threadIdx.x; q < nb; q += blockDim.x) vs[q] = t[b0 + q];
   __syncthreads();
-  C acc = czero<C>();
-#pragma unroll
-  for (int k = 0; k < kQ; ++k)
-    if (q0 + k < nb) acc = cfma(acc, fv[k], vs[q0 + k]);
+  const C acc = dot_cols<C, kQ>(fv, vs + q0, full, nb - q0);
   red[wp][lane] = acc;
   __syncthreads();
   if (wp == 0 && r < hi) {
-    C v = t[r];
+    if constexpr (sizeof(C) != sizeof(float2)) v = t[r];
 #pragma unroll
     for (int k = 0; k < 8; ++k) v = csub(v, red[k][lane]);
     t[r] = v;
@@ -917,7 +954,7 @@ __global__ void __launch_bounds__(256)
                 const C *__restrict__ work, C *__restrict__ work2,
                 const double2 *__restrict__ partial, int nck, int pmax,
                 const int *__restrict__ nodes, C *__restrict__ x) {
-  __shared__ C zs[SW];
+  __shared__ __align__(16) C zs[SW];
   __shared__ C red[8][32];
   pdl_launch_dependents();
   const int fq = blockIdx.y, fid = fl[fq];
@@ -931,32 +968,41 @@ __global__ void __launch_bounds__(256)
   const C *Dm = dmat + inv_off[fid] + (long long)blk * SW * SW;
   constexpr int kQ = SW / 8;
   const int q0 = wp * kQ;
+  const bool full = q0 + kQ <= nb;
   C dv[kQ];
+  if (full && rr < nb) {
+    const C *Dp = Dm + (long long)q0 * nb + rr;
 #pragma unroll
-  for (int k = 0; k < kQ; ++k)
-    dv[k] = (rr < nb && q0 + k < nb) ? Dm[(long long)(q0 + k) * nb + rr] : czero<C>();
+    for (int k = 0; k < kQ; ++k, Dp += nb) dv[k] = *Dp;
+  } else {
+#pragma unroll
+    for (int k = 0; k < kQ; ++k)
+      dv[k] = (rr < nb && q0 + k < nb) ? Dm[(long long)(q0 + k) * nb + rr] : czero<C>();
+  }
   pdl_wait();
+  // warp 0 sums its rows' border partials (in chunk order) while the other
+  // warps stage z
+  const int r = b0 + rr;
+  double2 s = make_double2(0, 0);
+  if (wp == 0 && rr < nb) {
+    const int nchf = f.m > f.p ? (f.m - f.p + kBC - 1) / kBC : 0;
+#pragma unroll 4
+    for (int k = 0; k < nchf; ++k) {
+      const double2 pv = partial[((long long)fq * nck + k) * pmax + r];
+      s.x += pv.x;
+      s.y += pv.y;
+    }
+  }
   const C *z = work + f.toff + b0;
   for (int q = threadIdx.x; q < nb; q += blockDim.x) zs[q] = z[q];
   __syncthreads();
-  C acc = czero<C>();
-#pragma unroll
-  for (int k = 0; k < kQ; ++k)
-    if (q0 + k < nb) acc = cfma(acc, dv[k], zs[q0 + k]);
+  const C acc = dot_cols<C, kQ>(dv, zs + q0, full, nb - q0);
   red[wp][lane] = acc;
   __syncthreads();
   if (wp == 0 && rr < nb) {
     C w = czero<C>();
 #pragma unroll
     for (int k = 0; k < 8; ++k) w = cadd(w, red[k][lane]);
-    const int r = b0 + rr;
-    const int nchf = f.m > f.p ? (f.m - f.p + kBC - 1) / kBC : 0;
-    double2 s = make_double2(0, 0);
-    for (int k = 0; k < nchf; ++k) {
-      const double2 pv = partial[((long long)fq * nck + k) * pmax + r];
-      s.x += pv.x;
-      s.y += pv.y;
-    }
     w = csub(w, from64<C>(s));
     work2[f.toff + r] = w;
     if (b0 + SW >= f.p) x[(long long)nodes[f.node_off + r / 5] * 5 + r % 5] = w;
