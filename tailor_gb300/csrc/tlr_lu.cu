@@ -943,6 +943,58 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The same border product for complex64 factors, with the warp's kBC/8
+// columns loaded before the programmatic-launch wait (the factor does not
+// depend on earlier kernels of the solve) and summed in the same order.
+__global__ void __launch_bounds__(256, 3)
+    k_border_gemv_pf(const int *__restrict__ fl, const float2 *__restrict__ pool,
+                     const DevFront *__restrict__ fr, const int *__restrict__ nodes,
+                     const float2 *__restrict__ x, double2 *__restrict__ partial, int nck,
+                     int pmax) {
+  using C = float2;
+  __shared__ __align__(16) C xs[kBC];
+  __shared__ C red[8][32];
+  pdl_launch_dependents();
+  const int fq = blockIdx.z;
+  const DevFront f = fr[fl[fq]];
+  const int r0 = blockIdx.x * 32;
+  const int c0 = f.p + blockIdx.y * kBC;
+  if (r0 >= f.p || c0 >= f.m) return;
+  const int nc = min(kBC, f.m - c0);
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int r = r0 + lane;
+  constexpr int kQ = kBC / 8;
+  const int ka = wp * kQ;
+  const bool full = ka + kQ <= nc;
+  const C *F = pool + f.off + (long long)c0 * f.m + r;
+  C fv[kQ];
+  if (full && r < f.p) {
+    const C *Fp = F + (long long)ka * f.m;
+#pragma unroll
+    for (int k = 0; k < kQ; ++k, Fp += f.m) fv[k] = *Fp;
+  } else {
+#pragma unroll
+    for (int k = 0; k < kQ; ++k)
+      fv[k] = (r < f.p && ka + k < nc) ? F[(long long)(ka + k) * f.m] : czero<C>();
+  }
+  pdl_wait();
+  for (int k = threadIdx.x; k < nc; k += blockDim.x) {
+    const int c = c0 + k;
+    xs[k] = x[(long long)nodes[f.node_off + c / 5] * 5 + c % 5];
+  }
+  __syncthreads();
+  C acc = czero<C>();
+  if (r < f.p) acc = dot_cols<C, kQ>(fv, xs + ka, full, nc - ka);
+  red[wp][lane] = acc;
+  __syncthreads();
+  if (wp == 0 && r < f.p) {
+    C v = czero<C>();
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v = cadd(v, red[k][lane]);
+    partial[((long long)fq * nck + blockIdx.y) * pmax + r] = to64(v);
+  }
+}
+
 // Start of a front's backward pass: rows of block b = blockIdx.x / 4
 // (32 per CTA) take w = D_b z_b minus the border chunks of pass 1 (summed
 // in chunk order), written to the backward vector (z stays in work for the
@@ -1752,9 +1804,15 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
     const Level &L = levels[h];
     const int *fl = d_sched + L.fronts_off;
     if (L.bmax > 0) {
-      TLR_CUDA(ctx, launch_pdl(pdl, k_border_gemv<C>, dim3(blocks_for(L.pmax, 32), L.nck_b, L.nfronts),
-                               dim3(256), st, fl, P, (const DevFront *)d_fronts,
-                               (const int *)d_nodes, (const C *)x, d_partial, L.nck_b, L.pmax));
+      const dim3 g(blocks_for(L.pmax, 32), L.nck_b, L.nfronts);
+      if constexpr (sizeof(C) == sizeof(float2))
+        TLR_CUDA(ctx, launch_pdl(pdl, k_border_gemv_pf, g, dim3(256), st, fl, P,
+                                 (const DevFront *)d_fronts, (const int *)d_nodes, (const C *)x,
+                                 d_partial, L.nck_b, L.pmax));
+      else
+        TLR_CUDA(ctx, launch_pdl(pdl, k_border_gemv<C>, g, dim3(256), st, fl, P,
+                                 (const DevFront *)d_fronts, (const int *)d_nodes, (const C *)x,
+                                 d_partial, L.nck_b, L.pmax));
       count_launches();
     }
     TLR_CUDA(ctx, launch_pdl(pdl, k_bwd_start<C, SW>,
