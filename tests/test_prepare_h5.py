@@ -1,0 +1,238 @@
+"""Case preparation, configuration and HDF5 I/O (no GPU).
+
+* the HDF5 reader/writer round trip, and the reader on the reference's own
+  files (FD-q rule caches, the structured sample, the prepared case) when a
+  reference checkout is present;
+* sample -> FD-q interpolation against the reference's prepared file
+  (interpolate.py:501-585), to 1e-13 relative per component;
+* config.yaml parsing and the checks of Parser.cpp:37-148;
+* prepared-case (Prepare.cpp:443-687) and result-file (EigenOutput.cpp)
+  writers read back by the reader, and the deterministic mode phase.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from tailor_gb300 import config, h5, output, prepare, rules
+from tailor_gb300.case import Physics, make_case
+
+REF = Path("/root/reference")
+GOLDEN = Path(__file__).resolve().parent / "golden"
+needs_ref = pytest.mark.skipif(not (REF / "case" / "config.yaml").is_file(),
+                               reason="reference checkout not present")
+
+
+def test_writer_reader_round_trip(tmp_path):
+    w = h5.Writer()
+    w.attrs.update({"i": 7, "f": 2.5, "s": "k_j_dof", "u8": np.uint8(1), "neg": -3})
+    a = np.arange(60.0).reshape(5, 6, 2)
+    w.dataset("grid", a, {"complex": np.uint8(1)})
+    w.dataset("ints", np.arange(12, dtype=np.int64).reshape(3, 4))
+    for i in range(19):  # three symbol table nodes in one group
+        w.dataset(f"modes/mode_{i:03d}", np.full((2, 5, 2), float(i)))
+    w.group("empty")
+    w.group("deep/er").dataset("x", np.array([1.0, -2.0]))
+    p = tmp_path / "t.h5"
+    w.write(p)
+    with h5.File(p) as f:
+        assert f.attrs["i"] == 7 and f.attrs["f"] == 2.5 and f.attrs["s"] == "k_j_dof"
+        assert f.attrs["u8"] == 1 and f.attrs["neg"] == -3
+        assert sorted(f) == ["deep", "empty", "grid", "ints", "modes"]
+        assert np.array_equal(f["grid"][...], a) and f["grid"].attrs["complex"] == 1
+        assert np.array_equal(f["ints"][...], np.arange(12).reshape(3, 4))
+        assert list(f["modes"]) == [f"mode_{i:03d}" for i in range(19)]
+        assert np.all(f["modes/mode_017"][...] == 17.0)
+        assert list(f["empty"]) == []
+        assert np.array_equal(f["deep/er/x"][...], [1.0, -2.0])
+        with pytest.raises(KeyError):
+            f["nope"]
+
+
+def test_reader_rejects_non_hdf5(tmp_path):
+    p = tmp_path / "x.h5"
+    p.write_bytes(b"not an hdf5 file at all")
+    with pytest.raises(h5.H5Error):
+        h5.File(p)
+
+
+@needs_ref
+def test_reader_on_reference_rule_caches():
+    """The reference's cached rules (fdqNodes/*.h5) read here equal the
+    host generator's rules (nodes 1e-14, weights 1e-12 relative)."""
+    for name, nc, q, per in (("N100_q10", 101, 10, False), ("N200_q10", 201, 10, False),
+                             ("N50_q6p", 50, 6, True)):
+        with h5.File(REF / "fdqNodes" / f"{name}.h5") as f:
+            # N100_q10.h5 is the older schema 1 (no topology attribute)
+            assert f.attrs.get("topology", "bounded") == ("periodic" if per else "bounded")
+            assert int(f.attrs["node_count"]) == nc and int(f.attrs["q"]) == q
+            g = rules.generate_rule(nc, q, per)
+            assert np.max(np.abs(f["nodes"][...] - g.nodes)) < 1e-14
+            assert np.array_equal(f["stencil_indices"][...], g.indices)
+            for k in range(3):
+                w = f[f"weights/d{k}"][...]
+                assert np.max(np.abs(w - g.weights[k])) <= 1e-12 * np.max(np.abs(w))
+
+
+@needs_ref
+def test_interpolation_matches_reference_prepared_file():
+    cfg = config.load_config(REF / "case" / "config.yaml")
+    ours = prepare.prepare_sample(cfg.source_file, cfg.q_y, cfg.q_z, cfg.physics)
+    ref = prepare.load_prepared(cfg.input_file, cfg.q_y, cfg.q_z, cfg.physics)
+    assert (ours.ny, ours.nz, ours.spanwise_period) == (ref.ny, ref.nz, ref.spanwise_period)
+    for a, b in ((ours.grid, ref.grid), (ours.baseflow, ref.baseflow)):
+        scale = np.maximum(np.max(np.abs(b), axis=0), 1e-300)
+        assert np.max(np.abs(a - b) / scale) < 1e-13
+    assert np.array_equal(ours.eta.weights, ref.eta.weights)
+    assert np.max(np.abs(ours.xi.nodes - ref.xi.nodes)) < 1e-14
+
+
+@needs_ref
+def test_sample_fixture_is_the_reference_prepared_case():
+    cfg = config.load_config(REF / "case" / "config.yaml")
+    ref = prepare.load_prepared(cfg.input_file, cfg.q_y, cfg.q_z)
+    fx = np.load(GOLDEN / "sample_201x50_fields.npz")
+    assert np.array_equal(fx["grid"], ref.grid[..., 0])
+    assert np.array_equal(fx["baseflow"], ref.baseflow[..., 0])
+    assert float(fx["spanwise_period"]) == ref.spanwise_period
+
+
+CONFIG = """CaseTitle: Sample   # comment
+Folder: data
+File: "sample.h5"
+Q-Value:
+    y: 10
+    z: 6
+
+Stability:
+    Alpha:
+        Real: 2.43
+        Imag: 0.0
+EigenSolver:
+    SearchCenterOmega:
+        Real: 0.3
+        Imag: 0.01
+    NumberOfEigenvalues: 8
+    Tolerance: 1.0e-10
+    MaximumIterations: 1000
+Output:
+    File: data/results/out.h5
+Physics:
+    Targets:
+        ReynoldsNumber: 32500
+        MachNumber: 6.0
+    Gas:
+        PrandtlNumber: 0.72
+        GasConstant: 287.05
+        RatioOfSpecificHeats: 1.4
+    Transport:
+        ReferenceMu: 1.716E-5       # Pa s
+        ReferenceTemperature: 63.3340
+        SutherlandConstant: 110.4
+"""
+
+
+def test_config_parse_and_paths(tmp_path):
+    p = tmp_path / "config.yaml"
+    p.write_text(CONFIG)
+    c = config.load_config(p)
+    assert c.case_title == "Sample" and (c.q_y, c.q_z) == (10, 6)
+    assert c.source_file == tmp_path / "data" / "sample.h5"
+    assert c.input_file == tmp_path / "data" / "FD-q" / "fdq_sample_qy10_qz6.h5"
+    assert c.output_file == tmp_path / "data" / "results" / "out.h5"
+    ph = c.physics
+    assert (ph.reynolds, ph.mach, ph.prandtl, ph.gas_constant, ph.gamma) == \
+        (32500.0, 6.0, 0.72, 287.05, 1.4)
+    assert (ph.reference_viscosity, ph.reference_temperature, ph.sutherland_constant) == \
+        (1.716e-5, 63.334, 110.4)
+    assert ph.alpha == 2.43 and ph.omega == complex(0.3, 0.01)
+    assert (ph.nev, ph.tol, ph.max_it) == (8, 1e-10, 1000)
+    with pytest.raises(config.ConfigError, match="FD-q input file does not exist"):
+        config.load_config(p, require_input=True)
+
+
+@pytest.mark.parametrize("edit,message", [
+    (("    y: 10\n", ""), "Missing YAML key: y"),
+    (("        MachNumber: 6.0\n", "        MachNumber: -6.0\n"), "outside their valid ranges"),
+    (("    NumberOfEigenvalues: 8\n", "    NumberOfEigenvalues: 0\n"), "must be positive"),
+    (("        Real: 2.43\n", "        Real: .nan\n"), "Stability.Alpha.Real must be finite"),
+    (("    y: 10\n", "    y: 1\n"), "must both be at least 2"),
+    (("Output:\n    File: data/results/out.h5\n", ""), "Missing or invalid YAML mapping: Output"),
+    (("Folder: data\n", "Folder: data\nFolder: other\n"), "duplicate key"),
+    (("    z: 6\n", "    z: [6]\n"), "unsupported YAML construct"),
+    (("    z: 6\n", "\tz: 6\n"), "tabs"),
+])
+def test_config_errors(tmp_path, edit, message):
+    p = tmp_path / "config.yaml"
+    p.write_text(CONFIG.replace(*edit))
+    with pytest.raises(config.ConfigError, match=message):
+        config.load_config(p)
+
+
+@needs_ref
+def test_reference_config():
+    c = config.load_config(REF / "case" / "config.yaml", require_input=True)
+    assert c.physics.reynolds == 32500 and c.physics.mach == 6.0 and c.physics.nev == 8
+    assert c.input_file == REF / "case" / "data" / "FD-q" / "fdq_sample_qy10_qz6.h5"
+
+
+def test_prepared_round_trip_and_checks(tmp_path):
+    case = make_case(24, 16, physics=Physics())
+    p = output.write_prepared(tmp_path / "fdq_x_qy10_qz6.h5", case)
+    back = prepare.load_prepared(p, 10, 6)
+    assert np.array_equal(back.grid, case.grid) and np.array_equal(back.baseflow, case.baseflow)
+    for r0, r1 in ((case.xi, back.xi), (case.eta, back.eta)):
+        assert np.array_equal(r0.nodes, r1.nodes) and np.array_equal(r0.weights, r1.weights)
+        assert np.array_equal(r0.indices, r1.indices) and np.array_equal(r0.offsets, r1.offsets)
+    with pytest.raises(prepare.PrepareError, match="do not match the YAML"):
+        prepare.load_prepared(p, 8, 6)
+    # a wrong schema version and ordering, as Prepare::readMetadata rejects them
+    for key, value, msg in (("schema_version", 3, "Unsupported FD-q schema version 3"),
+                            ("ordering", "j_k_dof", "ordering must be k_j_dof"),
+                            ("spanwise_periodic", 0, "spanwise_periodic=1")):
+        w = h5.Writer()
+        with h5.File(p) as f:
+            w.attrs.update(f.attrs)
+            w.attrs[key] = value
+            w.dataset("grid", f["grid"][...])
+            w.dataset("baseflow", f["baseflow"][...])
+        bad = tmp_path / f"bad_{key}.h5"
+        w.write(bad)
+        with pytest.raises(prepare.PrepareError, match=msg):
+            prepare.load_prepared(bad)
+
+
+def test_mode_phase():
+    rng = np.random.default_rng(3)
+    v = rng.standard_normal(50) + 1j * rng.standard_normal(50)
+    m = output.fix_mode_phase(v * (2 - 3j))
+    assert abs(np.linalg.norm(m) - 1) < 1e-14
+    k = int(np.argmax(np.abs(m)))
+    assert abs(m[k].imag) <= 1e-15 * abs(m[k]) and m[k].real > 0
+    assert np.allclose(output.fix_mode_phase(1j * v), m)  # phase-independent
+    with pytest.raises(ValueError):
+        output.fix_mode_phase(np.zeros(4))
+
+
+def test_eigen_output_schema(tmp_path):
+    case = make_case(24, 16, physics=Physics(alpha=1.2, omega=complex(0.3, 0.01)))
+    lam = np.array([0.01 - 0.3j, 0.02 - 0.25j])
+    rng = np.random.default_rng(0)
+    modes = rng.standard_normal((2, 5 * case.nodes)) + 1j * rng.standard_normal((2, 5 * case.nodes))
+    p = output.write_eigen_output(tmp_path / "r" / "out.h5", case, "T", lam, [1e-12, 2e-12],
+                                  modes, 8, complex(0.01, -0.3))
+    with h5.File(p) as f:
+        a = f.attrs
+        assert a["schema_version"] == 1 and a["case"] == "T" and a["ordering"] == "k_j_dof"
+        assert a["converged_modes"] == 2 and a["requested_modes"] == 8
+        assert a["lambda_convention"] == "lambda=-i*omega; A_bc*q=lambda*B_bc*q"
+        assert (a["search_center_lambda_real"], a["search_center_lambda_imag"]) == (0.01, -0.3)
+        sl = f["spectrum/lambda"][...]
+        assert np.array_equal(sl[:, 0] + 1j * sl[:, 1], lam)
+        so = f["spectrum/omega"][...]
+        assert np.allclose(so[:, 0] + 1j * so[:, 1], 1j * lam)
+        m0 = f["modes/mode_000"][...]
+        assert m0.shape == (case.nodes, 5, 2)
+        mc = (m0[..., 0] + 1j * m0[..., 1]).reshape(-1)
+        assert np.allclose(mc, output.fix_mode_phase(modes[0]))
+        assert np.array_equal(f["grid"][...], case.grid)
