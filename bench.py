@@ -342,7 +342,8 @@ def main():
                    if last["factor_ms"] > 0 else 0.0},
         "solve": {k: last[k] for k in ("iterations", "solves", "refinement_steps", "factor_ms",
                                        "krylov_ms", "total_ms", "max_relative_error",
-                                       "trisolve_ms", "trisolves")},
+                                       "trisolve_ms", "trisolves", "ortho_ms", "dense_ms",
+                                       "residual_ms")},
         "cpu_baseline": cpu,
         "plain_fp64": plain,
         "sweep_c3": sweep,
