@@ -211,7 +211,10 @@ typedef struct {
                              pivots and factors.  A panel step uses the
                              cluster when at least cluster_panel fully
                              summed rows are left (1: always); 0 (default):
-                             1024; -1: never                                */
+                             256; -1: never.  The cluster keeps the
+                             panel in distributed shared memory when its
+                             rows fit (up to about 3000 rows at complex64,
+                             64 columns)                                */
   int persistent_solve;   /* 0 (default): each triangular solve replays a
                              CUDA graph of per-step launches; 1: one
                              persistent cooperative launch with grid

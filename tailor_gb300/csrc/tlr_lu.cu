@@ -223,6 +223,9 @@ __global__ void __launch_bounds__(512)
 // arithmetic are those of k_panel, so the factors are identical.  Panel
 // data written by other CTAs is read past L1.
 constexpr int kPanelCluster = 8;
+constexpr int kPanelW = 128;  // widest panel (complex64)
+// dynamic shared memory of the shared-memory cluster panel (its rows x w columns)
+constexpr size_t kPanelSmemMax = 200 * 1024;
 
 template <class C>
 __global__ void __cluster_dims__(kPanelCluster, 1, 1) __launch_bounds__(256)
@@ -344,6 +347,161 @@ __global__ void __cluster_dims__(kPanelCluster, 1, 1) __launch_bounds__(256)
     __syncthreads();
   }
   cluster.sync();  // no CTA leaves while others may still read its candidates
+}
+
+// The cluster panel with the panel held in distributed shared memory: each
+// CTA loads its rows of the ww panel columns once (column-major, leading
+// dimension ldp), factors them in shared memory and writes them back at the
+// end, so a column step costs two cluster barriers and a few shared-memory
+// passes instead of several round trips through L2.  CTA 0 owns the top ww
+// rows (pivot rows land there and the sub-panels' U rows live there);
+// CTAs 1.. own contiguous chunks of the rest.  The pivot row swap is done
+// by CTA 0 alone (its own row and the remote row through DSMEM); the other
+// CTAs read the pivot and the sub-panel's U entries from CTA 0.  Pivots,
+// tie-breaking and every arithmetic operation are those of k_panel.
+template <class C>
+__global__ void __cluster_dims__(kPanelCluster, 1, 1) __launch_bounds__(256)
+    k_panel_cluster_sm(const int *__restrict__ fl, int s, int w, C *__restrict__ pool,
+                       const DevFront *__restrict__ fr, int *__restrict__ ipiv,
+                       int *__restrict__ pert, double tiny, int ldp) {
+  namespace cg = cooperative_groups;
+  using T = typename Real<C>::T;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int q = (int)cluster.block_rank();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *P = reinterpret_cast<C *>(smem_raw);  // P[(c - k0) * ldp + (r - ra)]
+  __shared__ T sval[32];
+  __shared__ int sidx[32];
+  __shared__ T cval;
+  __shared__ int cidx;
+  __shared__ C lsub[kSB][kSB];
+  __shared__ C urow[kSB];               // pivot row entries of the sub-panel
+  __shared__ C ublk[kSB][kPanelW];      // sub-panel U rows for the rank-nb update
+  __shared__ C piv;
+  const DevFront f = fr[fl[blockIdx.x / kPanelCluster]];
+  C *F = pool + f.off;
+  const int m = f.m, p = f.p;
+  const int k0 = s * w, ww = min(w, p - k0);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int top_end = k0 + ww;
+  const int rest = p - top_end;
+  const int chunk = (rest + kPanelCluster - 2) / (kPanelCluster - 1);
+  const int ra = q == 0 ? k0 : min(p, top_end + (q - 1) * chunk);
+  const int rb = q == 0 ? top_end : min(p, ra + chunk);
+  const int nown = rb - ra;
+  C *P0 = cluster.map_shared_rank(P, 0);  // CTA 0's panel rows
+  // load the owned rows of the panel
+  for (int x = tid; x < nown * ww; x += nt) {
+    const int rr = x % nown, cc = x / nown;
+    P[cc * ldp + rr] = F[(long long)(k0 + cc) * m + ra + rr];
+  }
+  __syncthreads();
+  for (int jb = 0; jb < ww; jb += kSB) {
+    const int nb = min(kSB, ww - jb);
+    const int c0 = k0 + jb, c1 = c0 + nb;
+    for (int col = c0; col < c1; ++col) {
+      const int cc = col - k0;
+      T best = -1;
+      int bi = p;
+      for (int r = max(ra, col) + tid; r < rb; r += nt) {
+        const T a = cabs1(P[cc * ldp + r - ra]);
+        if (a > best) { best = a; bi = r; }
+      }
+      block_argmax(best, bi, sval, sidx);
+      if (tid == 0) {
+        cval = best;
+        cidx = bi;
+      }
+      cluster.sync();
+      T gb = -1;
+      int gi = p;
+      for (int k = 0; k < kPanelCluster; ++k) {
+        const T a = *cluster.map_shared_rank(&cval, k);
+        const int ia = *cluster.map_shared_rank(&cidx, k);
+        if (a > gb || (a == gb && ia < gi)) {
+          gb = a;
+          gi = ia;
+        }
+      }
+      const int pr = gi < p ? gi : col;
+      if (q == 0) {
+        if (tid == 0) ipiv[f.toff + col] = pr;
+        if (pr != col) {
+          // owner of row pr and its local row (CTA 0 owns [k0, top_end))
+          const int qo = pr < top_end ? 0 : 1 + (pr - top_end) / chunk;
+          const int ro = pr - (qo == 0 ? k0 : top_end + (qo - 1) * chunk);
+          C *Po = cluster.map_shared_rank(P, qo);
+          for (int c = tid; c < ww; c += nt) {
+            const C t = P[c * ldp + col - k0];
+            P[c * ldp + col - k0] = Po[c * ldp + ro];
+            Po[c * ldp + ro] = t;
+          }
+        }
+        __syncthreads();  // the pivot's own column may have been swapped by another thread
+        if (tid == 0 && cabs1(P[cc * ldp + col - k0]) == T(0)) {
+          P[cc * ldp + col - k0] = cmake<C>((T)tiny, 0);
+          atomicAdd(pert, 1);
+        }
+      }
+      cluster.sync();
+      if (tid == 0) piv = P0[cc * ldp + col - k0];
+      if (tid < c1 - col - 1) urow[tid] = P0[(cc + 1 + tid) * ldp + col - k0];
+      __syncthreads();
+      const C inv = cinv(piv);
+      const int r0 = max(ra, col + 1);
+      for (int r = r0 + tid; r < rb; r += nt)
+        P[cc * ldp + r - ra] = cmul(P[cc * ldp + r - ra], inv);
+      __syncthreads();
+      const int nr = rb - r0, nc = c1 - col - 1;
+      for (int x = tid; x < nr * nc; x += nt) {
+        const int r = r0 + x % nr, c = col + 1 + x / nr;
+        P[(c - k0) * ldp + r - ra] =
+            cfms(P[(c - k0) * ldp + r - ra], P[cc * ldp + r - ra], urow[c - col - 1]);
+      }
+      __syncthreads();
+    }
+    if (c1 >= k0 + ww) break;
+    if (q == 0) {
+      for (int x = tid; x < nb * nb; x += nt)
+        lsub[x / nb][x % nb] = P[(c0 - k0 + x % nb) * ldp + c0 - k0 + x / nb];
+      __syncthreads();
+      for (int c = c1 + tid; c < k0 + ww; c += nt) {
+        C xr[kSB];
+#pragma unroll
+        for (int r = 0; r < kSB; ++r) {
+          if (r >= nb) break;
+          C v = P[(c - k0) * ldp + c0 - k0 + r];
+          for (int rp = 0; rp < r; ++rp) v = cfms(v, lsub[r][rp], xr[rp]);
+          xr[r] = v;
+          P[(c - k0) * ldp + c0 - k0 + r] = v;
+        }
+      }
+    }
+    cluster.sync();
+    // the sub-panel's U rows (CTA 0) for the rank-nb update of the owned rows
+    const int ncr = k0 + ww - c1;
+    for (int x = tid; x < nb * ncr; x += nt) {
+      const int t = x / ncr, c = c1 + x % ncr;
+      ublk[t][c - c1] = P0[(c - k0) * ldp + c0 - k0 + t];
+    }
+    __syncthreads();
+    const int r0 = max(ra, c1);
+    const int nr = rb - r0;
+    for (int x = tid; x < nr * ncr; x += nt) {
+      const int r = r0 + x % nr, c = c1 + x / nr;
+      C v = P[(c - k0) * ldp + r - ra];
+#pragma unroll
+      for (int t = 0; t < kSB; ++t)
+        if (t < nb) v = cfms(v, P[(c0 - k0 + t) * ldp + r - ra], ublk[t][c - c1]);
+      P[(c - k0) * ldp + r - ra] = v;
+    }
+    __syncthreads();
+  }
+  cluster.sync();  // every remote read and swap is done
+  for (int x = tid; x < nown * ww; x += nt) {
+    const int rr = x % nown, cc = x / nown;
+    F[(long long)(k0 + cc) * m + ra + rr] = P[cc * ldp + rr];
+  }
 }
 
 template <class C>
@@ -1648,6 +1806,9 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
   TLR_CUDA(ctx, cudaFuncSetAttribute(k_trsm_urow<C>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+  TLR_CUDA(ctx, cudaFuncSetAttribute(k_panel_cluster_sm<C>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kPanelSmemMax));
   for (size_t h = 0; h < levels.size(); ++h) {
     const Level &L = levels[h];
     TLR_CUDA(ctx, cudaMemsetAsync(P + L.pool_begin, 0,
@@ -1668,8 +1829,14 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
       const Step &S = L.steps[s];
       // the cluster panel pays off once the largest front still has many
       // fully summed rows; both give the same pivots and factors
-      const bool cluster = L.pmax - s * w >= cluster_rows;
-      if (cluster)
+      const int rem = L.pmax - s * w;
+      const bool cluster = rem >= cluster_rows;
+      // rows per CTA of the cluster (CTA 0: the top w rows)
+      const int ldp = std::max(w, (rem + kPanelCluster - 2) / (kPanelCluster - 1));
+      const size_t psm = (size_t)w * ldp * sizeof(C);
+      if (cluster && psm <= kPanelSmemMax)
+        { k_panel_cluster_sm<C><<<S.nf * kPanelCluster, 256, psm, st>>>(fl, s, w, P, d_fronts, d_ipiv, d_pert, tiny, ldp); count_launches(); }
+      else if (cluster)
         { k_panel_cluster<C><<<S.nf * kPanelCluster, 256, 0, st>>>(fl, s, w, P, d_fronts, d_ipiv, d_pert, tiny); count_launches(); }
       else
         { k_panel<C><<<S.nf, 512, 0, st>>>(fl, s, w, P, d_fronts, d_ipiv, d_pert, tiny); count_launches(); }

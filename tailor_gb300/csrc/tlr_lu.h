@@ -15,7 +15,7 @@ struct DevFront {
 
 
 // Default of Factor::cluster_rows (the automatic cluster-panel choice).
-constexpr int kClusterPanelRows = 1024;
+constexpr int kClusterPanelRows = 256;
 
 struct Step {  // one panel step of one level
   int nf, max_m, max_b, max_ext, prefix_off, tiles;
