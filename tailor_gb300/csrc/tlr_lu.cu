@@ -212,6 +212,36 @@ __global__ void __launch_bounds__(512)
   }
 }
 
+// The cluster-wide pivot: the largest candidate value over the KC CTAs,
+// ties to the smaller row (the order of a sequential scan over the CTAs).
+// Warp 0 reads one candidate per lane from the other CTAs' shared memory
+// and reduces with shuffles; the winner is broadcast through shared memory.
+template <class T, int KC>
+__device__ __forceinline__ int cluster_argmax(cooperative_groups::cluster_group &cluster,
+                                              T *cval, int *cidx, int none, int *gsel) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    T a = -1;
+    int ia = none;
+    if (lane < KC) {
+      a = *cluster.map_shared_rank(cval, lane);
+      ia = *cluster.map_shared_rank(cidx, lane);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const T a2 = __shfl_down_sync(0xffffffffu, a, o);
+      const int i2 = __shfl_down_sync(0xffffffffu, ia, o);
+      if (a2 > a || (a2 == a && i2 < ia)) {
+        a = a2;
+        ia = i2;
+      }
+    }
+    if (lane == 0) gsel[0] = ia;
+  }
+  __syncthreads();
+  return gsel[0];
+}
+
 // The same panel factorisation spread over a thread-block cluster of
 // kPanelCluster CTAs (one cluster per front): CTA 0 owns the panel's top ww
 // rows (where pivots land, and the U rows of every sub-panel), CTAs 1..7
@@ -240,6 +270,7 @@ __global__ void __cluster_dims__(kPanelCluster, 1, 1) __launch_bounds__(256)
   __shared__ int sidx[32];
   __shared__ T cval;
   __shared__ int cidx;
+  __shared__ int gsel[1];
   __shared__ C lsub[kSB][kSB];
   const DevFront f = fr[fl[blockIdx.x / kPanelCluster]];
   C *F = pool + f.off;
@@ -270,16 +301,7 @@ __global__ void __cluster_dims__(kPanelCluster, 1, 1) __launch_bounds__(256)
       }
       cluster.sync();
       // every CTA reads the kPanelCluster candidates and picks the same pivot
-      T gb = -1;
-      int gi = p;
-      for (int k = 0; k < kPanelCluster; ++k) {
-        const T a = *cluster.map_shared_rank(&cval, k);
-        const int ia = *cluster.map_shared_rank(&cidx, k);
-        if (a > gb || (a == gb && ia < gi)) {
-          gb = a;
-          gi = ia;
-        }
-      }
+      const int gi = cluster_argmax<T, kPanelCluster>(cluster, &cval, &cidx, p, gsel);
       const int pr = gi < p ? gi : col;
       if (q == 0) {
         if (tid == 0) ipiv[f.toff + col] = pr;
@@ -374,6 +396,7 @@ __global__ void __cluster_dims__(kPanelCluster, 1, 1) __launch_bounds__(256)
   __shared__ int sidx[32];
   __shared__ T cval;
   __shared__ int cidx;
+  __shared__ int gsel[1];
   __shared__ C lsub[kSB][kSB];
   __shared__ C urow[kSB];               // pivot row entries of the sub-panel
   __shared__ C ublk[kSB][kPanelW];      // sub-panel U rows for the rank-nb update
@@ -413,16 +436,7 @@ __global__ void __cluster_dims__(kPanelCluster, 1, 1) __launch_bounds__(256)
         cidx = bi;
       }
       cluster.sync();
-      T gb = -1;
-      int gi = p;
-      for (int k = 0; k < kPanelCluster; ++k) {
-        const T a = *cluster.map_shared_rank(&cval, k);
-        const int ia = *cluster.map_shared_rank(&cidx, k);
-        if (a > gb || (a == gb && ia < gi)) {
-          gb = a;
-          gi = ia;
-        }
-      }
+      const int gi = cluster_argmax<T, kPanelCluster>(cluster, &cval, &cidx, p, gsel);
       const int pr = gi < p ? gi : col;
       if (q == 0) {
         if (tid == 0) ipiv[f.toff + col] = pr;
