@@ -142,7 +142,7 @@ def c3_sweep_inputs(npoints=64, seed=2026):
 def run_c3(api, npoints=64):
     """The sweep in the plain FP64 form (one instance at a time, CUDA-core
     FP64 fronts) and in the mixed + batched form (complex64 fronts with
-    tensor-core Schur updates and FP64 refinement, six concurrent instances,
+    tensor-core Schur updates and FP64 refinement, eight concurrent instances,
     autotuned kernels): eigenpairs at resid <= 1e-10 per wall second."""
     cases, points = c3_sweep_inputs(npoints)
     out = {}
