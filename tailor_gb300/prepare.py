@@ -82,14 +82,31 @@ def periodic_quintic_spline(z_old, y_old, values, z_new, y_new, z_period=2.0,
     from scipy.interpolate import make_interp_spline
 
     z_old = np.asarray(z_old, dtype=np.float64)
+    y_old = np.asarray(y_old, dtype=np.float64)
+    z_new = np.asarray(z_new, dtype=np.float64)
+    y_new = np.asarray(y_new, dtype=np.float64)
     field = np.asarray(values)
+    if z_old.ndim != 1 or y_old.ndim != 1:
+        raise PrepareError("source logical coordinates must be one-dimensional")
+    if z_new.ndim != 1 or y_new.ndim != 1:
+        raise PrepareError("target logical coordinates must be one-dimensional")
+    if z_old.size < 6 or y_old.size < 6:
+        raise PrepareError("periodic quintic interpolation requires at least 6 nodes per axis")
+    if field.shape != (z_old.size, y_old.size):
+        raise PrepareError(f"values must have shape {(z_old.size, y_old.size)}; got {field.shape}")
+    if not np.isfinite(z_period) or z_period <= 0.0:
+        raise PrepareError("z_period must be finite and positive")
+    if not all(np.all(np.isfinite(a)) for a in (z_old, y_old, z_new, y_new, field)):
+        raise PrepareError("periodic spline coordinates and values must be finite")
+    if np.any(np.diff(z_old) <= 0.0) or np.any(np.diff(y_old) <= 0.0):
+        raise PrepareError("source logical coordinates must be strictly increasing")
     spacing = z_period / z_old.size
     if float(np.max(np.abs(np.diff(z_old) - spacing))) > 5e-13 * max(1.0, abs(spacing)):
         raise PrepareError("periodic source logical nodes must be uniformly spaced")
     if z_old[-1] >= z_old[0] + z_period:
         raise PrepareError("periodic source nodes must not include the repeated endpoint")
     src_phase = (z_old - z_old[0]) / z_period
-    tgt_phase = (np.asarray(z_new) - z_old[0]) / z_period
+    tgt_phase = (z_new - z_old[0]) / z_period
     periodic = field - src_phase[:, None] * value_translation
 
     def scalar(v):

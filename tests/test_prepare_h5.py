@@ -236,3 +236,101 @@ def test_eigen_output_schema(tmp_path):
         mc = (m0[..., 0] + 1j * m0[..., 1]).reshape(-1)
         assert np.allclose(mc, output.fix_mode_phase(modes[0]))
         assert np.array_equal(f["grid"][...], case.grid)
+
+
+# ---- the reference's interpolation and preparation tests
+# (tests/Python/test_interpolate.py:77-176), restated
+
+def test_periodic_complex_field_and_affine_translation():
+    z_old = -1.0 + 2.0 * np.arange(24) / 24
+    y_old = np.linspace(-1.0, 1.0, 9)
+    zg, yg = np.meshgrid(z_old, y_old, indexing="ij")
+    tr = 7.5
+
+    def field(z, y):
+        return (np.sin(np.pi * z) * (1.0 + y ** 3) + 1j * np.cos(2.0 * np.pi * z) * (2.0 - y)
+                + 0.5 * (z + 1.0) * tr)
+
+    z_new = -1.0 + 2.0 * np.arange(48) / 48
+    y_new = np.linspace(-1.0, 1.0, 13)
+    got = prepare.periodic_quintic_spline(z_old, y_old, field(zg, yg), z_new, y_new,
+                                          value_translation=tr)
+    zt, yt = np.meshgrid(z_new, y_new, indexing="ij")
+    np.testing.assert_allclose(got, field(zt, yt), rtol=2e-6, atol=5e-6)
+
+
+def test_periodic_spline_rejections():
+    y = np.linspace(-1.0, 1.0, 8)
+    z = np.linspace(-1.0, 1.0, 12)  # repeats the periodic endpoint
+    with pytest.raises(prepare.PrepareError, match="uniformly spaced"):
+        prepare.periodic_quintic_spline(z, y, np.zeros((12, 8)), z[:-1], y)
+    zp = -1.0 + 2.0 * np.arange(5) / 5
+    with pytest.raises(prepare.PrepareError, match="at least 6"):
+        prepare.periodic_quintic_spline(zp, y, np.zeros((5, 8)), zp, y)
+    zp = -1.0 + 2.0 * np.arange(12) / 12
+    with pytest.raises(prepare.PrepareError, match="values must have shape"):
+        prepare.periodic_quintic_spline(zp, y, np.zeros((8, 12)), zp, y)
+
+
+def _write_source(path, ny=8, nz=12, period=6.0):
+    y = np.linspace(-1.0, 1.0, ny)
+    eta = -1.0 + 2.0 * np.arange(nz) / nz
+    eg, yg = np.meshgrid(eta, y, indexing="ij")
+    grid = np.zeros((nz, ny, 3), dtype=np.complex128)
+    grid[..., 1] = yg
+    grid[..., 2] = 0.5 * (eg + 1.0) * period
+    base = np.zeros((nz, ny, 5), dtype=np.complex128)
+    base[..., 0] = 1.0 + 0.02 * np.cos(np.pi * eg)
+    base[..., 1] = 0.5 + 0.1 * (1.0 + yg)
+    base[..., 2] = 0.01 * np.sin(np.pi * eg)
+    base[..., 3] = 0.02 * np.cos(np.pi * eg)
+    base[..., 4] = 1.0 + 0.05 * yg
+    w = h5.Writer()
+    w.attrs.update({"Ny": ny, "Nz": nz, "spanwise_periodic": 1, "spanwise_period": period})
+    w.dataset("grid", np.stack((grid.real, grid.imag), axis=-1))
+    w.dataset("baseflow", np.stack((base.real, base.imag), axis=-1))
+    w.write(path)
+    return grid, base
+
+
+def test_schema_v2_preparation_and_stale_cache_rebuild(tmp_path):
+    from tailor_gb300 import run
+    data = tmp_path / "data"
+    data.mkdir()
+    grid, base = _write_source(data / "sample.h5")
+    (tmp_path / "config.yaml").write_text(
+        CONFIG.replace("    y: 10\n    z: 6\n", "    y: 4\n    z: 4\n"))
+    cfg = config.load_config(tmp_path / "config.yaml")
+    case = run.prepared_case(cfg, verbose=False)
+    assert (case.ny, case.nz, case.qy, case.qz) == (8, 12, 4, 4)
+    with h5.File(cfg.input_file) as f:
+        assert f.attrs["schema_version"] == 2 and f.attrs["source_file"] == "sample.h5"
+        assert f.attrs["interpolation_version"] == 3
+        assert f["discretization/z"].attrs["topology"] == "periodic"
+        assert f["discretization/z/stencil_offsets"][...].shape == (12, 5)
+    # corner preservation: the source's corner values survive interpolation
+    g = (case.grid[..., 0] + 1j * case.grid[..., 1]).reshape(12, 8, 3)
+    assert np.allclose(g[0, 0], grid[0, 0]) and np.allclose(g[-1, -1], grid[-1, -1])
+    # a stale cache (wrong schema) is rebuilt
+    w = h5.Writer()
+    with h5.File(cfg.input_file) as f:
+        w.attrs.update(f.attrs)
+        w.attrs["schema_version"] = 1
+    w.write(cfg.input_file)
+    run.prepared_case(cfg, verbose=False)
+    with h5.File(cfg.input_file) as f:
+        assert f.attrs["schema_version"] == 2
+
+
+def test_launcher_prepare_only(tmp_path):
+    from tailor_gb300 import run
+    data = tmp_path / "data"
+    data.mkdir()
+    _write_source(data / "sample.h5")
+    (tmp_path / "config.yaml").write_text(
+        CONFIG.replace("    y: 10\n    z: 6\n", "    y: 4\n    z: 4\n"))
+    assert run.main(["-c", str(tmp_path / "config.yaml"), "--prepare-only"]) == 0
+    assert (data / "FD-q" / "fdq_sample_qy4_qz4.h5").is_file()
+    (tmp_path / "bad.yaml").write_text(CONFIG.replace("Q-Value:\n    y: 10\n    z: 6\n",
+                                                      "Q-Value: 5\n"))
+    assert run.main(["-c", str(tmp_path / "bad.yaml"), "--prepare-only"]) == 1
