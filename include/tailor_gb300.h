@@ -345,6 +345,20 @@ int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sweep_point *
 int tlr_schur_update_c64(const float *front, int m, int p, int k0, int w, unsigned lbo,
                          unsigned sbo, float *out);
 
+/* An explicit generalized pencil A x = lambda B x as a solver context
+ * (EigenSolver::solve(recipe, eigenMatrix, massMatrix, ...),
+ * EigenSolver.hpp:60-67: the overload for small independently known
+ * problems).  A and B are dense n x n complex matrices, column-major with
+ * interleaved (re, im) doubles; B must be block diagonal in 5 x 5 blocks
+ * (TLR_ERR_ARG otherwise).  The recipe supplies the search centre omega,
+ * nev, tol and max_it.  The context accepts tlr_solve (FP64 or mixed
+ * form), tlr_spmv and tlr_copy_out of A and B, tlr_set_alpha (a new search
+ * centre) and tlr_set_physics; the grid stages return TLR_ERR_WRONGSTATE.
+ * Modes are returned as 5 * ceil(n / 5) complex entries (the first n are
+ * the eigenvector). */
+int tlr_pencil_create(const tlr_recipe *recipe, int n, const double *A, const double *B,
+                      int device, tlr_ctx **out);
+
 /* FD-q rule generation on the host (src/Python/fdq_nodes.py:280-353,
  * calculate_fdq_rule and calculate_periodic_fdq_rule).  periodic = 0: the
  * equal-error nodes on [-1, 1] with node_count - 1 intervals (period is

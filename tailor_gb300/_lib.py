@@ -147,6 +147,7 @@ SIGNATURES = {
     "tlr_sweep": ([_P, _I, _P, _I, _P, _P, _P, _P, _P, _P], _I),
     "tlr_schur_update_c64": ([_P, _I, _I, _I, _I, ctypes.c_uint, ctypes.c_uint, _P], _I),
     "tlr_wait_selftest": ([_I, ctypes.c_uint, _P], _I),
+    "tlr_pencil_create": ([_P, _I, _P, _P, _I, _P], _I),
     "tlr_fdq_rule": ([_I, _I, _I, ctypes.c_double, _P, _P, _P, _P, _P], _I),
     "tlr_frobenius_noalloc": ([_P, ctypes.c_size_t, _P, _P], _I),
     "tlr_mlp_create": ([_I, _I, _I, _I, ctypes.c_ulonglong, _P], _I),

@@ -249,6 +249,57 @@ class EigenSolver:
         return EigenSolution(lam_c, res[:nconv], vec_c, _diag_dict(d))
 
 
+class PencilProblem(Problem):
+    """An explicit generalized pencil A x = lambda B x in place of the
+    assembled operators: the reference's EigenSolver overload for small
+    independently known problems (EigenSolver.hpp:60-67).  B must be block
+    diagonal in 5 x 5 blocks.  ``physics`` supplies omega (the search
+    centre), nev, tol and max_it; ``EigenSolver(p).solve(...)`` runs as for
+    a grid problem and ``solve_pencil`` trims the modes to n entries."""
+
+    def __init__(self, A, B, physics=None, device: int = -1):
+        from types import SimpleNamespace
+        from .case import Physics
+        self.lib = L.load()
+        self._keep = []
+        self.ctx = None
+        A = np.asarray(A, dtype=np.complex128)
+        B = np.asarray(B, dtype=np.complex128)
+        if A.ndim != 2 or A.shape[0] != A.shape[1] or B.shape != A.shape:
+            raise ValueError("A and B must be square matrices of the same order")
+        self.n = A.shape[0]
+        ph = physics or Physics()
+        self.case = SimpleNamespace(nodes=(self.n + 4) // 5, physics=ph)
+        recipe = L.Recipe(0, 0, ph.mach, ph.reynolds, ph.prandtl, ph.gas_constant, ph.gamma,
+                          ph.reference_viscosity, ph.reference_temperature,
+                          ph.sutherland_constant, complex(ph.alpha).real,
+                          complex(ph.alpha).imag, complex(ph.omega).real,
+                          complex(ph.omega).imag, ph.nev, ph.tol, ph.max_it)
+        # column-major, interleaved (re, im)
+        a = np.ascontiguousarray(np.stack([A.T.real, A.T.imag], axis=-1))
+        b = np.ascontiguousarray(np.stack([B.T.real, B.T.imag], axis=-1))
+        ctx = ctypes.c_void_p()
+        st = self.lib.tlr_pencil_create(ctypes.byref(recipe), self.n, a.ctypes.data,
+                                        b.ctypes.data, device, ctypes.byref(ctx))
+        if st:
+            raise TailorError(st, self.lib.tlr_last_error(None).decode())
+        self.ctx = ctx
+
+
+def solve_pencil(A, B, omega: complex = 0j, nev: int = 2, tol: float = 1e-10,
+                 max_it: int = 1000, precision: int = 0, modes: bool = True,
+                 **kw) -> EigenSolution:
+    """The nev eigenpairs of A x = lambda B x nearest lambda_s = Im(omega) -
+    i Re(omega) (EigenSolver.cpp:118-120), on the GPU."""
+    from .case import Physics
+    with PencilProblem(A, B, Physics(omega=omega, nev=nev, tol=tol, max_it=max_it)) as p:
+        sol = EigenSolver(p).solve(nev=nev, tol=tol, max_it=max_it, precision=precision,
+                                   modes=modes, **kw)
+        if sol.modes is not None:
+            sol.modes = sol.modes[:, :p.n]
+    return sol
+
+
 @dataclass
 class SweepResult:
     lam: np.ndarray        # [points][nev] complex (0 where not converged)

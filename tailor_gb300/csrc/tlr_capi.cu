@@ -267,6 +267,7 @@ void tlr_ctx_destroy(tlr_ctx *ctx) {
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->own_sym_free) ctx->own_sym_free(ctx->own_sym);
   delete ctx;
 }
 
@@ -277,6 +278,10 @@ int tlr_set_alpha(tlr_ctx *ctx, double alpha_re, double alpha_im, double omega_r
   ctx->recipe.alpha_im = alpha_im;
   ctx->recipe.omega_re = omega_re;
   ctx->recipe.omega_im = omega_im;
+  if (ctx->pencil) {  // a new search centre; the pencil itself is unchanged
+    invalidate_factor(ctx);
+    return TLR_OK;
+  }
   ctx->assembled = false;
   ctx->have_bc = false;
   invalidate_factor(ctx);
@@ -288,13 +293,16 @@ int tlr_set_physics(tlr_ctx *ctx, const tlr_recipe *recipe) {
   if (recipe->q_y != ctx->recipe.q_y || recipe->q_z != ctx->recipe.q_z)
     return fail(ctx, TLR_ERR_SIZE, "FD-q degrees cannot change within a context");
   ctx->recipe = *recipe;
+  invalidate_factor(ctx);
+  if (ctx->pencil) return TLR_OK;
   ctx->assembled = false;
   ctx->have_bc = false;
-  invalidate_factor(ctx);
   return TLR_OK;
 }
 
 int tlr_load_fields(tlr_ctx *ctx, const double *grid, const double *baseflow) {
+  if (ctx && ctx->pencil)
+    return fail(ctx, TLR_ERR_WRONGSTATE, "not available for an explicit pencil");
   if (!ctx || !grid || !baseflow) return fail(ctx, TLR_ERR_ARG, "null field array");
   TLR_CUDA(ctx, cudaMemcpyAsync(ctx->grid_c, grid, sizeof(double) * 6 * ctx->nn,
                                 cudaMemcpyHostToDevice, ctx->stream));
@@ -308,6 +316,8 @@ int tlr_load_fields(tlr_ctx *ctx, const double *grid, const double *baseflow) {
 }
 
 int tlr_metrics(tlr_ctx *ctx, tlr_metric_diag *diag) {
+  if (ctx && ctx->pencil)
+    return fail(ctx, TLR_ERR_WRONGSTATE, "not available for an explicit pencil");
   if (!ctx) return TLR_ERR_ARG;
   if (!ctx->fields)
     return fail(ctx, TLR_ERR_WRONGSTATE, "Grid data must be prepared before computing metrics");
@@ -318,6 +328,8 @@ int tlr_metrics(tlr_ctx *ctx, tlr_metric_diag *diag) {
 }
 
 int tlr_baseflow_derivatives(tlr_ctx *ctx, tlr_deriv_diag *diag) {
+  if (ctx && ctx->pencil)
+    return fail(ctx, TLR_ERR_WRONGSTATE, "not available for an explicit pencil");
   if (!ctx) return TLR_ERR_ARG;
   if (!ctx->fields)
     return fail(ctx, TLR_ERR_WRONGSTATE,
@@ -332,6 +344,8 @@ int tlr_baseflow_derivatives(tlr_ctx *ctx, tlr_deriv_diag *diag) {
 }
 
 int tlr_assemble(tlr_ctx *ctx, tlr_operator_diag *diag) {
+  if (ctx && ctx->pencil)
+    return fail(ctx, TLR_ERR_WRONGSTATE, "not available for an explicit pencil");
   if (!ctx) return TLR_ERR_ARG;
   if (!ctx->have_metrics)
     return fail(ctx, TLR_ERR_WRONGSTATE, "Metrics are required before matrix assembly");
@@ -346,6 +360,8 @@ int tlr_assemble(tlr_ctx *ctx, tlr_operator_diag *diag) {
 }
 
 int tlr_apply_bc(tlr_ctx *ctx, tlr_bc_diag *diag) {
+  if (ctx && ctx->pencil)
+    return fail(ctx, TLR_ERR_WRONGSTATE, "not available for an explicit pencil");
   if (!ctx) return TLR_ERR_ARG;
   if (!ctx->assembled)
     return fail(ctx, TLR_ERR_WRONGSTATE,
@@ -360,6 +376,8 @@ int tlr_apply_bc(tlr_ctx *ctx, tlr_bc_diag *diag) {
 int tlr_spmv(tlr_ctx *ctx, int which, const double *x, double *y, int device_pointers) {
   if (!ctx || !x || !y) return fail(ctx, TLR_ERR_ARG, "null vector");
   const bool need_bc = which == TLR_MAT_A || which == TLR_MAT_B;
+  if (ctx->pencil && !need_bc)
+    return fail(ctx, TLR_ERR_WRONGSTATE, "not available for an explicit pencil");
   if ((need_bc && !ctx->have_bc) || (!need_bc && !ctx->assembled))
     return fail(ctx, TLR_ERR_WRONGSTATE, "operator is not available yet");
   const size_t bytes = sizeof(double2) * 5 * ctx->nn;
@@ -406,6 +424,9 @@ int tlr_copy_out(tlr_ctx *ctx, int what, void *dst, size_t bytes) {
     return fail(ctx, TLR_ERR_SIZE, "destination size does not match the array");
   const void *src = nullptr;
   bool ready = true;
+  if (ctx->pencil && what != TLR_OUT_ROW_PTR && what != TLR_OUT_COL_IDX &&
+      what != TLR_OUT_A_VALUES && what != TLR_OUT_B_VALUES)
+    return fail(ctx, TLR_ERR_WRONGSTATE, "not available for an explicit pencil");
   switch (what) {
     case TLR_OUT_METRICS:
       if (!ctx->have_metrics) ready = false;

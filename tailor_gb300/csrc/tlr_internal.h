@@ -114,6 +114,10 @@ struct tlr_ctx {
 
   bool fields = false, have_metrics = false, have_derivs = false;
   bool assembled = false, have_bc = false;
+  // an explicit pencil (tlr_pencil_create): only A, B and the solve exist
+  bool pencil = false;
+  void *own_sym = nullptr;                 // symbolic analysis owned by the context
+  void (*own_sym_free)(void *) = nullptr;
   std::string last_error;
   tlr::Factor *factor = nullptr;
 };

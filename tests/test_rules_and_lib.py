@@ -87,3 +87,20 @@ def test_rebuilt_baseflow_matches_synthetic_case():
     c.physics = Physics(mach=0.85)
     assert np.array_equal(rebuild_baseflow(c),
                           make_case(24, 16, physics=Physics(mach=0.85), amplitude=0.08).baseflow)
+
+
+def test_pencil_argument_checks_without_gpu():
+    """tlr_pencil_create rejects malformed pencils before touching the device."""
+    from tailor_gb300 import api
+    tb.build()
+    A = np.eye(6, dtype=complex)
+    B = np.eye(6, dtype=complex)
+    B[0, 5] = 0.5  # couples two 5 x 5 blocks
+    with pytest.raises(api.TailorError, match="block diagonal"):
+        api.PencilProblem(A, B)
+    B = np.eye(6, dtype=complex)
+    A[2, 3] = np.nan
+    with pytest.raises(api.TailorError, match="non-finite"):
+        api.PencilProblem(A, B)
+    with pytest.raises(ValueError, match="square"):
+        api.PencilProblem(np.eye(3), np.eye(4))
