@@ -46,24 +46,35 @@ int upload_rule(tlr_ctx *ctx, const tlr_rule *r, int expected_nodes,
   h_w1.assign(r->weights + (size_t)n * s, r->weights + (size_t)2 * n * s);
   h_w2.assign(r->weights + (size_t)2 * n * s, r->weights + (size_t)3 * n * s);
   std::vector<int> centre(n, -1), order((size_t)n * s);
+  // messages of Prepare.cpp:374-407 (validateRule)
+  const char *name = periodic ? "eta" : "xi";
+  char msg[160];
   for (int row = 0; row < n; ++row) {
     for (int k = 0; k < s; ++k) {
       const int off = h_off[(size_t)row * s + k], idx = h_idx[(size_t)row * s + k];
       const int un = row + off;
       const int wrapped = periodic ? ((un % n) + n) % n : un;
-      if (idx < 0 || idx >= n || wrapped != idx)
-        return fail(ctx, TLR_ERR_STENCIL,
-                    "FD-q stencil indices and offsets are inconsistent");
-      if (!periodic && (un < 0 || un >= n))
-        return fail(ctx, TLR_ERR_STENCIL,
-                    "An FD-q stencil extends outside the bounded grid");
+      if (idx < 0 || idx >= n) {
+        snprintf(msg, sizeof msg, "%s FD-q row %d contains out-of-range index %d", name, row, idx);
+        return fail(ctx, TLR_ERR_STENCIL, msg);
+      }
+      if (wrapped != idx) {
+        snprintf(msg, sizeof msg, "%s %s row %d has inconsistent stencil index/offset", name,
+                 periodic ? "periodic" : "bounded", row);
+        return fail(ctx, TLR_ERR_STENCIL, msg);
+      }
       if (off == 0) centre[row] = k;
       for (int d = 0; d < 3; ++d)
-        if (!std::isfinite(r->weights[(size_t)d * n * s + (size_t)row * s + k]))
-          return fail(ctx, TLR_ERR_NONFINITE, "FD-q weights are not finite");
+        if (!std::isfinite(r->weights[(size_t)d * n * s + (size_t)row * s + k])) {
+          snprintf(msg, sizeof msg, "%s FD-q weight is not finite at row %d", name, row);
+          return fail(ctx, TLR_ERR_NONFINITE, msg);
+        }
     }
-    if (centre[row] < 0)
-      return fail(ctx, TLR_ERR_STENCIL, "FD-q stencil does not contain its own node");
+    if (centre[row] < 0) {
+      snprintf(msg, sizeof msg, "%s FD-q stencil row %d does not contain its evaluation node",
+               name, row);
+      return fail(ctx, TLR_ERR_STENCIL, msg);
+    }
     std::vector<int> o(s);
     std::iota(o.begin(), o.end(), 0);
     std::stable_sort(o.begin(), o.end(), [&](int a, int b) {

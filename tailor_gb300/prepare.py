@@ -212,23 +212,70 @@ def prepare_sample(path: str | Path, q_y: int = 10, q_z: int = 6,
 
 # ---- prepared schema-2 case files -----------------------------------------
 
-def _rule_from(group, node_count: int, q: int, periodic: bool, period: float) -> Rule:
+def _dataset(group, gpath: str, name: str, shape: tuple[int, ...]) -> np.ndarray:
+    """A rule dataset with the reference's messages (Prepare.cpp:74-110)."""
+    path = f"{gpath}/{name}"
     try:
-        nodes = np.asarray(group["nodes"][...], dtype=np.float64)
-        idx = np.asarray(group["stencil_indices"][...])
-        off = np.asarray(group["stencil_offsets"][...])
-        w = np.stack([np.asarray(group[f"weights/d{k}"][...], dtype=np.float64)
-                      for k in range(3)])
+        a = np.asarray(group[name][...])
     except KeyError as e:
-        raise PrepareError(f"Failed to load FD-q discretization: missing {e}") from e
+        raise PrepareError(f"Failed to load FD-q discretization: Missing HDF5 dataset: "
+                           f"{path}") from e
+    if a.shape != shape:
+        raise PrepareError(f"Failed to load FD-q discretization: Unexpected shape for HDF5 "
+                           f"dataset: {path}")
+    return a
+
+
+def _rule_from(group, gpath: str, node_count: int, q: int, periodic: bool,
+               period: float) -> Rule:
     s = q + 1
-    if nodes.shape != (node_count,) or idx.shape != (node_count, s) or \
-            off.shape != (node_count, s) or w.shape != (3, node_count, s):
-        raise PrepareError("Failed to load FD-q discretization: rule arrays have the wrong shape")
+    nodes = _dataset(group, gpath, "nodes", (node_count,)).astype(np.float64)
+    idx = _dataset(group, gpath, "stencil_indices", (node_count, s))
+    off = _dataset(group, gpath, "stencil_offsets", (node_count, s))
+    w = np.stack([_dataset(group, gpath, f"weights/d{k}", (node_count, s)).astype(np.float64)
+                  for k in range(3)])
     return Rule(n=node_count, q=q, periodic=periodic, period=period, nodes=nodes,
                 indices=np.ascontiguousarray(idx, dtype=np.int32),
                 offsets=np.ascontiguousarray(off, dtype=np.int32),
                 weights=np.ascontiguousarray(w))
+
+
+def validate_rule(name: str, r: Rule) -> None:
+    """The rule checks of Prepare.cpp:328-437 with its messages: metadata,
+    node order, stencil indices and offsets, finite weights, the evaluation
+    node in every stencil, and exactness on 1, x, x^2 (5e-9 x max(1, |exact|))."""
+    n, s = r.n, r.q + 1
+    if not (n >= 3 and 2 <= r.q < n):
+        raise PrepareError(f"{name} FD-q metadata must satisfy node_count > q >= 2")
+    if not np.isfinite(r.period) or r.period <= 0:
+        raise PrepareError(f"{name} FD-q period must be finite and positive")
+    if r.periodic and r.q % 2:
+        raise PrepareError(f"{name} periodic FD-q degree must be even")
+    for row in range(n):
+        x = r.nodes[row]
+        if not np.isfinite(x):
+            raise PrepareError(f"{name} FD-q node {row} is not finite")
+        if row > 0 and not x > r.nodes[row - 1]:
+            raise PrepareError(f"{name} FD-q nodes must be strictly increasing")
+        cols, offs = r.indices[row], r.offsets[row]
+        for c, o in zip(cols, offs):
+            if not 0 <= c < n:
+                raise PrepareError(f"{name} FD-q row {row} contains out-of-range index {c}")
+            if (row + o) % n != c if r.periodic else row + o != c:
+                kind = "periodic" if r.periodic else "bounded"
+                raise PrepareError(f"{name} {kind} row {row} has inconsistent stencil index/offset")
+        if not np.all(np.isfinite(r.weights[:, row])):
+            raise PrepareError(f"{name} FD-q weight is not finite at row {row}")
+        if row not in cols:
+            raise PrepareError(f"{name} FD-q stencil row {row} does not contain its evaluation node")
+        xs = x + offs * (r.period / n) if r.periodic else r.nodes[cols]
+        for d in range(3):
+            for pw in range(3):
+                approx = float(np.sum(r.weights[d, row] * xs ** pw))
+                exact = [[1.0, x, x * x], [0.0, 1.0, 2.0 * x], [0.0, 0.0, 2.0]][d][pw]
+                if abs(approx - exact) > 5e-9 * max(1.0, abs(exact)):
+                    raise PrepareError(f"{name} FD-q order-{d} weights fail degree-{pw} "
+                                       f"polynomial check at row {row}")
 
 
 def load_prepared(path: str | Path, q_y: int | None = None, q_z: int | None = None,
@@ -269,8 +316,10 @@ def load_prepared(path: str | Path, q_y: int | None = None, q_z: int | None = No
         if gy.attrs.get("topology") != "bounded" or gz.attrs.get("topology") != "periodic":
             raise PrepareError("Failed to load FD-q discretization: Expected bounded y and "
                                "periodic z FD-q topologies")
-        xi = _rule_from(gy, ny, q_y, False, float(gy.attrs["period"]))
-        eta = _rule_from(gz, nz, q_z, True, float(gz.attrs["period"]))
+        xi = _rule_from(gy, "/discretization/y", ny, q_y, False, float(gy.attrs["period"]))
+        eta = _rule_from(gz, "/discretization/z", nz, q_z, True, float(gz.attrs["period"]))
+        validate_rule("xi", xi)
+        validate_rule("eta", eta)
         if "baseflow" not in f:
             raise PrepareError("HDF5 dataset /baseflow is missing")
         if "grid" not in f:

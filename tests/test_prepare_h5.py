@@ -334,3 +334,76 @@ def test_launcher_prepare_only(tmp_path):
     (tmp_path / "bad.yaml").write_text(CONFIG.replace("Q-Value:\n    y: 10\n    z: 6\n",
                                                       "Q-Value: 5\n"))
     assert run.main(["-c", str(tmp_path / "bad.yaml"), "--prepare-only"]) == 1
+
+
+# ---- malformed prepared files (tests/CPlusPlus/test_fdq_loader_failures.py:37-72)
+
+def _copy_with(src, dst, mutate):
+    """Copy a prepared file through the writer, letting mutate(attrs, data)
+    change root attributes and datasets (paths -> arrays; None removes)."""
+    with h5.File(src) as f:
+        attrs = dict(f.attrs)
+        data = {}
+
+        def walk(g, pre):
+            for k in g:
+                o = g[k]
+                if isinstance(o, h5.Group):
+                    walk(o, f"{pre}{k}/")
+                else:
+                    data[f"{pre}{k}"] = (o[...], dict(o.attrs))
+        walk(f, "")
+        gattrs = {p: dict(f[p].attrs) for p in ("discretization/y", "discretization/z")}
+    mutate(attrs, data)
+    w = h5.Writer()
+    w.attrs.update(attrs)
+    for path, (arr, a) in data.items():
+        if arr is not None:
+            w.dataset(path, arr, a)
+    for p, a in gattrs.items():
+        w.group(p).attrs.update(a)
+    w.write(dst)
+
+
+def _drop(path):
+    return lambda attrs, data: data.__setitem__(path, (None, {}))
+
+
+def _wrong_q(attrs, data):
+    attrs["q_y"] = int(attrs["q_y"]) - 1
+
+
+def _wrong_shape(attrs, data):
+    a, at = data["discretization/y/weights/d2"]
+    data["discretization/y/weights/d2"] = (a[:, :-1], at)
+
+
+def _bad_index(attrs, data):
+    a, at = data["discretization/y/stencil_indices"]
+    a = a.copy()
+    a[0, 0] = int(attrs["Ny"])
+    data["discretization/y/stencil_indices"] = (a, at)
+
+
+def _nan_weight(attrs, data):
+    a, at = data["discretization/y/weights/d1"]
+    a = a.copy()
+    a[0, 0] = np.nan
+    data["discretization/y/weights/d1"] = (a, at)
+
+
+@pytest.mark.parametrize("mutate,message", [
+    (_drop("discretization/y/weights/d1"), "Missing HDF5 dataset"),
+    (_wrong_q, "do not match the YAML configuration"),
+    (_wrong_shape, "Unexpected shape for HDF5 dataset"),
+    (_bad_index, "out-of-range index"),
+    (_nan_weight, "weight is not finite"),
+], ids=["missing_weight", "wrong_q", "wrong_shape", "out_of_range_index", "non_finite_weight"])
+def test_malformed_prepared_file(tmp_path, mutate, message):
+    case = make_case(24, 16, physics=Physics())
+    good = output.write_prepared(tmp_path / "good.h5", case)
+    prepare.load_prepared(good, 10, 6)  # the unmodified copy loads
+    bad = tmp_path / "bad.h5"
+    _copy_with(good, bad, mutate)
+    with pytest.raises(prepare.PrepareError, match=message):
+        prepare.load_prepared(bad, 10, 6)
