@@ -27,11 +27,10 @@ import numpy as np
 
 from . import h5
 from .case import Case, Physics
-from .rules import Rule, load_rule
+from .rules import Rule, RuleError, load_rule, validate_rule
 
 
-class PrepareError(ValueError):
-    pass
+PrepareError = RuleError  # rule and case preparation share one error type
 
 
 # ---- structured source samples --------------------------------------------
@@ -238,44 +237,6 @@ def _rule_from(group, gpath: str, node_count: int, q: int, periodic: bool,
                 indices=np.ascontiguousarray(idx, dtype=np.int32),
                 offsets=np.ascontiguousarray(off, dtype=np.int32),
                 weights=np.ascontiguousarray(w))
-
-
-def validate_rule(name: str, r: Rule) -> None:
-    """The rule checks of Prepare.cpp:328-437 with its messages: metadata,
-    node order, stencil indices and offsets, finite weights, the evaluation
-    node in every stencil, and exactness on 1, x, x^2 (5e-9 x max(1, |exact|))."""
-    n, s = r.n, r.q + 1
-    if not (n >= 3 and 2 <= r.q < n):
-        raise PrepareError(f"{name} FD-q metadata must satisfy node_count > q >= 2")
-    if not np.isfinite(r.period) or r.period <= 0:
-        raise PrepareError(f"{name} FD-q period must be finite and positive")
-    if r.periodic and r.q % 2:
-        raise PrepareError(f"{name} periodic FD-q degree must be even")
-    for row in range(n):
-        x = r.nodes[row]
-        if not np.isfinite(x):
-            raise PrepareError(f"{name} FD-q node {row} is not finite")
-        if row > 0 and not x > r.nodes[row - 1]:
-            raise PrepareError(f"{name} FD-q nodes must be strictly increasing")
-        cols, offs = r.indices[row], r.offsets[row]
-        for c, o in zip(cols, offs):
-            if not 0 <= c < n:
-                raise PrepareError(f"{name} FD-q row {row} contains out-of-range index {c}")
-            if (row + o) % n != c if r.periodic else row + o != c:
-                kind = "periodic" if r.periodic else "bounded"
-                raise PrepareError(f"{name} {kind} row {row} has inconsistent stencil index/offset")
-        if not np.all(np.isfinite(r.weights[:, row])):
-            raise PrepareError(f"{name} FD-q weight is not finite at row {row}")
-        if row not in cols:
-            raise PrepareError(f"{name} FD-q stencil row {row} does not contain its evaluation node")
-        xs = x + offs * (r.period / n) if r.periodic else r.nodes[cols]
-        for d in range(3):
-            for pw in range(3):
-                approx = float(np.sum(r.weights[d, row] * xs ** pw))
-                exact = [[1.0, x, x * x], [0.0, 1.0, 2.0 * x], [0.0, 0.0, 2.0]][d][pw]
-                if abs(approx - exact) > 5e-9 * max(1.0, abs(exact)):
-                    raise PrepareError(f"{name} FD-q order-{d} weights fail degree-{pw} "
-                                       f"polynomial check at row {row}")
 
 
 def load_prepared(path: str | Path, q_y: int | None = None, q_z: int | None = None,

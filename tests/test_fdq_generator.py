@@ -116,3 +116,65 @@ def test_unshipped_size_is_generated_on_demand():
     r = rules.load_rule(41, 10, False)
     assert time.perf_counter() - t < 5.0
     assert r.n == 41 and r.nodes[0] == -1.0 and r.nodes[-1] == 1.0
+
+
+# ---- HDF5 rule caches (fdq_nodes.py:458-627; test_fdq_nodes.py:143-219)
+
+def test_rule_cache_round_trip(tmp_path):
+    for nc, q, per in ((16, 4, False), (24, 6, True)):
+        g, le = rules.generate_rule(nc, q, per, with_log_error=True)
+        p = rules.save_rule(g, tmp_path / f"{rules.rule_name(nc, q, per)}.h5", le)
+        r = rules.load_rule_file(p)
+        assert (r.n, r.q, r.periodic) == (nc, q, per)
+        for a, b in ((r.nodes, g.nodes), (r.indices, g.indices), (r.offsets, g.offsets),
+                     (r.weights, g.weights)):
+            assert np.array_equal(a, b)
+        from tailor_gb300 import h5
+        with h5.File(p) as f:
+            assert f.attrs["schema_version"] == 2 and f.attrs["stencil_size"] == q + 1
+            assert np.array_equal(f["diagnostics/log_error"][...], le)
+
+
+def test_load_or_create_uses_and_rebuilds_the_cache(tmp_path):
+    from tailor_gb300 import h5
+    r1 = rules.load_or_create_rule(21, 6, False, tmp_path)
+    path = tmp_path / "N20_q6.h5"
+    assert path.is_file()
+    stamp = path.stat().st_mtime_ns
+    r2 = rules.load_or_create_rule(21, 6, False, tmp_path)  # cache hit
+    assert path.stat().st_mtime_ns == stamp and np.array_equal(r1.nodes, r2.nodes)
+    # a stale schema is rebuilt
+    w = h5.Writer()
+    with h5.File(path) as f:
+        w.attrs.update(f.attrs)
+        w.attrs["schema_version"] = 1
+    w.write(path)
+    with pytest.raises(rules.RuleError, match="unsupported FD-q schema version 1"):
+        rules.load_rule_file(path)
+    r3 = rules.load_or_create_rule(21, 6, False, tmp_path)
+    assert np.array_equal(r3.nodes, r1.nodes) and rules.load_rule_file(path).n == 21
+
+
+@pytest.mark.skipif(not Path("/root/reference/fdqNodes/N200_q10.h5").is_file(),
+                    reason="reference checkout not present")
+def test_reference_rule_caches_load():
+    ref = Path("/root/reference/fdqNodes")
+    r = rules.load_rule_file(ref / "N200_q10.h5")
+    g = rules.generate_rule(201, 10, False)
+    assert np.max(np.abs(r.nodes - g.nodes)) < 1e-14
+    p = rules.load_rule_file(ref / "N50_q6p.h5")
+    assert p.periodic and np.array_equal(p.weights, rules.generate_rule(50, 6, True).weights)
+    with pytest.raises(rules.RuleError, match="schema version 1"):
+        rules.load_rule_file(ref / "N100_q10.h5")  # the older cache schema
+
+
+def test_validate_rule_rejects_broken_rules():
+    g = rules.generate_rule(16, 4, False)
+    import dataclasses
+    bad = dataclasses.replace(g, weights=g.weights.copy())
+    bad.weights[1, 3, 2] += 1e-3
+    with pytest.raises(rules.RuleError, match="order-1 weights fail degree-0 polynomial check at row 3"):
+        rules.validate_rule("xi", bad)
+    bad = dataclasses.replace(g, nodes=g.nodes[::-1].copy())
+    with pytest.raises(rules.RuleError, match="strictly increasing"):
+        rules.validate_rule("xi", bad)
