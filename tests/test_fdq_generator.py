@@ -175,6 +175,8 @@ def test_validate_rule_rejects_broken_rules():
     bad.weights[1, 3, 2] += 1e-3
     with pytest.raises(rules.RuleError, match="order-1 weights fail degree-0 polynomial check at row 3"):
         rules.validate_rule("xi", bad)
-    bad = dataclasses.replace(g, nodes=g.nodes[::-1].copy())
-    with pytest.raises(rules.RuleError, match="strictly increasing"):
-        rules.validate_rule("xi", bad)
+    pr = rules.generate_rule(24, 6, True)
+    nodes = pr.nodes.copy()
+    nodes[5] = nodes[4]  # periodic moments use x + offset h, so row 5 fails on order first
+    with pytest.raises(rules.RuleError, match="eta FD-q nodes must be strictly increasing"):
+        rules.validate_rule("eta", dataclasses.replace(pr, nodes=nodes))
