@@ -71,6 +71,38 @@ def read_structured_sample(path: str | Path):
     return grid, base, ny, nz, period
 
 
+def quintic_tensor_spline(z_old, y_old, values, z_new, y_new):
+    """One real or complex field on a bounded tensor grid onto (z_new, y_new)
+    with the exact (s = 0) degree-5 tensor-product spline
+    (interpolate.py:31-79, SciPy's RectBivariateSpline as there)."""
+    from scipy.interpolate import RectBivariateSpline
+
+    z_old, y_old = np.asarray(z_old, dtype=np.float64), np.asarray(y_old, dtype=np.float64)
+    z_new, y_new = np.asarray(z_new, dtype=np.float64), np.asarray(y_new, dtype=np.float64)
+    field = np.asarray(values)
+    if z_old.ndim != 1 or y_old.ndim != 1:
+        raise PrepareError("source logical coordinates must be one-dimensional")
+    if z_new.ndim != 1 or y_new.ndim != 1:
+        raise PrepareError("target logical coordinates must be one-dimensional")
+    if z_old.size < 6 or y_old.size < 6:
+        raise PrepareError("quintic B-spline interpolation requires at least 6 nodes per axis")
+    if field.shape != (z_old.size, y_old.size):
+        raise PrepareError(f"values must have shape ({z_old.size}, {y_old.size}); "
+                           f"got {field.shape}")
+    if not all(np.all(np.isfinite(a)) for a in (z_old, y_old, z_new, y_new, field)):
+        raise PrepareError("spline coordinates and values must be finite")
+    if np.any(np.diff(z_old) <= 0.0) or np.any(np.diff(y_old) <= 0.0):
+        raise PrepareError("source logical coordinates must be strictly increasing")
+
+    def real(v):
+        sp = RectBivariateSpline(z_old, y_old, np.asarray(v, dtype=np.float64), kx=5, ky=5, s=0.0)
+        return np.asarray(sp(z_new, y_new, grid=True), dtype=np.float64)
+
+    if np.iscomplexobj(field):
+        return real(field.real) + 1j * real(field.imag)
+    return real(field)
+
+
 def periodic_quintic_spline(z_old, y_old, values, z_new, y_new, z_period=2.0,
                             value_translation=0.0):
     """One component [nz_old, ny_old] onto (z_new, y_new): quintic not-a-knot

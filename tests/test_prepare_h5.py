@@ -407,3 +407,26 @@ def test_malformed_prepared_file(tmp_path, mutate, message):
     _copy_with(good, bad, mutate)
     with pytest.raises(prepare.PrepareError, match=message):
         prepare.load_prepared(bad, 10, 6)
+
+
+def test_quintic_tensor_spline_polynomial_exactness():
+    """interpolate.py's bounded spline reproduces degree-5 tensor polynomials
+    (tests/Python/test_interpolate.py:23-47, 8e-14)."""
+    z_old = np.linspace(-1.0, 1.0, 8)
+    y_old = np.linspace(-1.0, 1.0, 9)
+    zg, yg = np.meshgrid(z_old, y_old, indexing="ij")
+
+    def f(z, y):
+        return (1 + 2j) * z ** 5 + (2 - 3j) * y ** 4 + z ** 2 * y ** 3
+
+    z_new = np.sort(np.linspace(-1.0, 1.0, 13) ** 3)
+    y_new = np.sort(np.linspace(-1.0, 1.0, 14) ** 3)
+    got = prepare.quintic_tensor_spline(z_old, y_old, f(zg, yg), z_new, y_new)
+    zt, yt = np.meshgrid(z_new, y_new, indexing="ij")
+    np.testing.assert_allclose(got, f(zt, yt), rtol=0.0, atol=8e-14)
+    with pytest.raises(prepare.PrepareError, match="at least 6"):
+        prepare.quintic_tensor_spline(np.linspace(-1, 1, 5), np.linspace(-1, 1, 6),
+                                      np.zeros((5, 6)), [-1.0, 1.0], [-1.0, 1.0])
+    with pytest.raises(prepare.PrepareError, match="values must have shape"):
+        prepare.quintic_tensor_spline(np.linspace(-1, 1, 6), np.linspace(-1, 1, 7),
+                                      np.zeros((7, 6)), [-1.0, 1.0], [-1.0, 1.0])
