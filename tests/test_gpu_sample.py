@@ -60,3 +60,57 @@ def test_shipped_sample(gpu_lib, precision, tmp_path):
         lam = f["spectrum/lambda"][...]
         assert np.array_equal(lam[:, 0] + 1j * lam[:, 1], sol.lam)
         assert f["modes/mode_000"][...].shape == (case.nodes, 5, 2)
+
+
+def test_launcher_end_to_end(gpu_lib, tmp_path, capsys):
+    """python -m tailor_gb300.run on the shipped case: the prepared file is
+    found, the GPU stages run, the reference driver's report is printed and
+    the result file is written in the reference's schema."""
+    from tailor_gb300 import run
+    case = sample_case()
+    data = tmp_path / "data"
+    output.write_prepared(data / "FD-q" / "fdq_sample_qy10_qz6.h5", case)
+    (data / "sample.h5").write_bytes(b"")  # the source is not read on a cache hit
+    cfg = """CaseTitle: Sample
+Folder: data
+File: sample.h5
+Q-Value:
+    y: 10
+    z: 6
+Stability:
+    Alpha:
+        Real: 2.43
+        Imag: 0.0
+EigenSolver:
+    SearchCenterOmega:
+        Real: 0.0
+        Imag: 0.0
+    NumberOfEigenvalues: 8
+    Tolerance: 1.0e-10
+    MaximumIterations: 1000
+Output:
+    File: data/results/sample_eigenmodes.h5
+Physics:
+    Targets:
+        ReynoldsNumber: 32500
+        MachNumber: 6.0
+    Gas:
+        PrandtlNumber: 0.72
+        GasConstant: 287.05
+        RatioOfSpecificHeats: 1.4
+    Transport:
+        ReferenceMu: 1.716E-5
+        ReferenceTemperature: 63.3340
+        SutherlandConstant: 110.4
+"""
+    (tmp_path / "config.yaml").write_text(cfg)
+    assert run.main(["-c", str(tmp_path / "config.yaml")]) == 0
+    text = capsys.readouterr().out
+    assert "FD-q cache hit" in text and "Prepared case 'Sample'" in text
+    assert "  Ny x Nz: 201 x 50" in text and "eigensolver: requested=8, converged=" in text
+    ref = golden_eigs()
+    with h5.File(data / "results" / "sample_eigenmodes.h5") as f:
+        assert f.attrs["case"] == "Sample" and f.attrs["converged_modes"] >= 8
+        lam = f["spectrum/lambda"][...]
+        for l in lam[:, 0] + 1j * lam[:, 1]:
+            assert np.min(np.abs(ref - l)) / abs(l) <= 1e-8

@@ -430,3 +430,37 @@ def test_quintic_tensor_spline_polynomial_exactness():
     with pytest.raises(prepare.PrepareError, match="values must have shape"):
         prepare.quintic_tensor_spline(np.linspace(-1, 1, 6), np.linspace(-1, 1, 7),
                                       np.zeros((7, 6)), [-1.0, 1.0], [-1.0, 1.0])
+
+
+def test_stage_report_format(tmp_path):
+    """The launcher prints the reference driver's report (Process.cpp:62-146),
+    in the lines its tests parse (test_metrics.py:167-184)."""
+    from tailor_gb300 import run
+    p = tmp_path / "config.yaml"
+    p.write_text(CONFIG)
+    cfg = config.load_config(p)
+    case = make_case(24, 16, physics=cfg.physics)
+    stages = {"metrics": {"min_jacobian": 0.5, "max_jacobian": 2.25, "max_grid_imaginary": 0.0,
+                          "norms": [float(i) for i in range(10)]},
+              "derivatives": {"max_baseflow_imaginary": 0.0,
+                              "norms": [0.1 * i for i in range(25)]},
+              "operator": {"rows": 1920, "columns": 1920, "block_size": 5,
+                           "mass_used_blocks": 384.0, "mass_allocated_blocks": 384.0,
+                           "spatial_used_blocks": 29568.0, "spatial_allocated_blocks": 29568.0,
+                           "mass_frobenius_norm": 12.5, "spatial_frobenius_norm": 1e4},
+              "bc": {"wall_nodes": 16, "farfield_nodes": 16, "incoming_modes": 16,
+                     "neutral_modes": 48, "min_incoming_per_node": 1, "max_incoming_per_node": 1,
+                     "max_characteristic_imaginary": 0.0, "max_eigenvector_condition": 3.5,
+                     "eigen_frobenius_norm": 1e4, "eigen_mass_frobenius_norm": 12.0}}
+    text = run.report(cfg, case, stages).splitlines()
+    assert text[0] == "Prepared case 'Sample'"
+    assert "  Ny x Nz: 24 x 16" in text
+    assert "  Jacobian range: [0.5, 2.25]" in text
+    assert "  metric norm eta_yz: 9" in text
+    assert "  base-flow derivative norm dyz: 2 2.1 2.2 2.3 2.4" in text
+    assert "  FD-q degrees: y=10, z=6; DMDA stencil width: 10" in text
+    assert "  far-field incoming modes=16 (per node 1..1), neutral modes=48" in text
+    d = {"requested": 8, "converged": 8, "iterations": 5, "target_re": 0.0, "target_im": -0.0,
+         "max_relative_error": 3e-11}
+    assert run.solve_report(d, "x.h5", 8).splitlines()[0] == \
+        "  eigensolver: requested=8, converged=8, iterations=5"
