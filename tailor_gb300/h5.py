@@ -30,6 +30,23 @@ class H5Error(ValueError):
     pass
 
 
+def _guard(fn):
+    """Report a damaged or truncated file as H5Error, never as an index or
+    decoding error from deep inside the parser."""
+    def wrapped(*a, **k):
+        try:
+            return fn(*a, **k)
+        except H5Error:
+            raise
+        except KeyError:
+            raise
+        except (IndexError, ValueError, OverflowError, RecursionError, UnicodeDecodeError,
+                TypeError, MemoryError) as e:
+            raise H5Error(f"damaged or truncated HDF5 file ({type(e).__name__}: {e})") from e
+    wrapped.__name__, wrapped.__doc__ = fn.__name__, fn.__doc__
+    return wrapped
+
+
 class _Reader:
     def __init__(self, data: bytes):
         self.d = data
@@ -265,6 +282,8 @@ class Dataset:
                 a = int.from_bytes(b[2:10], "little")
                 if a == _UNDEF:
                     return bytes(nbytes)
+                if r.addr(a) + nbytes > len(r.d):
+                    raise H5Error("dataset extends past the end of the file")
                 return r.d[r.addr(a):r.addr(a) + nbytes]
             if cls == 2:  # chunked
                 rank = b[2] - 1
@@ -285,6 +304,8 @@ class Dataset:
 
     def _chunked(self, bt: int, cdims, shape, nbytes: int) -> bytes:
         r, es = self._r, self._type.size
+        if nbytes > 64 * len(r.d) + (1 << 20):
+            raise H5Error("chunked dataset far larger than the file")
         rank = len(cdims)
         out = np.zeros(nbytes, dtype=np.uint8)
         view = out.reshape(tuple(shape) + (es,)) if shape else out
@@ -314,6 +335,7 @@ class Dataset:
         walk(bt)
         return out.tobytes()
 
+    @_guard
     def __getitem__(self, key):
         a = _decode(self._r, self._type, self.shape or (), self._raw())
         return a if key is Ellipsis or key == () else a[key]
@@ -354,6 +376,7 @@ class Group:
     def keys(self):
         return sorted(self._links)
 
+    @_guard
     def __getitem__(self, path: str):
         node = self
         for part in [x for x in path.split("/") if x]:
@@ -367,6 +390,7 @@ class Group:
 
 
 class File(Group):
+    @_guard
     def __init__(self, path: str | Path):
         r = _Reader(Path(path).read_bytes())
         oh = r.u(r.root_entry + 8, 8)

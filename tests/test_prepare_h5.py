@@ -464,3 +464,25 @@ def test_stage_report_format(tmp_path):
          "max_relative_error": 3e-11}
     assert run.solve_report(d, "x.h5", 8).splitlines()[0] == \
         "  eigensolver: requested=8, converged=8, iterations=5"
+
+
+def test_reader_reports_damaged_files(tmp_path):
+    """Truncated or overwritten files raise H5Error (or KeyError for a name
+    that is gone), never an internal parser error."""
+    case = make_case(24, 16, physics=Physics())
+    good = output.write_prepared(tmp_path / "good.h5", case).read_bytes()
+    rng = np.random.default_rng(1)
+    cuts = sorted(set([96, 200, 400, len(good) // 3, len(good) // 2, len(good) - 64]))
+    for i, cut in enumerate(cuts):
+        for kind in ("truncate", "scribble"):
+            data = bytearray(good[:cut]) if kind == "truncate" else bytearray(good)
+            if kind == "scribble":
+                data[cut:cut + 64] = rng.integers(0, 256, 64, dtype=np.uint8).tobytes()
+            p = tmp_path / f"bad_{i}_{kind}.h5"
+            p.write_bytes(bytes(data))
+            try:
+                with h5.File(p) as f:
+                    for name in ("grid", "baseflow", "discretization/y/weights/d1"):
+                        f[name][...]
+            except (h5.H5Error, KeyError):
+                pass
