@@ -208,6 +208,11 @@ class EigenSolution:
         return 1j * self.lam
 
 
+# statuses after which a mixed-form solve is repeated in FP64: not converged,
+# a timed-out bounded device wait, a singular (perturbed) factorisation
+_FALLBACK_STATUS = (13, 14, 15)
+
+
 class EigenSolver:
     """EigenSolver::solve (EigenSolver.hpp:48-72): shift-invert
     Krylov-Schur on (A_bc, B_bc) with lambda target Im w - i Re w."""
@@ -220,7 +225,32 @@ class EigenSolver:
               start: np.ndarray | None = None, modes: bool = False,
               cuda_core_schur: bool = False, persistent_solve: bool = False,
               solve_block: int = 0, refinement: str = "ir",
-              panel_width: int = 0, cluster_panel: int = 0) -> EigenSolution:
+              panel_width: int = 0, cluster_panel: int = 0,
+              fallback: bool = True) -> EigenSolution:
+        """With fallback, a mixed-form solve (precision 1) that fails to
+        converge (or hits a singular pivot or a timed-out device wait) is
+        repeated in the plain FP64 form; diag["fallback"] is 1 then."""
+        kw = dict(nev=nev, ncv=ncv, tol=tol, max_it=max_it, sigma=sigma, start=start,
+                  modes=modes, cuda_core_schur=cuda_core_schur,
+                  persistent_solve=persistent_solve, solve_block=solve_block,
+                  refinement=refinement, panel_width=panel_width, cluster_panel=cluster_panel)
+        if precision == 1 and fallback:
+            try:
+                sol = self._solve(precision=1, **kw)
+            except TailorError as e:
+                if e.status not in _FALLBACK_STATUS:
+                    raise
+                sol = self._solve(precision=0, **kw)
+                sol.diag["fallback"] = 1
+                return sol
+        else:
+            sol = self._solve(precision=precision, **kw)
+        sol.diag["fallback"] = 0
+        return sol
+
+    def _solve(self, nev, ncv, tol, max_it, precision, sigma, start, modes, cuda_core_schur,
+               persistent_solve, solve_block, refinement, panel_width,
+               cluster_panel) -> EigenSolution:
         ph = self.p.case.physics
         k = nev or ph.nev
         opts = L.SolveOpts(nev, ncv, tol, max_it, precision,
@@ -311,10 +341,13 @@ class SweepResult:
 
 def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
           autotune: bool = True, tol: float = 0.0, ncv: int = 0, max_it: int = 0,
-          starts=None, device: int = 0, raise_on_error: bool = True) -> SweepResult:
+          starts=None, device: int = 0, raise_on_error: bool = True,
+          fallback: bool = True) -> SweepResult:
     """Batched alpha-sweep (tlr_sweep): points are (class index, alpha) or
     (class index, alpha, Re); each class is a Case (grid, base flow,
-    physics) whose alpha (and Re when given) is overridden."""
+    physics) whose alpha (and Re when given) is overridden.  With fallback,
+    points that fail in the mixed form are solved again, one at a time, in
+    the plain FP64 form (diag["fallback_points"] counts them)."""
     lib = L.load()
     keep = []
     holder = Problem.__new__(Problem)  # reuse the rule marshalling
@@ -351,17 +384,63 @@ def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
     d = L.SweepDiag()
     rc = lib.tlr_sweep(gcs, len(cases), pts, npts, ctypes.byref(opts), _ptr(lam), _ptr(res),
                        st.ctypes.data, pd, ctypes.byref(d))
+    message = lib.tlr_last_error(None).decode() if rc else ""
+    point_diag = [_diag_dict(pd[i]) for i in range(npts)]
+    fallbacks = 0
+    failed = np.flatnonzero(st[:npts]) if rc else []
+    if fallback and precision == 1 and len(failed):
+        fallbacks = _fallback_points(cases, points, failed, k, ncv, tol, max_it, starts,
+                                     device, lam, res, st, point_diag)
+        if not np.any(st[:npts]):  # every failed point recovered in FP64
+            rc = 0
     if rc and raise_on_error:
-        raise TailorError(rc, lib.tlr_last_error(None).decode())
+        raise TailorError(rc, message)
     nc = len(cases)
     diag = {"wall_ms": d.wall_ms, "points": d.points, "failed": d.failed,
             "workers": d.workers, "converged_pairs": d.converged_pairs,
             "cuda_core_schur": list(d.cuda_core_schur[:nc]),
             "solve_block": list(d.solve_block[:nc]),
             "tune_factor_ms": [list(d.tune_factor_ms[c]) for c in range(nc)],
-            "tune_trisolve_ms": [list(d.tune_trisolve_ms[c]) for c in range(nc)]}
+            "tune_trisolve_ms": [list(d.tune_trisolve_ms[c]) for c in range(nc)],
+            "fallback_points": fallbacks}
     return SweepResult(lam[:npts, :, 0] + 1j * lam[:npts, :, 1], res[:npts], st[:npts], diag,
-                       [_diag_dict(pd[i]) for i in range(npts)])
+                       point_diag)
+
+
+def _fallback_points(cases, points, failed, k, ncv, tol, max_it, starts, device, lam, res, st,
+                     point_diag) -> int:
+    """Solve the failed sweep points again in FP64, one at a time, on one
+    context per grid class (copies of the classes, so the callers' cases are
+    not modified); fills lam / res / st / point_diag in place."""
+    import dataclasses
+    probs, done = {}, 0
+    try:
+        for i in failed:
+            c, a = int(points[i][0]), complex(points[i][1])
+            re_ov = float(points[i][2]) if len(points[i]) > 2 else 0.0
+            if c not in probs:
+                probs[c] = Problem(dataclasses.replace(cases[c]), device=device)
+            p = probs[c]
+            p.set_physics(dataclasses.replace(cases[c].physics, alpha=a,
+                                              reynolds=re_ov or cases[c].physics.reynolds))
+            try:
+                run_pipeline(p)
+                sol = EigenSolver(p).solve(nev=k, ncv=ncv, tol=tol, max_it=max_it, precision=0,
+                                           start=None if starts is None else starts[i])
+            except TailorError:
+                continue
+            n = len(sol.lam)
+            lam[i] = 0.0
+            lam[i, :n, 0], lam[i, :n, 1] = sol.lam.real, sol.lam.imag
+            res[i] = -1.0
+            res[i, :n] = sol.residual
+            st[i] = 0
+            point_diag[i] = dict(sol.diag, fallback=1)
+            done += 1
+    finally:
+        for p in probs.values():
+            p.close()
+    return done
 
 
 def lns_points(case_or_physics, q: np.ndarray, qy: int = 10, qz: int = 6):

@@ -221,7 +221,7 @@ def learned_solve(problem: api.Problem, proposal: Proposal, nev: int, precision=
     stats = {"sigma": sigma}
     try:
         sol = api.EigenSolver(problem).solve(nev=nev + extra, precision=precision, sigma=sigma,
-                                             start=start)
+                                             start=start, fallback=False)
     except api.TailorError:
         sol = None
     if sol is not None and len(sol.lam) == nev + extra:

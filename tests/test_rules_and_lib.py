@@ -104,3 +104,53 @@ def test_pencil_argument_checks_without_gpu():
         api.PencilProblem(A, B)
     with pytest.raises(ValueError, match="square"):
         api.PencilProblem(np.eye(3), np.eye(4))
+
+
+def test_mixed_solve_falls_back_to_fp64_without_gpu():
+    """EigenSolver.solve repeats a failed mixed-form solve in FP64 (a stand-in
+    library reports "not converged" for precision 1)."""
+    from types import SimpleNamespace
+    from tailor_gb300 import api
+    from tailor_gb300.case import Physics
+
+    class FakeLib:
+        def __init__(self, fail_status):
+            self.calls, self.fail_status = [], fail_status
+
+        def tlr_solve(self, ctx, opts, lam, res, vec, diag):
+            prec = opts._obj.precision
+            self.calls.append(prec)
+            if prec == 1:
+                return self.fail_status
+            diag._obj.converged = 2
+            diag._obj.requested = 2
+            return 0
+
+        def tlr_last_error(self, ctx):
+            return b"Krylov-Schur failed to converge"
+
+    for status, falls_back in ((13, True), (1, False)):
+        p = api.Problem.__new__(api.Problem)
+        p.lib, p.ctx, p._keep = FakeLib(status), None, []
+        p.case = SimpleNamespace(physics=Physics(nev=2), nodes=2)
+        if falls_back:
+            sol = api.EigenSolver(p).solve(precision=1)
+            assert p.lib.calls == [1, 0] and sol.diag["fallback"] == 1
+        else:  # an argument error is not retried
+            with pytest.raises(api.TailorError):
+                api.EigenSolver(p).solve(precision=1)
+            assert p.lib.calls == [1]
+    p = api.Problem.__new__(api.Problem)
+    p.lib, p.ctx, p._keep = FakeLib(13), None, []
+    p.case = SimpleNamespace(physics=Physics(nev=2), nodes=2)
+    with pytest.raises(api.TailorError):
+        api.EigenSolver(p).solve(precision=1, fallback=False)
+
+
+def test_sweep_argument_errors_are_not_hidden_by_the_fallback():
+    """An argument error of tlr_sweep (no point solved) still raises."""
+    from tailor_gb300 import api
+    from tailor_gb300.case import make_case
+    tb.build()
+    with pytest.raises(api.TailorError, match="invalid grid class"):
+        api.sweep([make_case(24, 16)], [(0, 1.0), (5, 2.0)], nev=6)
