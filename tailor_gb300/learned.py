@@ -188,6 +188,34 @@ class Proposal:
         hist = mlp.train((X - xm) / xs, (Y - ym) / ys, epochs=epochs, batch=batch, lr=lr)
         return cls(mlp, xm, xs, ym, ys, basis, target, nl, hist)
 
+    def save(self, path) -> None:
+        """Weights, normalisation, POD basis and target in one .npz, with a
+        SHA-256 of the parameters checked on load."""
+        import hashlib
+        params = self.mlp.get_params()
+        np.savez_compressed(path, params=params, shape=np.array(self.mlp.shape),
+                            x_mean=self.x_mean, x_std=self.x_std, y_mean=self.y_mean,
+                            y_std=self.y_std, basis=self.basis,
+                            target=np.array([self.target.real, self.target.imag]),
+                            n_lam=np.array(self.n_lam), history=self.history,
+                            sha256=np.array(hashlib.sha256(params.tobytes()).hexdigest()))
+
+    @classmethod
+    def load(cls, path) -> "Proposal":
+        import hashlib
+        z = np.load(path)
+        params = np.asarray(z["params"], dtype=np.float32)
+        if hashlib.sha256(params.tobytes()).hexdigest() != str(z["sha256"]):
+            raise ValueError(f"{path}: the stored parameters do not match their digest")
+        n_in, width, depth, n_out = (int(v) for v in z["shape"])
+        mlp = MLP(n_in, width, depth, n_out)
+        if mlp.n_params != params.size:
+            raise ValueError(f"{path}: {params.size} parameters for a network of {mlp.n_params}")
+        mlp.set_params(params)
+        t = z["target"]
+        return cls(mlp, z["x_mean"], z["x_std"], z["y_mean"], z["y_std"], z["basis"],
+                   complex(t[0], t[1]), int(z["n_lam"]), z["history"])
+
     def predict(self, points, bf16=True):
         X = np.array([features(*p) for p in points])
         Y = self.mlp.forward((X - self.x_mean) / self.x_std, bf16=bf16) * self.y_std + self.y_mean

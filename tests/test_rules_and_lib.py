@@ -154,3 +154,35 @@ def test_sweep_argument_errors_are_not_hidden_by_the_fallback():
     tb.build()
     with pytest.raises(api.TailorError, match="invalid grid class"):
         api.sweep([make_case(24, 16)], [(0, 1.0), (5, 2.0)], nev=6)
+
+
+def test_proposal_save_load_without_gpu(tmp_path, monkeypatch):
+    """Proposal.save / load round trip (a stand-in network keeps it on the CPU);
+    a tampered parameter file is rejected by its digest."""
+    from tailor_gb300 import learned
+
+    class FakeMLP:
+        def __init__(self, n_in=3, width=8, depth=2, n_out=4, seed=1):
+            self.shape = (n_in, width, depth, n_out)
+            self.n_params = 10
+            self.p = np.arange(10, dtype=np.float32) * seed
+
+        def get_params(self):
+            return self.p.copy()
+
+        def set_params(self, p):
+            self.p = np.asarray(p, dtype=np.float32).copy()
+
+    monkeypatch.setattr(learned, "MLP", FakeMLP)
+    prop = learned.Proposal(FakeMLP(seed=3), np.ones(3), np.ones(3), np.zeros(4), np.ones(4),
+                            np.eye(6, 2, dtype=complex), 0.01 - 0.3j, 2, np.array([1.0, 0.5]))
+    prop.save(tmp_path / "p.npz")
+    back = learned.Proposal.load(tmp_path / "p.npz")
+    assert np.array_equal(back.mlp.p, prop.mlp.p) and back.mlp.shape == prop.mlp.shape
+    assert back.target == prop.target and back.n_lam == 2
+    assert np.array_equal(back.basis, prop.basis) and np.array_equal(back.history, prop.history)
+    z = dict(np.load(tmp_path / "p.npz"))
+    z["params"] = z["params"] + 1
+    np.savez(tmp_path / "bad.npz", **z)
+    with pytest.raises(ValueError, match="digest"):
+        learned.Proposal.load(tmp_path / "bad.npz")
