@@ -1,6 +1,7 @@
 """Shipped FD-q rules (polynomial exactness, like Prepare.cpp:328-437's
 moment checks) and the C ABI library surface (loads, exports every
 function declared in include/tailor_gb300.h) -- no GPU needed."""
+import os
 import re
 from pathlib import Path
 
@@ -186,3 +187,39 @@ def test_proposal_save_load_without_gpu(tmp_path, monkeypatch):
     np.savez(tmp_path / "bad.npz", **z)
     with pytest.raises(ValueError, match="digest"):
         learned.Proposal.load(tmp_path / "bad.npz")
+
+
+def test_header_is_c11_and_the_library_links_from_c(tmp_path):
+    """include/tailor_gb300.h compiles as strict C11 and a plain C program
+    linked against libtailor_gb300.so calls it (here the host FD-q generator,
+    which needs no GPU) -- what a cgo / FFI binding of the path relies on."""
+    import shutil
+    import subprocess
+    lib = tb.build()
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "t.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include "tailor_gb300.h"
+int main(void) {
+  double nodes[11], w[3 * 11 * 5], le[11];
+  int idx[11 * 5], off[11 * 5];
+  int rc = tlr_fdq_rule(11, 4, 0, 2.0, nodes, idx, off, w, le);
+  if (rc) return rc;
+  rc = tlr_fdq_rule(2, 4, 0, 2.0, nodes, idx, off, w, NULL);
+  printf("%s|%s|%.17g\n", tlr_status_string(rc), tlr_last_error(NULL), nodes[0]);
+  return 0;
+}
+''')
+    exe = tmp_path / "t"
+    cuda_lib = Path(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc").resolve().parents[1] / "lib64"
+    subprocess.run([gcc, "-std=c11", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
+                    str(src), "-L", str(lib.parent), "-ltailor_gb300", "-o", str(exe)], check=True)
+    env = dict(os.environ, LD_LIBRARY_PATH=f"{lib.parent}:{cuda_lib}:" +
+               os.environ.get("LD_LIBRARY_PATH", ""))
+    out = subprocess.run([str(exe)], capture_output=True, text=True, env=env, check=True).stdout
+    status, message, x0 = out.strip().split("|")
+    assert status == "invalid argument" and "N must be at least 2" in message
+    assert float(x0) == -1.0
