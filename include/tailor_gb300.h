@@ -355,7 +355,8 @@ int tlr_schur_update_c64(const float *front, int m, int p, int k0, int w, unsign
  * form), tlr_spmv and tlr_copy_out of A and B, tlr_set_alpha (a new search
  * centre) and tlr_set_physics; the grid stages return TLR_ERR_WRONGSTATE.
  * Modes are returned as 5 * ceil(n / 5) complex entries (the first n are
- * the eigenvector). */
+ * the eigenvector).  1 <= n <= 5000 (TLR_ERR_SIZE otherwise): the pencil
+ * is stored densely. */
 int tlr_pencil_create(const tlr_recipe *recipe, int n, const double *A, const double *B,
                       int device, tlr_ctx **out);
 

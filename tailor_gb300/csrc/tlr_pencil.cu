@@ -45,8 +45,8 @@ extern "C" int tlr_pencil_create(const tlr_recipe *recipe, int n, const double *
     return TLR_ERR_ARG;
   }
   *out = nullptr;
-  if (n < 1 || n > 20000) {
-    set_global_error("the pencil order must be between 1 and 20000");
+  if (n < 1 || n > 5000) {
+    set_global_error("the pencil order must be between 1 and 5000");
     return TLR_ERR_SIZE;
   }
   const int nb = (n + 4) / 5, N = 5 * nb;
