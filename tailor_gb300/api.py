@@ -16,7 +16,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib as L
-from .case import Case, rebuild_baseflow, target_lambda
+from .case import Case, rebuild_baseflow
 
 TLR_MAT_M, TLR_MAT_L, TLR_MAT_A, TLR_MAT_B = 0, 1, 2, 3
 (OUT_METRICS, OUT_DERIVS, OUT_ROW_PTR, OUT_COL, OUT_M, OUT_L, OUT_A,
