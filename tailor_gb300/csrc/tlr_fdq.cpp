@@ -13,7 +13,9 @@
 // Jacobian (fdq_nodes.py:152-181).  The system is square (N parameters,
 // N adjacent differences), so here every order is a damped Newton solve
 // with the exact Jacobian: at an extremum x* of E the stationarity
-// sum_j 1 / (x* - s_j) = 0 makes d log|E(x*)| / d s_k = -1 / (x* - s_k).
+// sum_j 1 / (x* - s_j) = 0 makes d log|E(x*)| / d s_k = -1 / (x* - s_k),
+// and the Jacobian factors into a banded matrix times the (explicitly
+// invertible) derivative of the softmax parameterisation.
 // The result is symmetrised and checked as in fdq_nodes.py:184-216.
 //
 // Weights for derivative orders 0..2 come from Fornberg's recursion
@@ -23,8 +25,8 @@
 // (fdq_nodes.py:307-353).  Every rule passes the reference's metadata and
 // polynomial-moment checks (fdq_nodes.py:356-455) before it is returned.
 //
-// Pure host code: the node solve is a sequence of small dense Newton
-// steps (N <= a few hundred) that no device launch would speed up.
+// Pure host code: the node solve is a sequence of banded Newton steps,
+// O(N q^2) each, that no device launch would speed up.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -159,55 +161,76 @@ double norm_inf(const Vec &v) {
   return s;
 }
 
-// Exact Jacobian of the adjacent log-error differences in theta.
-// d aux_i / d theta_m = 2 gap_m ([m <= i] - cum_i);
-// d logerr_i / d aux_k = -1 / (node_i - aux_k) for k in node i's stencil.
-Vec jacobian(const Aux &a, const EqualError &d, int o) {
+// Newton step of the adjacent log-error differences r in theta, J step = -r,
+// with J factored as J = M A:
+//   M (N x N, banded): M(i, k) = dE(i+1, k) - dE(i, k), where
+//     dE(i, k) = d logerr_i / d aux_k = -1 / (node_i - aux_k) for k in node
+//     i's stencil (the other entries are zero);
+//   A (N x N): d aux_i / d theta_m = 2 gap_m ([m <= i] - cum_i).
+// M u = -r is solved by banded Gaussian elimination with partial pivoting;
+// A step = u has the closed form below (y_m = gap_m step_m, S its prefix
+// sums, T = S_{N-1}: u_i / 2 = S_i - cum_i T), so a step costs O(N o^2)
+// instead of the O(N^3) of a dense Jacobian.
+bool newton_step(const Aux &a, const EqualError &d, int o, const Vec &r, Vec &step) {
   const int n = (int)a.x.size();
-  Vec rows((size_t)(n + 1) * n, 0.0);  // d logerr / d theta
-  for (int i = 0; i <= n; ++i) {
-    double *row = &rows[(size_t)i * n];
+  // rows of M as [lo, lo + width) windows of a dense n x n store
+  Vec M((size_t)n * n, 0.0);
+  std::vector<int> lo(n), hi(n);
+  for (int i = 0; i < n; ++i) {
+    lo[i] = std::min(d.start[i], d.start[i + 1]);
+    hi[i] = std::max(d.start[i], d.start[i + 1]) + o;  // exclusive
+    double *row = &M[(size_t)i * n];
     for (int j = 0; j < o; ++j) {
-      const int k = d.start[i] + j;
-      const double w = -1.0 / (d.nodes[i] - a.x[k]);
-      const double c = 2.0 * w;
-      for (int m = 0; m < n; ++m) row[m] += c * a.gap[m] * ((m <= k ? 1.0 : 0.0) - a.cum[k]);
+      const int k1 = d.start[i + 1] + j, k0 = d.start[i] + j;
+      row[k1] += -1.0 / (d.nodes[i + 1] - a.x[k1]);
+      row[k0] -= -1.0 / (d.nodes[i] - a.x[k0]);
     }
   }
-  Vec J((size_t)n * n);
-  for (int i = 0; i < n; ++i)
-    for (int m = 0; m < n; ++m)
-      J[(size_t)i * n + m] = rows[(size_t)(i + 1) * n + m] - rows[(size_t)i * n + m];
-  return J;
-}
-
-// Solve J x = b in place (Gaussian elimination with partial pivoting).
-bool dense_solve(Vec &J, Vec &b) {
-  const int n = (int)b.size();
+  int kl = 0, ku = 0;  // band of M
+  for (int i = 0; i < n; ++i) {
+    kl = std::max(kl, i - lo[i]);
+    ku = std::max(ku, hi[i] - 1 - i);
+  }
+  const int kue = kl + ku;  // upper band after row interchanges
+  Vec u(n);
+  for (int i = 0; i < n; ++i) u[i] = -r[i];
   for (int c = 0; c < n; ++c) {
+    const int rend = std::min(n, c + kl + 1), cend = std::min(n, c + kue + 1);
     int p = c;
-    for (int r = c + 1; r < n; ++r)
-      if (std::fabs(J[(size_t)r * n + c]) > std::fabs(J[(size_t)p * n + c])) p = r;
-    if (!(std::fabs(J[(size_t)p * n + c]) > 0.0)) return false;
+    for (int rr = c + 1; rr < rend; ++rr)
+      if (std::fabs(M[(size_t)rr * n + c]) > std::fabs(M[(size_t)p * n + c])) p = rr;
+    if (!(std::fabs(M[(size_t)p * n + c]) > 0.0)) return false;
     if (p != c) {
-      for (int k = 0; k < n; ++k) std::swap(J[(size_t)p * n + k], J[(size_t)c * n + k]);
-      std::swap(b[p], b[c]);
+      for (int k = c; k < cend; ++k) std::swap(M[(size_t)p * n + k], M[(size_t)c * n + k]);
+      std::swap(u[p], u[c]);
     }
-    const double inv = 1.0 / J[(size_t)c * n + c];
-    for (int r = c + 1; r < n; ++r) {
-      const double f = J[(size_t)r * n + c] * inv;
+    const double inv = 1.0 / M[(size_t)c * n + c];
+    const double *mc = &M[(size_t)c * n];
+    for (int rr = c + 1; rr < rend; ++rr) {
+      double *mr = &M[(size_t)rr * n];
+      const double f = mr[c] * inv;
       if (f == 0.0) continue;
-      double *jr = &J[(size_t)r * n];
-      const double *jc = &J[(size_t)c * n];
-      for (int k = c + 1; k < n; ++k) jr[k] -= f * jc[k];
-      b[r] -= f * b[c];
+      for (int k = c + 1; k < cend; ++k) mr[k] -= f * mc[k];
+      u[rr] -= f * u[c];
     }
   }
-  for (int r = n - 1; r >= 0; --r) {
-    double s = b[r];
-    for (int k = r + 1; k < n; ++k) s -= J[(size_t)r * n + k] * b[k];
-    b[r] = s / J[(size_t)r * n + r];
+  for (int rr = n - 1; rr >= 0; --rr) {
+    double v = u[rr];
+    const int cend = std::min(n, rr + kue + 1);
+    for (int k = rr + 1; k < cend; ++k) v -= M[(size_t)rr * n + k] * u[k];
+    u[rr] = v / M[(size_t)rr * n + rr];
   }
+  // A step = u
+  const double T = u[n - 1] / (2.0 * (1.0 - a.cum[n - 1]));
+  double prev = 0.0;
+  step.assign(n, 0.0);
+  for (int i = 0; i < n; ++i) {
+    const double S = 0.5 * u[i] + a.cum[i] * T;
+    step[i] = (S - prev) / a.gap[i];
+    prev = S;
+  }
+  for (double v : step)
+    if (!std::isfinite(v)) return false;
   return true;
 }
 
@@ -221,10 +244,8 @@ double newton_order(Vec &theta, int o, int *iterations) {
   int it = 0;
   for (; it < 100; ++it) {
     if (norm_inf(r) < 1e-14) break;
-    Vec J = jacobian(a, d, o);
-    Vec step(n);
-    for (int i = 0; i < n; ++i) step[i] = -r[i];
-    if (!dense_solve(J, step)) break;
+    Vec step;
+    if (!newton_step(a, d, o, r, step)) break;
     const double r0 = norm2(r);
     double t = 1.0;
     bool better = false;
