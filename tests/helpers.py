@@ -55,7 +55,6 @@ def deterministic_vector(ny: int, nz: int) -> np.ndarray:
 def matrix_free_action(case, metrics, derivs, oracle_obj, x):
     """computeReferenceAction (test_global_operator.cpp:105-222): the
     stencil-by-stencil action of M_Gamma and L on x, independent of BSR."""
-    import ctypes
     ny, nz = case.ny, case.nz
     xi, eta = case.xi, case.eta
     sx, se = xi.q + 1, eta.q + 1

@@ -10,7 +10,7 @@ the arrays agree bit for bit; the test reports the bitwise fraction too.
 import numpy as np
 import pytest
 
-from oracle.oracle import boundary_rows, characteristics, to_complex_blocks
+from oracle.oracle import boundary_rows, to_complex_blocks
 from tailor_gb300 import api
 from tailor_gb300.case import make_case
 from tests.helpers import deterministic_vector, matrix_free_action

@@ -6,7 +6,6 @@ Fortran-generated gold at 5e-13 * max(1, |x|); the same comparison here
 pins the oracle (tests/golden/make_golden.py restates the generators).
 """
 import numpy as np
-import pytest
 
 from tailor_gb300.case import Physics
 from tests.helpers import read_lns_gold, read_transform_gold, rel_close, transform_inputs
