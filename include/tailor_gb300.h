@@ -27,7 +27,7 @@
  *   complex numbers are interleaved (re, im) doubles;
  *   BSR: row_ptr[nb+1], col_idx[nnzb] sorted ascending, values
  *   [nnzb][5][5] complex, row-major 5x5 blocks (the reference inserts
- *   row-oriented blocks, GlobalOperator.cpp:188).
+ *   row-oriented blocks, GlobalOperator.cpp:117).
  */
 #ifndef TAILOR_GB300_H
 #define TAILOR_GB300_H
@@ -182,7 +182,7 @@ int tlr_transform_points(int np, const double *alpha, const double *phys,
                          const double *metrics, double *fourier,
                          double *curvilinear, int *status);
 
-/* Shift-and-invert Krylov-Schur solve (EigenSolver.cpp:103-161). */
+/* Shift-and-invert Krylov-Schur solve (EigenSolver.cpp:31-89). */
 typedef struct {
   int nev;                /* 0: recipe value                                */
   int ncv;                /* 0: max(2 nev, nev + 15) (SLEPc default)        */

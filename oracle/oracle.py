@@ -17,7 +17,7 @@ Pieces:
   (``scipy.sparse.linalg.splu``) factors A - sigma B and ARPACK
   (``eigs``) iterates on (A - sigma B)^-1 B in the Euclidean inner product,
   lambda = sigma + 1/theta, nev nearest the target -- the arithmetic of
-  SLEPc's STSINVERT + PCLU (EigenSolver.cpp:103-161).
+  SLEPc's STSINVERT + PCLU (EigenSolver.cpp:61-67).
 """
 from __future__ import annotations
 

@@ -7,13 +7,13 @@
  *
  * It restates, in plain C with scalar loops and no fused multiply-add
  * (built with -ffp-contract=off), the reference algorithm of
- *   - Metrics.cpp:143-312 (first-order metrics, Jacobian checks)
- *   - Metrics.cpp:314-439 (second-order metrics by the chain rule)
- *   - BaseFlowDerivatives.cpp:162-362 (25 physical base-flow derivatives)
- *   - LNSCoefficients.cpp:260-589 (point validation, 11 physical blocks)
- *   - StreamwiseFourier.cpp:81-109 (d/dx = i alpha substitution)
- *   - CurvilinearTransform.cpp:244-310 (chain rule to xi/eta blocks)
- *   - GlobalOperator.cpp:232-449 (validation, exact pattern, insertion in
+ *   - Metrics.cpp:57-225 (first-order metrics, Jacobian checks)
+ *   - Metrics.cpp:227-352 (second-order metrics by the chain rule)
+ *   - BaseFlowDerivatives.cpp:51-251 (25 physical base-flow derivatives)
+ *   - LNSCoefficients.cpp:75-110, 173-404 (point validation, 11 physical blocks)
+ *   - StreamwiseFourier.cpp:16-44 (d/dx = i alpha substitution)
+ *   - CurvilinearTransform.cpp:35-101 (chain rule to xi/eta blocks)
+ *   - GlobalOperator.cpp:162-378 (validation, exact pattern, insertion in
  *     the reference's ADD order: centre K0, xi line, eta line, eta-major
  *     cross product)
  * Complex arithmetic is written out in real parts.  With the imaginary
@@ -73,7 +73,7 @@ enum {
 static int finite_d(double v) { return isfinite(v); }
 
 static int wrap_count(int index, int count) {
-  /* Metrics.cpp:115-119 */
+  /* periodicWrap, Metrics.cpp:28-32 */
   if (index >= 0) return index / count;
   return -((-index + count - 1) / count);
 }
@@ -94,7 +94,7 @@ int orc_metrics(int ny, int nz, double spanwise_period, const orc_rule *xi,
   double min_j = DBL_MAX, max_j = -DBL_MAX, max_im = 0.0;
   memset(metrics, 0, sizeof(double) * (size_t)nn * 10);
 
-  /* first order: Metrics.cpp:178-274 */
+  /* first order: Metrics.cpp:91-186 */
   for (int j = 0; j < nz; ++j) {
     for (int i = 0; i < ny; ++i) {
       double y_xi = 0.0, y_eta = 0.0, z_xi = 0.0, z_eta = 0.0;
@@ -163,7 +163,7 @@ int orc_metrics(int ny, int nz, double spanwise_period, const orc_rule *xi,
   if (fail[2]) return ORC_JACOBIAN;
   if (fail[3]) return ORC_COMPLEX;
 
-  /* second order: Metrics.cpp:342-424.  Reads the first-order values of
+  /* second order: Metrics.cpp:255-336.  Reads the first-order values of
    * all nodes (the reference's ghosted copy), writes components 4..9. */
   double *first = (double *)malloc(sizeof(double) * (size_t)nn * 4);
   for (int n = 0; n < nn; ++n)
@@ -461,7 +461,7 @@ int orc_lns_physical(const orc_physics *ph, const double *q, double *blk) {
   return 0;
 }
 
-/* Inviscid Gamma, Bc, Cc (LNSCoefficients.cpp:303-356). */
+/* Inviscid Gamma, Bc, Cc (LNSCoefficients.cpp:118-171). */
 int orc_lns_inviscid(const orc_physics *ph, const double *state, double *blk) {
   for (int k = 0; k < 5; ++k)
     if (!finite_d(state[k])) return 1;
@@ -486,8 +486,8 @@ int orc_lns_inviscid(const orc_physics *ph, const double *state, double *blk) {
   return 0;
 }
 
-/* Fourier + curvilinear transforms (StreamwiseFourier.cpp:81-109,
- * CurvilinearTransform.cpp:271-310).  phys: 11 real blocks; m: 10 metrics.
+/* Fourier + curvilinear transforms (StreamwiseFourier.cpp:16-44,
+ * CurvilinearTransform.cpp:62-101).  phys: 11 real blocks; m: 10 metrics.
  * out: 7 complex blocks Gamma, K0, Kxi, Keta, Vxixi, Vxieta, Vetaeta,
  * each [25][2].  Also writes the Fourier blocks (Gamma, K0, Ky, Kz, Vyy,
  * Vyz, Vzz) into four if non-null. */
@@ -552,8 +552,8 @@ int orc_transform(double ar, double ai, const double *phys, const double *m,
   return 0;
 }
 
-/* One node through GlobalOperator.cpp:193-216 (evaluateNode) with the
- * BiGlobal point of LNSCoefficients.cpp:260-295 (x derivatives zero). */
+/* One node through GlobalOperator.cpp:124-145 (evaluateNode) with the
+ * BiGlobal point of LNSCoefficients.cpp:75-110 (x derivatives zero). */
 static int evaluate_node(const orc_physics *ph, const double *bf /*[5][2]*/,
                          const double *dv /*[25]*/, const double *m,
                          double *curv /*[7][25][2]*/) {
@@ -596,7 +596,7 @@ static void eta_order(const orc_rule *eta, int j, int *order) {
   }
 }
 
-/* Column pattern of L (GlobalOperator.cpp:280-354); M is block diagonal. */
+/* Column pattern of L (GlobalOperator.cpp:209-283); M is block diagonal. */
 int orc_pattern(int ny, int nz, const orc_rule *xi, const orc_rule *eta,
                 int *row_ptr, int *col_idx) {
   const int sx = xi->q + 1, se = eta->q + 1, S = sx * se;
@@ -617,7 +617,7 @@ int orc_pattern(int ny, int nz, const orc_rule *xi, const orc_rule *eta,
   return 0;
 }
 
-/* Numeric assembly (GlobalOperator.cpp:356-449).  mass: [nn][25][2];
+/* Numeric assembly (GlobalOperator.cpp:285-378).  mass: [nn][25][2];
  * spatial: [nn*S][25][2] in the pattern order of orc_pattern. */
 int orc_assemble(int ny, int nz, const orc_rule *xi, const orc_rule *eta,
                  const orc_physics *ph, const double *baseflow,
@@ -627,7 +627,7 @@ int orc_assemble(int ny, int nz, const orc_rule *xi, const orc_rule *eta,
   const int nn = ny * nz;
   int order[64], rank[64];
   double curv[350];
-  /* validation pass (GlobalOperator.cpp:232-278) */
+  /* validation pass (GlobalOperator.cpp:162-207) */
   for (int n = 0; n < nn; ++n) {
     if (evaluate_node(ph, baseflow + (size_t)n * 10, derivs + (size_t)n * 25,
                       metrics + (size_t)n * 10, curv))

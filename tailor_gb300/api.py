@@ -320,7 +320,7 @@ def solve_pencil(A, B, omega: complex = 0j, nev: int = 2, tol: float = 1e-10,
                  max_it: int = 1000, precision: int = 0, modes: bool = True,
                  **kw) -> EigenSolution:
     """The nev eigenpairs of A x = lambda B x nearest lambda_s = Im(omega) -
-    i Re(omega) (EigenSolver.cpp:118-120), on the GPU."""
+    i Re(omega) (EigenSolver.cpp:46-48), on the GPU."""
     from .case import Physics
     with PencilProblem(A, B, Physics(omega=omega, nev=nev, tol=tol, max_it=max_it)) as p:
         sol = EigenSolver(p).solve(nev=nev, tol=tol, max_it=max_it, precision=precision,

@@ -107,5 +107,5 @@ def rebuild_baseflow(case: Case) -> np.ndarray:
 
 
 def target_lambda(omega: complex) -> complex:
-    """lambda_s = Im(omega) - i Re(omega)  (EigenSolver.cpp:118-120)."""
+    """lambda_s = Im(omega) - i Re(omega)  (EigenSolver.cpp:46-48)."""
     return complex(omega.imag, -omega.real)

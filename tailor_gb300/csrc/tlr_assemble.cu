@@ -1,7 +1,7 @@
 // tlr_assemble.cu -- BSR pattern, pointwise coefficients and the numeric
 // assembly of M_Gamma and L (K3).
 //
-// Reference: GlobalOperator.cpp:232-449.  The reference evaluates the
+// Reference: GlobalOperator.cpp:162-378.  The reference evaluates the
 // coefficient pipeline twice per node and makes 97 blocked insertions per
 // node; here one kernel evaluates each node's curvilinear blocks once into a
 // per-node SoA record (L2-resident), and a second kernel streams the block
@@ -35,7 +35,7 @@ __constant__ int c_vidx[25] = {-1, -1, -1, -1, -1, -1, 0,  -1, -1,
 
 __device__ inline bool finite(double v) { return isfinite(v); }
 
-// BSR column pattern (GlobalOperator.cpp:304-342): row n = j*ny + i holds
+// BSR column pattern (GlobalOperator.cpp:209-283): row n = j*ny + i holds
 // the tensor product of its eta and xi stencils, eta slots in ascending
 // wrapped index, xi slots ascending.
 __global__ void k_pattern(int ny, int nz, DevRule xi, DevRule eta,
@@ -91,7 +91,7 @@ struct CoefBody {
   }
 };
 
-// One thread per node: evaluateNode (GlobalOperator.cpp:193-216) into
+// One thread per node: evaluateNode (GlobalOperator.cpp:124-145) into
 // the SoA coefficient record; status on any invalid input or output.
 __global__ void __launch_bounds__(128)
     k_coefficients(CoefParams p, const double *__restrict__ base_c,

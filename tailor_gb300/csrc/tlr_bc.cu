@@ -137,7 +137,7 @@ __device__ void characteristics(const double *state, const double *m10,
     ch.ok = 6;  // SingularEigenvectors
     return;
   }
-  // Gamma (LNSCoefficients.cpp:326-331) is diag(1, rho, rho, rho, g44)
+  // Gamma (LNSCoefficients.cpp:141-146) is diag(1, rho, rho, rho, g44)
   // plus Gamma[4][0] = -Pe T; its inverse in closed form.
   const double g44 = rho * g2 - Pe * rho;
   if (!isfinite(g44) || fabs(g44) <= 100.0 * kEps) {

@@ -1,8 +1,8 @@
 // tlr_fields.cu -- curvilinear metrics and base-flow derivatives (K1, K2).
 //
 // Thread-per-node stencil kernels.  Every node's sums run over the same
-// slots in the same order as the reference (Metrics.cpp:178-274 and
-// 342-424, BaseFlowDerivatives.cpp:196-329), and this file is compiled with
+// slots in the same order as the reference (Metrics.cpp:91-186 and
+// 255-336, BaseFlowDerivatives.cpp:85-218), and this file is compiled with
 // --fmad=false, so each product and sum is rounded separately: the device
 // values equal a scalar CPU evaluation of the same expressions bit for bit.
 // Failure flags follow the reference's collective checks; diagnostics use
@@ -58,7 +58,7 @@ __device__ inline int wrap_index(int index, int count) {
   return r < 0 ? r + count : r;
 }
 
-// First-order metrics, Jacobian checks (Metrics.cpp:178-274).
+// First-order metrics, Jacobian checks (Metrics.cpp:91-224).
 __global__ void k_metrics_first(int ny, int nz, double span, DevRule xi,
                                 DevRule eta, const double *__restrict__ grid,
                                 double *__restrict__ met, int *status,
@@ -135,7 +135,7 @@ __global__ void k_metrics_first(int ny, int nz, double span, DevRule xi,
   }
 }
 
-// Second-order metrics by the chain rule (Metrics.cpp:342-424).
+// Second-order metrics by the chain rule (Metrics.cpp:255-336).
 __global__ void k_metrics_second(int ny, int nz, DevRule xi, DevRule eta,
                                  double *__restrict__ met, int *status) {
   const int nn = ny * nz;
@@ -176,7 +176,7 @@ __global__ void k_metrics_second(int ny, int nz, DevRule xi, DevRule eta,
 }
 
 // Complex base flow -> real SoA, with the node checks of
-// BaseFlowDerivatives.cpp:200-209 and the realness scan (339-340).
+// BaseFlowDerivatives.cpp:89-98 and the realness test (228-229).
 __global__ void k_baseflow_prep(int nn, const double *__restrict__ base_c,
                                 double *__restrict__ base, int *status,
                                 double *red) {
@@ -199,7 +199,7 @@ __global__ void k_baseflow_prep(int nn, const double *__restrict__ base_c,
   if ((threadIdx.x & 31) == 0) atomic_max_d(red + RD_BFIM, imax);
 }
 
-// 25 physical derivatives per node (BaseFlowDerivatives.cpp:211-324).
+// 25 physical derivatives per node (BaseFlowDerivatives.cpp:100-213).
 __global__ void k_derivatives(int ny, int nz, DevRule xi, DevRule eta,
                               const double *__restrict__ base,
                               const double *__restrict__ met,

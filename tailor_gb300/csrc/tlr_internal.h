@@ -24,7 +24,7 @@
 namespace tlr {
 
 // Coefficient record, one SoA plane per entry (CurvilinearLNSCoefficients,
-// CurvilinearTransform.hpp:170-188): K0, Kxi, Keta complex (re, im planes),
+// CurvilinearTransform.hpp:61-78): K0, Kxi, Keta complex (re, im planes),
 // Vxixi, Vxieta, Vetaeta and Gamma real.
 enum : int {
   CF_K0_RE = 0,

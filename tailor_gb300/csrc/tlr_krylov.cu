@@ -1,5 +1,5 @@
 // tlr_krylov.cu -- shift-and-invert Krylov-Schur eigen solve
-// (EigenSolver.cpp:103-161: EPS_GNHEP, EPSKRYLOVSCHUR, STSINVERT with a
+// (EigenSolver.cpp:50-72: EPS_GNHEP, EPSKRYLOVSCHUR, STSINVERT with a
 // single LU of A - sigma B, EPS_TARGET_MAGNITUDE, relative convergence,
 // EPSComputeError(EPS_ERROR_RELATIVE) for the reported residuals).
 //
@@ -487,7 +487,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   ncv = (int)std::min<long long>(ncv, n - 1);
   if (nev < 1 || nev >= ncv || !lambda || !residual)
     return fail(ctx, TLR_ERR_ARG, "invalid eigen-solver dimensions");
-  // lambda target = Im(omega) - i Re(omega)  (EigenSolver.cpp:118-120)
+  // lambda target = Im(omega) - i Re(omega)  (EigenSolver.cpp:46-48)
   const cd target(rcp.omega_im, -rcp.omega_re);
   const cd sigma = o.use_sigma ? cd(o.sigma_re, o.sigma_im) : target;
   const int prec = o.precision == 1 ? 1 : 0;

@@ -3,7 +3,7 @@
 //
 // phys_entry<RC>() returns the entry (RC / 5, RC % 5) of the eleven
 // physical blocks Gamma, A, B, C, D, Vxx, Vxy, Vxz, Vyy, Vyz, Vzz
-// (LNSCoefficients.cpp:445-584).  Every nonzero entry is the reference's
+// (LNSCoefficients.cpp:236-399).  Every nonzero entry is the reference's
 // expression with the same operator order, so with --fmad=false the value is
 // the reference's to the last bit.  Entries that are structurally zero in
 // the reference are zero here, and the masks below let the transforms drop
@@ -202,7 +202,7 @@ struct CurvEntry {  // Gamma, K0, Kxi, Keta complex; Vxixi, Vxieta, Vetaeta
   double G, K0r, K0i, Kxr, Kxi, Ker, Kei, Vxx, Vxe, Vee;
 };
 
-// StreamwiseFourier.cpp:88-103 for one entry.  ia = i*alpha, a2 = alpha^2.
+// StreamwiseFourier.cpp:27-37 for one entry.  ia = i*alpha, a2 = alpha^2.
 template <int RC>
 __device__ __forceinline__ FourierEntry fourier_entry(const Entry &p,
                                                       double ia_re,
@@ -239,7 +239,7 @@ __device__ __forceinline__ FourierEntry fourier_entry(const Entry &p,
   return o;
 }
 
-// CurvilinearTransform.cpp:278-304 for one entry.
+// CurvilinearTransform.cpp:71-94 for one entry.
 template <int RC>
 __device__ __forceinline__ CurvEntry curv_entry(const FourierEntry &f,
                                                 const Metric10 &m) {
@@ -292,8 +292,8 @@ namespace tlr {
 
 // General (dense) forms of the two transforms for arbitrary real physical
 // blocks, as exercised by the reference's transform fixtures
-// (test_lns_transforms.cpp:43-65): every term of StreamwiseFourier.cpp:93-102
-// and CurvilinearTransform.cpp:286-303 is kept.
+// (test_lns_transforms.cpp:43-65): every term of StreamwiseFourier.cpp:27-37
+// and CurvilinearTransform.cpp:75-94 is kept.
 __device__ __forceinline__ FourierEntry fourier_entry_full(const Entry &p,
                                                            double ia_re,
                                                            double ia_im,

@@ -2,7 +2,7 @@
 // (inputs -> depth x width SiLU hidden layers -> outputs) trained and
 // evaluated on the GPU by the kernels in this file.  No reference
 // counterpart: the reference always starts Krylov-Schur from SLEPc's
-// random vector at the configured target (EigenSolver.cpp:118-135).
+// random vector at the configured target (EigenSolver.cpp:46-72).
 //
 // Parameters are FP32, flat: for each layer l, W_l [out][in] row-major then
 // b_l [out].  Training: mean-squared error, full forward/backward per

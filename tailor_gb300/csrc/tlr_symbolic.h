@@ -1,7 +1,7 @@
 // tlr_symbolic.h -- nested-dissection ordering and multifrontal structure
 // of the shift-and-invert matrix K = A_bc - sigma B_bc.
 //
-// The reference hands K to PETSc's PCLU / MUMPS (EigenSolver.cpp:133-143),
+// The reference hands K to PETSc's PCLU / MUMPS (EigenSolver.cpp:61-71),
 // whose orderings come from graph partitioners.  Here the graph is the
 // structured (xi, eta) grid, so the separators are grid lines: a cut across
 // xi is as wide as the symmetric xi coupling reach (5 lines in the

@@ -2,7 +2,7 @@
 
 No reference counterpart: the reference always solves around the target
 lambda_s = Im(omega) - i Re(omega) from SLEPc's random start vector
-(EigenSolver.cpp:118-135).  Here an MLP, trained on eigenpairs the solver
+(EigenSolver.cpp:46-72).  Here an MLP, trained on eigenpairs the solver
 itself produced over (alpha, log10 Re, Mach), predicts
 
 * the nev eigenvalues nearest the target (8 complex numbers), and

@@ -244,7 +244,7 @@ def prepare_sample(path: str | Path, q_y: int = 10, q_z: int = 6,
 # ---- prepared schema-2 case files -----------------------------------------
 
 def _dataset(group, gpath: str, name: str, shape: tuple[int, ...]) -> np.ndarray:
-    """A rule dataset with the reference's messages (Prepare.cpp:74-110)."""
+    """A rule dataset with the reference's messages (Prepare.cpp:78-111)."""
     path = f"{gpath}/{name}"
     try:
         a = np.asarray(group[name][...])

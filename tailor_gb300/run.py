@@ -13,7 +13,7 @@ unless --prepare-only, the case runs through the GPU stages (metrics,
 derivatives, assembly, boundary rows, shift-and-invert Krylov-Schur) and
 the spectrum and phased modes are written in the reference's result
 schema.  The printed stage report is the reference driver's, line for line
-(Process.cpp:62-146).  --precision 1 selects the mixed form (complex64 factors,
+(Process.cpp:62-176).  --precision 1 selects the mixed form (complex64 factors,
 tensor-core Schur updates, FP64 refinement); the default is the FP64 form
 the reference runs.  Exit status 0 on success, 1 on a configuration or
 preparation error, 2 on a solver error.
@@ -61,7 +61,7 @@ def _g(x) -> str:
 
 
 def report(cfg: config.Config, case, stages: dict) -> str:
-    """The stage report of the reference's driver (Process.cpp:62-146), line
+    """The stage report of the reference's driver (Process.cpp:62-152), line
     for line, from the stage diagnostics of ``api.run_pipeline``: scripts that
     parse Tailor's output (Jacobian range, metric and derivative norms,
     operator and boundary statistics) read this one unchanged."""
@@ -105,7 +105,7 @@ def report(cfg: config.Config, case, stages: dict) -> str:
 
 
 def solve_report(d: dict, output_file, modes: int) -> str:
-    """The eigensolver lines of Process.cpp:131-146."""
+    """The eigensolver lines of Process.cpp:161-175."""
     return (f"  eigensolver: requested={d['requested']}, converged={d['converged']}, "
             f"iterations={d['iterations']}\n"
             f"  lambda target: {d['target_re']:.16g} {d['target_im']:+.16g}i; "

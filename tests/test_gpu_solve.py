@@ -2,7 +2,7 @@
 (SuperLU + ARPACK on the oracle's own A_bc, B_bc): every reported
 eigenvalue within |dlambda|/|lambda| <= 1e-8 of an oracle eigenvalue and
 with relative residual ||A x - lambda B x|| / (|lambda| ||x||) <= 1e-10
-(EigenSolver.cpp:149-154), for the FP64 drop-in form and for the mixed
+(EigenSolver.cpp:77-82), for the FP64 drop-in form and for the mixed
 form (complex64 factorisation + FP64 refinement)."""
 import numpy as np
 import pytest

@@ -433,7 +433,7 @@ def test_quintic_tensor_spline_polynomial_exactness():
 
 
 def test_stage_report_format(tmp_path):
-    """The launcher prints the reference driver's report (Process.cpp:62-146),
+    """The launcher prints the reference driver's report (Process.cpp:62-176),
     in the lines its tests parse (test_metrics.py:167-184)."""
     from tailor_gb300 import run
     p = tmp_path / "config.yaml"
