@@ -360,6 +360,36 @@ int tlr_schur_update_c64(const float *front, int m, int p, int k0, int w, unsign
 int tlr_pencil_create(const tlr_recipe *recipe, int n, const double *A, const double *B,
                       int device, tlr_ctx **out);
 
+/* Symbolic analysis on the host, no GPU needed: the nested-dissection
+ * ordering and the multifrontal structure that tlr_solve and tlr_sweep use
+ * for the grid of the rules xi (bounded, Ny nodes) and eta (periodic, Nz
+ * nodes).  The reference leaves this to MUMPS's analysis phase behind
+ * PCLU (EigenSolver.cpp:61-71); here it lets a caller size a
+ * factorisation (flops, factor and front-pool entries) before creating a
+ * context.  leaf_nodes: boxes of at most this many nodes become leaf
+ * fronts (0: the solver's 48).  ring_slack_percent: a box of the periodic
+ * ring is cut across xi instead of across the ring when that separator
+ * has at most this percentage of the ring cut's nodes (0: the solver's
+ * 100; 100..1000).  Optional outputs: node_rank[Ny*Nz] (elimination
+ * position of node j*Ny + i), node_front[Ny*Nz] (front that eliminates
+ * it), front_parent[front_capacity] (-1 for the root; fronts are numbered
+ * in postorder).  *info is filled first, so a call with front_parent NULL
+ * sizes the array; a front_capacity below info->fronts returns
+ * TLR_ERR_SIZE. */
+typedef struct {
+  int fronts;                /* fronts in the elimination tree               */
+  int levels;                /* tree height + 1: batched launches per sweep  */
+  int max_front_order;       /* largest front, scalar rows                   */
+  int max_pivots;            /* largest pivot block, scalar rows             */
+  double flops;              /* factorisation flops, 8 real per complex MAC  */
+  long long factor_elems;    /* stored L and U entries: sum p (p + 2 b)      */
+  long long pool_elems;      /* front pool entries: sum m^2                  */
+} tlr_symbolic_info;
+
+int tlr_symbolic_analyze(const tlr_rule *xi, const tlr_rule *eta, int leaf_nodes,
+                         int ring_slack_percent, tlr_symbolic_info *info, int *node_rank,
+                         int *node_front, int *front_parent, int front_capacity);
+
 /* FD-q rule generation on the host (src/Python/fdq_nodes.py:280-353,
  * calculate_fdq_rule and calculate_periodic_fdq_rule).  periodic = 0: the
  * equal-error nodes on [-1, 1] with node_count - 1 intervals (period is

@@ -122,6 +122,13 @@ class SweepDiag(ctypes.Structure):
                 ("tune_trisolve_ms", (ctypes.c_double * 2) * 16)]
 
 
+class SymbolicInfo(ctypes.Structure):
+    _fields_ = [("fronts", ctypes.c_int), ("levels", ctypes.c_int),
+                ("max_front_order", ctypes.c_int), ("max_pivots", ctypes.c_int),
+                ("flops", ctypes.c_double), ("factor_elems", ctypes.c_longlong),
+                ("pool_elems", ctypes.c_longlong)]
+
+
 # Exported symbols and their signatures (argtypes, restype).
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -149,6 +156,7 @@ SIGNATURES = {
     "tlr_wait_selftest": ([_I, ctypes.c_uint, _P], _I),
     "tlr_pencil_create": ([_P, _I, _P, _P, _I, _P], _I),
     "tlr_fdq_rule": ([_I, _I, _I, ctypes.c_double, _P, _P, _P, _P, _P], _I),
+    "tlr_symbolic_analyze": ([_P, _P, _I, _I, _P, _P, _P, _P, _I], _I),
     "tlr_frobenius_noalloc": ([_P, ctypes.c_size_t, _P, _P], _I),
     "tlr_mlp_create": ([_I, _I, _I, _I, ctypes.c_ulonglong, _P], _I),
     "tlr_mlp_destroy": ([_P], None),

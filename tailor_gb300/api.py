@@ -443,6 +443,34 @@ def _fallback_points(cases, points, failed, k, ncv, tol, max_it, starts, device,
     return done
 
 
+def symbolic_analysis(xi, eta, leaf_nodes: int = 0, ring_slack_percent: int = 0) -> dict:
+    """Host-only symbolic analysis (tlr_symbolic_analyze) of the grid of the
+    rules xi (bounded) and eta (periodic): the ordering and front tree the
+    solver factors, with its flop and storage counts.  Returns the info
+    fields plus node_rank, node_front [Ny*Nz] and front_parent [fronts]."""
+    lib = L.load()
+    holder = Problem.__new__(Problem)  # reuse the rule marshalling
+    holder._keep = []
+    rx, re_ = holder._rule(xi), holder._rule(eta)
+    info = L.SymbolicInfo()
+    nn = xi.n * eta.n
+    rank = np.zeros(nn, dtype=np.int32)
+    front = np.zeros(nn, dtype=np.int32)
+    args = (ctypes.byref(rx), ctypes.byref(re_), int(leaf_nodes), int(ring_slack_percent),
+            ctypes.byref(info))
+    st = lib.tlr_symbolic_analyze(*args, None, None, None, 0)
+    if st:
+        raise TailorError(st, lib.tlr_last_error(None).decode())
+    parent = np.zeros(max(info.fronts, 1), dtype=np.int32)
+    st = lib.tlr_symbolic_analyze(*args, rank.ctypes.data, front.ctypes.data,
+                                  parent.ctypes.data, info.fronts)
+    if st:
+        raise TailorError(st, lib.tlr_last_error(None).decode())
+    out = {name: getattr(info, name) for name, _ in L.SymbolicInfo._fields_}
+    out.update(node_rank=rank, node_front=front, front_parent=parent[:info.fronts])
+    return out
+
+
 def lns_points(case_or_physics, q: np.ndarray, qy: int = 10, qz: int = 6):
     """Pointwise LNS blocks on the GPU: q [np][10][5] -> [np][11][5][5]."""
     lib = L.load()

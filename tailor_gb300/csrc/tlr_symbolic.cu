@@ -1,8 +1,12 @@
 // tlr_symbolic.cu -- host-side nested dissection and front structures.
 #include <algorithm>
+#include <climits>
+#include <cstdio>
 #include <cstdlib>
 #include <numeric>
+#include <string>
 
+#include "../../include/tailor_gb300.h"
 #include "tlr_symbolic.h"
 
 namespace tlr {
@@ -15,7 +19,7 @@ struct Box {
 };
 
 struct Builder {
-  int ny, nz, re, leaf;
+  int ny, nz, re, leaf, slack;
   std::vector<int> lo, hi;   // symmetric xi reach per line
   std::vector<FrontInfo> &fronts;
 
@@ -56,7 +60,7 @@ struct Builder {
         w = std::max(w, 1);
         if (m + w < b.i1 - 1) {
           const long long s = (long long)w * b.jl;
-          if (best < 0 || s < best || (b.ring && kind == 1 && s <= best)) {
+          if (best < 0 || s < best || (b.ring && kind == 1 && s * 100 <= best * slack)) {
             best = s;
             kind = 3;
             mcut = m;
@@ -101,7 +105,7 @@ struct Builder {
 int build_symbolic(int ny, int nz, const std::vector<int> &xi_idx, int sx,
                    const std::vector<int> &eta_off, int se,
                    const std::vector<int> &row_ptr, const std::vector<int> &col,
-                   int leaf_nodes, Symbolic &out) {
+                   int leaf_nodes, Symbolic &out, int ring_slack_percent) {
   out = Symbolic{};
   out.ny = ny;
   out.nz = nz;
@@ -122,7 +126,7 @@ int build_symbolic(int ny, int nz, const std::vector<int> &xi_idx, int sx,
   for (int v : eta_off) re = std::max(re, std::abs(v));
   if (re < 1) return 1;
 
-  Builder b{ny, nz, re, std::max(leaf_nodes, 1), lo, hi, out.fronts};
+  Builder b{ny, nz, re, std::max(leaf_nodes, 1), ring_slack_percent, lo, hi, out.fronts};
   b.rec(Box{0, ny, 0, nz, true});
   auto &F = out.fronts;
   const int nf = (int)F.size();
@@ -229,4 +233,85 @@ int build_symbolic(int ny, int nz, const std::vector<int> &xi_idx, int sx,
   return 0;
 }
 
+void set_global_error(const std::string &msg);
+
 }  // namespace tlr
+
+extern "C" int tlr_symbolic_analyze(const tlr_rule *xi, const tlr_rule *eta, int leaf_nodes,
+                                    int ring_slack_percent, tlr_symbolic_info *info,
+                                    int *node_rank, int *node_front, int *front_parent,
+                                    int front_capacity) {
+  auto bad = [](int code, const char *msg) {
+    tlr::set_global_error(msg);
+    return code;
+  };
+  if (!xi || !eta || !info) return bad(TLR_ERR_ARG, "null argument");
+  if (!xi->stencil_indices || !eta->stencil_indices || !eta->stencil_offsets)
+    return bad(TLR_ERR_ARG, "FD-q rule arrays are missing");
+  if (xi->periodic || !eta->periodic)
+    return bad(TLR_ERR_ARG, "the xi rule must be bounded and the eta rule periodic");
+  const int ny = xi->node_count, nz = eta->node_count;
+  if (ny < 2 || nz < 2 || xi->q < 1 || eta->q < 1 || xi->q >= ny || eta->q >= nz)
+    return bad(TLR_ERR_SIZE, "FD-q node counts or degrees out of range");
+  if ((long long)ny * nz > INT_MAX / 128) return bad(TLR_ERR_SIZE, "grid too large");
+  if (leaf_nodes == 0) leaf_nodes = 48;
+  if (ring_slack_percent == 0) ring_slack_percent = 100;
+  if (leaf_nodes < 1) return bad(TLR_ERR_ARG, "leaf_nodes must be positive");
+  if (ring_slack_percent < 100 || ring_slack_percent > 1000)
+    return bad(TLR_ERR_ARG, "ring_slack_percent must lie in [100, 1000]");
+  const int sx = xi->q + 1, se = eta->q + 1, nn = ny * nz;
+  const std::vector<int> xi_idx(xi->stencil_indices, xi->stencil_indices + (size_t)ny * sx);
+  const std::vector<int> eta_idx(eta->stencil_indices, eta->stencil_indices + (size_t)nz * se);
+  const std::vector<int> eta_off(eta->stencil_offsets, eta->stencil_offsets + (size_t)nz * se);
+  for (int v : xi_idx)
+    if (v < 0 || v >= ny) return bad(TLR_ERR_STENCIL, "xi stencil index out of range");
+  for (int v : eta_idx)
+    if (v < 0 || v >= nz) return bad(TLR_ERR_STENCIL, "eta stencil index out of range");
+  for (int v : eta_off)
+    if (v <= -nz || v >= nz) return bad(TLR_ERR_STENCIL, "eta stencil offset out of range");
+
+  // block pattern of A_bc: the tensor product of the two stencils at every
+  // node, sorted and unique (the pattern tlr_assemble builds)
+  std::vector<int> row_ptr((size_t)nn + 1, 0), col, cols;
+  col.reserve((size_t)nn * sx * se);
+  for (int u = 0; u < nn; ++u) {
+    const int i = u % ny, j = u / ny;
+    cols.clear();
+    for (int t = 0; t < se; ++t)
+      for (int s = 0; s < sx; ++s)
+        cols.push_back(eta_idx[(size_t)j * se + t] * ny + xi_idx[(size_t)i * sx + s]);
+    std::sort(cols.begin(), cols.end());
+    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+    col.insert(col.end(), cols.begin(), cols.end());
+    row_ptr[u + 1] = (int)col.size();
+  }
+  tlr::Symbolic sym;
+  const int rc = tlr::build_symbolic(ny, nz, xi_idx, sx, eta_off, se, row_ptr, col, leaf_nodes,
+                                     sym, ring_slack_percent);
+  if (rc) {
+    char msg[64];
+    std::snprintf(msg, sizeof msg, "symbolic analysis failed (code %d)", rc);
+    return bad(TLR_ERR_ARG, msg);
+  }
+  const int nf = (int)sym.fronts.size();
+  *info = tlr_symbolic_info{};
+  info->fronts = nf;
+  info->levels = (int)sym.levels.size();
+  for (const auto &f : sym.fronts) {
+    info->max_front_order = std::max(info->max_front_order, f.m);
+    info->max_pivots = std::max(info->max_pivots, f.p);
+  }
+  info->flops = sym.flops;
+  info->factor_elems = sym.factor_elems;
+  info->pool_elems = sym.pool_elems;
+  if (node_rank) std::copy(sym.rank.begin(), sym.rank.end(), node_rank);
+  if (node_front)
+    for (int t = 0; t < nf; ++t)
+      for (int u : sym.fronts[t].piv) node_front[u] = t;
+  if (front_parent) {
+    if (front_capacity < nf)
+      return bad(TLR_ERR_SIZE, "front_parent holds fewer entries than the analysis has fronts");
+    for (int t = 0; t < nf; ++t) front_parent[t] = sym.fronts[t].parent;
+  }
+  return TLR_OK;
+}

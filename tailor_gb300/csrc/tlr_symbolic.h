@@ -52,10 +52,13 @@ struct Symbolic {
 };
 
 // Build the symbolic structure from the host copies of the rules and the
-// BSR pattern (row_ptr / col of A_bc).
+// BSR pattern (row_ptr / col of A_bc).  A box of the periodic ring is cut
+// across xi instead of across the ring when the xi separator has at most
+// ring_slack_percent / 100 times the ring cut's nodes; 100 is the solver's
+// ordering.
 int build_symbolic(int ny, int nz, const std::vector<int> &xi_idx, int sx,
                    const std::vector<int> &eta_off, int se,
                    const std::vector<int> &row_ptr, const std::vector<int> &col,
-                   int leaf_nodes, Symbolic &out);
+                   int leaf_nodes, Symbolic &out, int ring_slack_percent = 100);
 
 }  // namespace tlr
