@@ -497,7 +497,7 @@ class WGroup(_Node):
         arr = np.asarray(data)
         if arr.dtype not in (np.float64,) and arr.dtype.kind not in "iu":
             raise H5Error(f"cannot write element type {arr.dtype}")
-        d = _WData(np.ascontiguousarray(arr))
+        d = _WData(np.array(arr, order="C"))  # keeps 0-d arrays scalar
         d.attrs.update(attrs or {})
         g.children[leaf] = d
 
