@@ -60,16 +60,37 @@ def _scalar(text: str, lineno: int):
 
 
 def _strip_comment(line: str) -> str:
-    out, quote = [], None
-    for i, ch in enumerate(line):
+    """The line without its comment: a '#' at the start of the line or after
+    whitespace, outside quotes.  A quote opens a quoted scalar only where a
+    key or a value begins, so apostrophes inside plain scalars are text."""
+    out, quote, i, n = [], None, 0, len(line)
+    at_start = True  # the next non-blank character begins a key or a value
+    while i < n:
+        ch = line[i]
         if quote:
+            out.append(ch)
+            if quote == "'" and ch == "'" and line[i + 1:i + 2] == "'":
+                out.append("'")  # '' inside a single-quoted scalar
+                i += 2
+                continue
+            if quote == '"' and ch == "\\" and i + 1 < n:
+                out.append(line[i + 1])
+                i += 2
+                continue
             if ch == quote:
                 quote = None
-        elif ch in "'\"":
-            quote = ch
-        elif ch == "#" and (i == 0 or line[i - 1] in " \t"):
+            i += 1
+            continue
+        if ch == "#" and (i == 0 or line[i - 1] in " \t"):
             break
+        if ch in "'\"" and at_start:
+            quote = ch
+        if ch == ":" and line[i + 1:i + 2] in ("", " ", "\t"):
+            at_start = True
+        elif ch not in " \t":
+            at_start = False
         out.append(ch)
+        i += 1
     return "".join(out).rstrip()
 
 
