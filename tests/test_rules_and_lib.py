@@ -223,3 +223,19 @@ int main(void) {
     status, message, x0 = out.strip().split("|")
     assert status == "invalid argument" and "N must be at least 2" in message
     assert float(x0) == -1.0
+
+
+def test_no_gpu_means_an_error_not_a_fallback():
+    """Without a CUDA device the product path stops with TLR_ERR_CUDA and the
+    driver's message; nothing computes on the CPU in its place."""
+    from conftest import has_gpu
+    if has_gpu():
+        pytest.skip("a CUDA device is present")
+    from tailor_gb300 import api
+    from tailor_gb300.case import make_case
+    with pytest.raises(api.TailorError) as e:
+        api.Problem(make_case(24, 16))
+    assert e.value.status == 11 and "CUDA" in e.value.message
+    with pytest.raises(api.TailorError) as e:
+        api.solve_pencil(np.eye(10, dtype=complex), np.eye(10, dtype=complex), 0.5j, nev=2)
+    assert e.value.status == 11
