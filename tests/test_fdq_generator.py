@@ -180,3 +180,17 @@ def test_validate_rule_rejects_broken_rules():
     nodes[5] = nodes[4]  # periodic moments use x + offset h, so row 5 fails on order first
     with pytest.raises(rules.RuleError, match="eta FD-q nodes must be strictly increasing"):
         rules.validate_rule("eta", dataclasses.replace(pr, nodes=nodes))
+
+
+@pytest.mark.parametrize("q", [2, 3, 4, 5, 6, 7, 8, 9, 10, 12])
+def test_generator_sweep_passes_the_loader_checks(q):
+    """Every degree with node counts from the full-stencil limit (q + 1
+    nodes) to 400 bounded and 500 periodic nodes converges and passes the
+    C++ loader's rule checks (Prepare.cpp:328-437)."""
+    for n in sorted({q + 1, q + 2, q + 3, 2 * q, 3 * q + 1, 25, 40, 64, 101, 150, 257, 400}):
+        r = rules.generate_rule(n, q, False)
+        rules.validate_rule("xi", r)
+        assert r.n == n and np.all(np.diff(r.nodes) > 0)
+    if q % 2 == 0:
+        for n in (q + 1, q + 2, 16, 33, 64, 128, 192, 500):
+            rules.validate_rule("eta", rules.generate_rule(n, q, True))
