@@ -106,3 +106,42 @@ def test_unwritable_types_rejected():
                 np.zeros(2, dtype=np.float32)):
         with pytest.raises(h5.H5Error, match="cannot write element type"):
             w.dataset("bad", bad)
+
+
+@pytest.mark.timeout(120)
+def test_damaged_files_raise_h5error(tmp_path):
+    """Random byte flips, 8-byte address overwrites and truncations of a
+    written file either read or raise H5Error -- no other exception."""
+    rng = np.random.default_rng(7)
+    w = h5.Writer()
+    w.attrs["title"] = "damaged"
+    for i in range(20):
+        w.dataset(f"g{i % 3}/d{i}", rng.standard_normal((3, 4)), {"k": i})
+    good = tmp_path / "good.h5"
+    w.write(good)
+    base = good.read_bytes()
+
+    def walk(g):
+        for k in g.keys():
+            x = g[k]
+            walk(x) if isinstance(x, h5.Group) else x[...]
+            dict(x.attrs)
+
+    path = tmp_path / "bad.h5"
+    for _ in range(600):
+        b = bytearray(base)
+        mode = rng.integers(3)
+        if mode == 0:
+            for _ in range(int(rng.integers(1, 8))):
+                b[int(rng.integers(len(b)))] = int(rng.integers(256))
+        elif mode == 1:
+            b = b[:int(rng.integers(len(b)))]
+        else:
+            p = int(rng.integers(len(b) - 8))
+            b[p:p + 8] = int(rng.integers(0, 2 ** 63)).to_bytes(8, "little")
+        path.write_bytes(bytes(b))
+        try:
+            with h5.File(path) as f:
+                walk(f)
+        except h5.H5Error:
+            pass
