@@ -162,3 +162,23 @@ def test_argument_errors():
     assert st == 3 and info.fronts > 4  # TLR_ERR_SIZE, info filled for sizing
     assert lib.tlr_symbolic_analyze(None, ctypes.byref(re_), 0, 0, ctypes.byref(info),
                                     None, None, None, 0) == 1
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_grids(seed):
+    """Random grid sizes, stencil degrees (odd and even bounded q, even
+    periodic q), leaf sizes and ring slack: the tree stays valid and the
+    counts match the independent recount."""
+    rng = np.random.default_rng(seed)
+    qy = int(rng.integers(2, 11))
+    qz = int(rng.choice([2, 4, 6, 8]))
+    ny = int(rng.integers(qy + 1, 90))
+    nz = int(rng.integers(qz + 2, 70))
+    xi, eta = rules.generate_rule(ny, qy, False), rules.generate_rule(nz, qz, True)
+    leaf = int(rng.choice([0, 1, 8, 32, 200]))
+    slack = int(rng.choice([0, 100, 150, 400]))
+    res = api.symbolic_analysis(xi, eta, leaf, slack)
+    u, v, _ = _check_tree(xi, eta, res)
+    flops, factor, pool, max_m = _recount(xi, eta, res, u, v)
+    assert (res["factor_elems"], res["pool_elems"], res["max_front_order"]) == (factor, pool, max_m)
+    assert flops == pytest.approx(res["flops"], rel=1e-12)
