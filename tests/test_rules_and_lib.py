@@ -239,3 +239,82 @@ def test_no_gpu_means_an_error_not_a_fallback():
     with pytest.raises(api.TailorError) as e:
         api.solve_pencil(np.eye(10, dtype=complex), np.eye(10, dtype=complex), 0.5j, nev=2)
     assert e.value.status == 11
+
+
+def test_shift_mode_is_judged_by_the_plain_answer(monkeypatch):
+    """learned_solve in shift mode keeps a shifted answer only when every
+    eigenvalue within R of the target lies inside the disk the shifted solve
+    covered and every kept residual meets 1e-10; otherwise the plain solve
+    runs and is returned.  Stand-ins replace the GPU solver and the network."""
+    from types import SimpleNamespace
+    from tailor_gb300 import api, learned
+
+    target = 0.0 + 0.0j
+    plain_lam = np.array([0.10 + 0.0j, -0.20j])
+    calls = []
+
+    class FakeSolver:
+        def __init__(self, problem):
+            pass
+
+        def solve(self, nev=0, precision=1, sigma=None, start=None, fallback=True, **kw):
+            calls.append(("shift" if sigma is not None else "plain", nev))
+            if sigma is None:
+                return api.EigenSolution(plain_lam.copy(), np.full(2, 1e-12), None,
+                                         {"iterations": 5, "solves": 50})
+            return shifted(nev)
+
+    class FakeProposal:
+        target = 0.0 + 0.0j
+
+        def propose(self, point, nev):
+            return sigma_p, np.ones(4, complex), np.zeros(8, complex)
+
+    monkeypatch.setattr(api, "EigenSolver", FakeSolver)
+    monkeypatch.setattr(api, "run_pipeline", lambda p: {})
+    prob = SimpleNamespace(case=SimpleNamespace(physics=SimpleNamespace(alpha=1.0, reynolds=1e3,
+                                                                        mach=0.5)))
+
+    def covering(nev):  # nev + 2 values around sigma, far ones beyond the target disk
+        lam = np.array([0.10 + 0.0j, -0.20j, 0.9 + 0.0j, -0.9 + 0.0j])[:nev]
+        return api.EigenSolution(lam, np.full(nev, 1e-12), None, {"iterations": 3, "solves": 30})
+
+    # covered: |target - sigma| + R <= r' with sigma near the target
+    sigma_p, shifted = 0.01 + 0.0j, covering
+    sol, used, st = learned.learned_solve(prob, FakeProposal(), nev=2, shift=True, extra=2)
+    assert used and calls == [("shift", 4)]
+    assert np.allclose(np.sort_complex(sol.lam), np.sort_complex(plain_lam))
+
+    # not covered: sigma far from the target; the nev + 2 values nearest it
+    # span a disk that misses the target's neighbourhood
+    calls.clear()
+    sigma_p = 5.0 + 0.0j
+
+    def around_sigma(nev):
+        lam = sigma_p + np.array([-0.1, 0.1, 0.15j, -0.2])[:nev]
+        return api.EigenSolution(lam, np.full(nev, 1e-12), None, {"iterations": 3, "solves": 30})
+    shifted = around_sigma
+    sol, used, st = learned.learned_solve(prob, FakeProposal(), nev=2, shift=True, extra=2)
+    assert not used and st["fallback"] and calls == [("shift", 4), ("plain", 2)]
+    assert np.array_equal(sol.lam, plain_lam)
+
+    # a kept pair above the residual bar
+    calls.clear()
+    sigma_p = 0.01 + 0.0j
+
+    def loose(nev):
+        s = covering(nev)
+        s.residual[0] = 1e-8
+        return s
+    shifted = loose
+    sol, used, st = learned.learned_solve(prob, FakeProposal(), nev=2, shift=True, extra=2)
+    assert not used and calls[-1] == ("plain", 2)
+
+    # the shifted solve fails outright
+    calls.clear()
+
+    def failing(nev):
+        raise api.TailorError(13, "not converged")
+    shifted = failing
+    sol, used, st = learned.learned_solve(prob, FakeProposal(), nev=2, shift=True, extra=2)
+    assert not used and calls == [("shift", 4), ("plain", 2)]
