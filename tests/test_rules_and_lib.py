@@ -241,7 +241,7 @@ def test_no_gpu_means_an_error_not_a_fallback():
     assert e.value.status == 11
 
 
-def test_shift_mode_is_judged_by_the_plain_answer(monkeypatch):
+def test_shift_mode_answer_is_checked_against_the_plain_one(monkeypatch):
     """learned_solve in shift mode keeps a shifted answer only when every
     eigenvalue within R of the target lies inside the disk the shifted solve
     covered and every kept residual meets 1e-10; otherwise the plain solve
