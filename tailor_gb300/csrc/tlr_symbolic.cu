@@ -260,6 +260,8 @@ extern "C" int tlr_symbolic_analyze(const tlr_rule *xi, const tlr_rule *eta, int
   if (ring_slack_percent < 100 || ring_slack_percent > 1000)
     return bad(TLR_ERR_ARG, "ring_slack_percent must lie in [100, 1000]");
   const int sx = xi->q + 1, se = eta->q + 1, nn = ny * nz;
+  if ((long long)nn * sx * se > INT_MAX)
+    return bad(TLR_ERR_SIZE, "grid and stencils too large for 32-bit pattern offsets");
   const std::vector<int> xi_idx(xi->stencil_indices, xi->stencil_indices + (size_t)ny * sx);
   const std::vector<int> eta_idx(eta->stencil_indices, eta->stencil_indices + (size_t)nz * se);
   const std::vector<int> eta_off(eta->stencil_offsets, eta->stencil_offsets + (size_t)nz * se);
