@@ -421,6 +421,11 @@ int tlr_wait_selftest(int which, unsigned limit, int *timed_out);
 long long tlr_kernel_launches(void);
 
 const char *tlr_status_string(int status);
+/* Message of the last failure: the context's own for a non-NULL ctx; for
+ * NULL, the last failure of a call without a context (creation, sweeps,
+ * pencils, rule generation, symbolic analysis) on the calling thread --
+ * each host thread keeps its own.  The pointer stays valid until the next
+ * call on the same context or thread. */
 const char *tlr_last_error(const tlr_ctx *ctx);
 
 #ifdef __cplusplus
