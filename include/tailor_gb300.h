@@ -268,16 +268,19 @@ int tlr_mlp_train(tlr_mlp *m, const float *x, const float *y, int n,
 int tlr_mlp_forward(tlr_mlp *m, const float *x, int n, float *y, int bf16);
 
 /* Frobenius norm sqrt(sum |v|^2) of `count` complex values at the device
- * address `values`, written to the host double `result`, computed on
- * `stream` (NULL: the default stream) -- the norm tlr_assemble and
- * tlr_apply_bc report for the operators.  No counterpart in the reference:
- * it serves callers that cannot allocate device memory (code running while
- * a CUDA graph is captured in global mode, or hosts whose allocator forbids
- * raw cudaMalloc).  It allocates nothing: its scratch is a fixed 32 KB
- * device array inside the library, so count is limited to 2^28 values
- * (TLR_ERR_SIZE beyond that).  The first call on a device looks up that
- * array and should come before any stream capture; calls that overlap on
- * the GPU share the array and race. */
+ * address `values` (16-byte aligned: TLR_ERR_ARG otherwise), written to the
+ * host double `result`, computed on `stream` (NULL: the default stream) --
+ * the norm tlr_assemble and tlr_apply_bc report for the operators.  No
+ * counterpart in the reference: it serves callers that cannot allocate
+ * device memory (hosts whose caching allocator forbids raw cudaMalloc from
+ * the libraries they load, or that reserve nearly all of HBM for their own
+ * pool).  It allocates nothing: its scratch is a fixed 32 KB device array
+ * inside the library, one per device, so count is limited to 2^28 values
+ * (TLR_ERR_SIZE beyond that).  It copies the result to the host and
+ * synchronises the stream before returning.  The first call on a device
+ * looks up that array and should come before any stream capture; every
+ * call shares the array, so calls that overlap on the GPU race: serialise
+ * them (one stream, or synchronise between calls). */
 int tlr_frobenius_noalloc(const double *values, size_t count, double *result,
                           void *stream);
 

@@ -1,24 +1,26 @@
 // tlr_noalloc.cu -- Frobenius norm of a complex array with no allocation.
 //
-// Some callers cannot allocate device memory.  Code that runs while a CUDA
-// graph is being captured in global capture mode may not call cudaMalloc,
-// and host frameworks that route every device allocation through their own
-// caching allocator forbid raw cudaMalloc/cudaFree from libraries they
-// load.  tlr_frobenius_noalloc serves them: it computes the same
-// Frobenius norm that tlr_assemble and tlr_apply_bc report for the
+// Some callers cannot allocate device memory.  Host frameworks that route
+// every device allocation through their own caching pool forbid raw
+// cudaMalloc/cudaFree from the libraries they load, and applications that
+// reserve nearly all of HBM for their own pool at start-up leave a library
+// nothing to allocate from.  tlr_frobenius_noalloc serves them: it computes
+// the same Frobenius norm that tlr_assemble and tlr_apply_bc report for the
 // operators (sqrt of the sum of |v|^2 over complex values), and its only
 // scratch is a file-scope __device__ array of kMaxPartials + 1 doubles
 // (32 KB + 8 B) that every GPU which loads the library keeps until exit.
 //
-// The caller passes the input (a device array) and the output (a host
-// double).  The entry point calls no cudaMalloc, cudaFree or allocating
-// library routine.  The first call on a device looks up the array's
-// device address (cudaGetSymbolAddress, with that device current) and
-// caches it; make that first call before any stream capture begins.
-// Every call shares the one array, so calls whose kernels overlap on the
-// GPU race: serialise them (one stream, or synchronise between calls).
-// Each call overwrites every partial slot it reads, so nothing needs
-// clearing between calls.
+// The caller passes the input (a 16-byte aligned device array) and the
+// output (a host double).  The entry point calls no cudaMalloc, cudaFree or
+// allocating library routine.  It copies the result to the host and
+// synchronises the stream before it returns.  The first call on a device
+// looks up the array's device address (cudaGetSymbolAddress, with that
+// device current) and caches it; make that first call before any stream
+// capture begins.  Every call shares the one array, so calls whose kernels
+// overlap on the GPU race: serialise them (one stream, or synchronise
+// between calls).  Each call overwrites every partial slot it reads, so
+// nothing needs clearing between calls.
+#include <cstdint>
 #include <mutex>
 
 #include "tlr_internal.h"
@@ -76,7 +78,13 @@ extern "C" int tlr_frobenius_noalloc(const double *values, size_t count, double 
     set_global_error("tlr_frobenius_noalloc: null values or result pointer");
     return TLR_ERR_ARG;
   }
-  if ((long long)count > kMaxCount) {
+  if ((reinterpret_cast<uintptr_t>(values) & 15u) != 0) {
+    // the kernel reads one complex value (two doubles) per 16-byte load
+    set_global_error("tlr_frobenius_noalloc: values must be 16-byte aligned "
+                     "(the start of a complex128 array)");
+    return TLR_ERR_ARG;
+  }
+  if (count > static_cast<size_t>(kMaxCount)) {
     set_global_error("tlr_frobenius_noalloc: count exceeds the maximum of 268435456 "
                      "complex values (the fixed scratch holds 4096 partial sums)");
     return TLR_ERR_SIZE;
@@ -104,6 +112,7 @@ extern "C" int tlr_frobenius_noalloc(const double *values, size_t count, double 
     scratch = g_addr[dev];
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  (void)cudaGetLastError();  // a stale error from earlier work is not this call's
   const int nb = count == 0 ? 1 : (int)(((long long)count + kPerBlock - 1) / kPerBlock);
   { k_partial<<<nb, 256, 0, st>>>((long long)count, reinterpret_cast<const double2 *>(values),
                                 scratch); count_launches(); }

@@ -80,6 +80,26 @@ def test_sweep_argument_checks_without_gpu():
     assert rc == 1 and b"invalid sweep arguments" in lib.tlr_last_error(None)
 
 
+def test_noalloc_norm_argument_checks_without_gpu():
+    """tlr_frobenius_noalloc refuses null, misaligned and oversized inputs
+    before it touches a device, so these calls launch no kernel."""
+    import ctypes
+    from tailor_gb300 import _lib as L
+    tb.build()
+    lib = L.load()
+    out = ctypes.c_double(0.0)
+    rc = lib.tlr_frobenius_noalloc(None, 4, ctypes.byref(out), None)
+    assert rc == 1 and b"null" in lib.tlr_last_error(None)
+    # base + 1 double: an odd-double offset into a complex128 array
+    rc = lib.tlr_frobenius_noalloc(ctypes.c_void_p(4096 + 8), 4, ctypes.byref(out), None)
+    assert rc == 1 and b"16-byte aligned" in lib.tlr_last_error(None)
+    rc = lib.tlr_frobenius_noalloc(ctypes.c_void_p(4096), 2 ** 28 + 1, ctypes.byref(out), None)
+    assert rc == 3 and b"maximum" in lib.tlr_last_error(None)
+    # a count above LLONG_MAX is still a size error, not a launch failure
+    rc = lib.tlr_frobenius_noalloc(ctypes.c_void_p(4096), 2 ** 63 + 5, ctypes.byref(out), None)
+    assert rc == 3 and b"maximum" in lib.tlr_last_error(None)
+
+
 def test_rebuilt_baseflow_matches_synthetic_case():
     """Mach changes reload the Crocco-Busemann base flow (api.Problem.set_physics)."""
     from tailor_gb300.case import Physics, make_case, rebuild_baseflow

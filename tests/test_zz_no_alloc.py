@@ -1,13 +1,14 @@
 """tlr_frobenius_noalloc: the allocation-free Frobenius norm.
 
-It is for callers that cannot allocate device memory (code running while a
-CUDA graph is captured in global mode, hosts whose allocator forbids raw
-cudaMalloc).  Its result must match the norm the existing entry point
-tlr_assemble reports for the assembled operator L, on two calls in a row
-(the calls share the library's fixed scratch array), and sizes beyond its
-fixed maximum must be refused.  The test allocates the input buffer
-itself; the entry point allocates nothing.  This file runs last so a
-stop-at-first-failure run has executed every other test before it."""
+It is for callers that cannot allocate device memory (hosts whose caching
+allocator forbids raw cudaMalloc from the libraries they load, or that hold
+nearly all of HBM in their own pool).  Its result must match the norm the
+existing entry point tlr_assemble reports for the assembled operator L, on
+two calls in a row (the calls share the library's fixed scratch array), and
+sizes beyond its fixed maximum and misaligned inputs must be refused.  The
+test allocates the input buffer itself; the entry point allocates nothing.
+This file runs last so a stop-at-first-failure run has executed every other
+test before it."""
 import ctypes
 
 import numpy as np
@@ -18,6 +19,7 @@ from tailor_gb300.case import make_case
 
 pytestmark = pytest.mark.gpu
 
+TLR_ERR_ARG = 1
 TLR_ERR_SIZE = 3
 
 
@@ -49,3 +51,7 @@ def test_frobenius_noalloc_matches_assembly_norm(gpu_lib):
     st = gpu_lib.tlr_frobenius_noalloc(ctypes.c_void_p(16), 2 ** 28 + 1, ctypes.byref(out), None)
     assert st == TLR_ERR_SIZE
     assert b"maximum" in gpu_lib.tlr_last_error(None)
+    # an odd-double offset into a complex array is refused before any launch
+    st = gpu_lib.tlr_frobenius_noalloc(ctypes.c_void_p(24), 4, ctypes.byref(out), None)
+    assert st == TLR_ERR_ARG
+    assert b"aligned" in gpu_lib.tlr_last_error(None)
