@@ -6,18 +6,20 @@ Two entry points mirror the reference's preparation layer:
   ``prepare_fdq_case`` (src/Python/interpolate.py:501-585) without its
   HDF5 cache: read a structured source sample (interpolate.py:170-215),
   take (or generate) the bounded y and periodic z FD-q rules, interpolate
-  every grid and base-flow component with the periodic quintic tensor
-  spline (interpolate.py:82-157, 220-246) and validate the result
-  (interpolate.py:249-337);
+  every grid and base-flow component in the reference's spline spaces
+  (quintic, periodic along z and not-a-knot along y; interpolate.py:82-157,
+  220-246) and check the result (the checks of interpolate.py:249-337);
 * ``load_prepared(path, q_y, q_z, physics)`` -- ``Prepare::initialize``
   (src/CPlusPlus/Prepare.cpp:443-687): read a prepared schema-2 FD-q case
   (attributes, the two rules under /discretization, the natural-order grid
   and base-flow vectors) with the reference's checks and messages.
 
 Both return a :class:`tailor_gb300.case.Case` ready for ``api.Problem``.
-The spline itself is SciPy's interpolating B-spline (``make_interp_spline``,
-degree 5; not-a-knot along y, periodic along z), the routine the reference
-calls, so prepared fields agree with the reference's to rounding.
+The splines are this package's own interpolation operators (``spline``):
+each axis becomes one dense matrix and every component is interpolated by
+two matrix products.  The spline spaces are the reference's, and the
+interpolants are unique, so prepared fields agree with the reference's to
+rounding.
 """
 from __future__ import annotations
 
@@ -25,7 +27,7 @@ from pathlib import Path
 
 import numpy as np
 
-from . import h5
+from . import h5, spline
 from .case import Case, Physics
 from .rules import Rule, RuleError, load_rule, validate_rule
 
@@ -71,139 +73,119 @@ def read_structured_sample(path: str | Path):
     return grid, base, ny, nz, period
 
 
-def quintic_tensor_spline(z_old, y_old, values, z_new, y_new):
-    """One real or complex field on a bounded tensor grid onto (z_new, y_new)
-    with the exact (s = 0) degree-5 tensor-product spline
-    (interpolate.py:31-79, SciPy's RectBivariateSpline as there)."""
-    from scipy.interpolate import RectBivariateSpline
-
-    z_old, y_old = np.asarray(z_old, dtype=np.float64), np.asarray(y_old, dtype=np.float64)
-    z_new, y_new = np.asarray(z_new, dtype=np.float64), np.asarray(y_new, dtype=np.float64)
-    field = np.asarray(values)
-    if z_old.ndim != 1 or y_old.ndim != 1:
-        raise PrepareError("source logical coordinates must be one-dimensional")
-    if z_new.ndim != 1 or y_new.ndim != 1:
-        raise PrepareError("target logical coordinates must be one-dimensional")
-    if z_old.size < 6 or y_old.size < 6:
-        raise PrepareError("quintic B-spline interpolation requires at least 6 nodes per axis")
-    if field.shape != (z_old.size, y_old.size):
-        raise PrepareError(f"values must have shape ({z_old.size}, {y_old.size}); "
-                           f"got {field.shape}")
-    if not all(np.all(np.isfinite(a)) for a in (z_old, y_old, z_new, y_new, field)):
-        raise PrepareError("spline coordinates and values must be finite")
-    if np.any(np.diff(z_old) <= 0.0) or np.any(np.diff(y_old) <= 0.0):
-        raise PrepareError("source logical coordinates must be strictly increasing")
-
-    def real(v):
-        sp = RectBivariateSpline(z_old, y_old, np.asarray(v, dtype=np.float64), kx=5, ky=5, s=0.0)
-        return np.asarray(sp(z_new, y_new, grid=True), dtype=np.float64)
-
-    if np.iscomplexobj(field):
-        return real(field.real) + 1j * real(field.imag)
-    return real(field)
+def _uniform_periodic_phase(z_old: np.ndarray, period: float) -> np.ndarray:
+    """Phases (in units of the period) of periodic source nodes, which must
+    be uniformly spaced and must not repeat the wrap-around node."""
+    n = z_old.size
+    h = period / n
+    if z_old[-1] - z_old[0] >= period:
+        raise PrepareError("periodic source nodes repeat the wrap-around node "
+                           "(give the open interval only)")
+    if float(np.max(np.abs(np.diff(z_old) - h))) > 5e-13 * max(1.0, abs(h)):
+        raise PrepareError("periodic source nodes are not uniformly spaced "
+                           f"(expected spacing {h!r})")
+    return (z_old - z_old[0]) / period
 
 
-def periodic_quintic_spline(z_old, y_old, values, z_new, y_new, z_period=2.0,
-                            value_translation=0.0):
-    """One component [nz_old, ny_old] onto (z_new, y_new): quintic not-a-knot
-    spline along y, then a periodic quintic spline along z; a field that is
-    periodic up to a constant shift (the spanwise coordinate) is interpolated
-    as the periodic remainder plus the shift's linear part
-    (interpolate.py:82-157)."""
-    from scipy.interpolate import make_interp_spline
-
+def tensor_interpolate(z_old, y_old, values, z_new, y_new, period: float = 2.0,
+                       shift=0.0) -> np.ndarray:
+    """Fields [nz_old, ny_old, ...] on a periodic (z) x bounded (y) tensor grid
+    onto (z_new, y_new) with quintic splines: periodic along z, not-a-knot
+    along y (spline.periodic_matrix, spline.bounded_matrix).  A component
+    that grows by ``shift`` over one period (the spanwise coordinate) is
+    interpolated as its periodic part plus the linear growth."""
     z_old = np.asarray(z_old, dtype=np.float64)
-    y_old = np.asarray(y_old, dtype=np.float64)
     z_new = np.asarray(z_new, dtype=np.float64)
-    y_new = np.asarray(y_new, dtype=np.float64)
     field = np.asarray(values)
-    if z_old.ndim != 1 or y_old.ndim != 1:
-        raise PrepareError("source logical coordinates must be one-dimensional")
-    if z_new.ndim != 1 or y_new.ndim != 1:
-        raise PrepareError("target logical coordinates must be one-dimensional")
-    if z_old.size < 6 or y_old.size < 6:
-        raise PrepareError("periodic quintic interpolation requires at least 6 nodes per axis")
-    if field.shape != (z_old.size, y_old.size):
-        raise PrepareError(f"values must have shape {(z_old.size, y_old.size)}; got {field.shape}")
-    if not np.isfinite(z_period) or z_period <= 0.0:
-        raise PrepareError("z_period must be finite and positive")
-    if not all(np.all(np.isfinite(a)) for a in (z_old, y_old, z_new, y_new, field)):
-        raise PrepareError("periodic spline coordinates and values must be finite")
-    if np.any(np.diff(z_old) <= 0.0) or np.any(np.diff(y_old) <= 0.0):
-        raise PrepareError("source logical coordinates must be strictly increasing")
-    spacing = z_period / z_old.size
-    if float(np.max(np.abs(np.diff(z_old) - spacing))) > 5e-13 * max(1.0, abs(spacing)):
-        raise PrepareError("periodic source logical nodes must be uniformly spaced")
-    if z_old[-1] >= z_old[0] + z_period:
-        raise PrepareError("periodic source nodes must not include the repeated endpoint")
-    src_phase = (z_old - z_old[0]) / z_period
-    tgt_phase = (z_new - z_old[0]) / z_period
-    periodic = field - src_phase[:, None] * value_translation
-
-    def scalar(v):
-        along_y = np.asarray(make_interp_spline(y_old, np.asarray(v, dtype=np.float64), k=5,
-                                                axis=1)(y_new), dtype=np.float64)
-        ext_z = np.concatenate((z_old, [z_old[0] + z_period]))
-        ext_v = np.concatenate((along_y, along_y[:1]), axis=0)
-        return np.asarray(make_interp_spline(ext_z, ext_v, k=5, bc_type="periodic",
-                                             axis=0)(z_new), dtype=np.float64)
-
-    if np.iscomplexobj(periodic):
-        out = scalar(periodic.real) + 1j * scalar(periodic.imag)
-    else:
-        out = scalar(periodic)
-    return out + tgt_phase[:, None] * value_translation
+    try:
+        w_y = spline.bounded_matrix(y_old, y_new)
+        if z_old.ndim != 1 or z_new.ndim != 1:
+            raise spline.SplineError("z coordinates must be 1-D arrays")
+        if z_old.size < spline.DEGREE + 1:
+            raise spline.SplineError("a quintic spline needs 6 or more source nodes per axis, "
+                                     f"got {z_old.size}")
+    except spline.SplineError as e:
+        raise PrepareError(str(e)) from e
+    if field.shape[:2] != (z_old.size, w_y.shape[1]):
+        raise PrepareError(f"values have shape {field.shape}; the source grid needs "
+                           f"({z_old.size}, {w_y.shape[1]}, ...)")
+    if not (np.isfinite(period) and period > 0.0):
+        raise PrepareError("the spanwise period must be finite and positive")
+    if not (np.all(np.isfinite(field)) and np.all(np.isfinite(z_old))
+            and np.all(np.isfinite(z_new))):
+        raise PrepareError("interpolation inputs must be finite")
+    if np.any(np.diff(z_old) <= 0.0):
+        raise PrepareError("source coordinates must increase strictly")
+    phase_old = _uniform_periodic_phase(z_old, period)
+    phase_new = (z_new - z_old[0]) / period
+    w_z = spline.periodic_matrix(z_old.size, phase_new)
+    growth = np.broadcast_to(np.asarray(shift), field.shape[2:])
+    lift = phase_old.reshape((-1,) + (1,) * (field.ndim - 1)) * growth[None, None]
+    out = spline.tensor_apply(w_z, field - lift, w_y)
+    return out + phase_new.reshape((-1,) + (1,) * (field.ndim - 1)) * growth[None, None]
 
 
-def _interpolate(values, z_old, y_old, z_new, y_new, translations=None):
-    out = np.empty((z_new.size, y_new.size, values.shape[2]), dtype=np.complex128)
-    tr = np.zeros(values.shape[2], dtype=np.complex128) if translations is None else \
-        np.asarray(translations, dtype=np.complex128)
-    for c in range(values.shape[2]):
-        out[..., c] = periodic_quintic_spline(z_old, y_old, values[..., c], z_new, y_new,
-                                              2.0, tr[c])
-    return out
+def _d1_operator(rule: Rule):
+    """(D, c): the rule's first-derivative matrix and, for a periodic rule,
+    the per-row derivative of the wrap count, so that a field that grows by
+    p over one period has the derivative D f + c p."""
+    n = rule.n
+    d = np.zeros((n, n))
+    rows = np.repeat(np.arange(n), rule.indices.shape[1])
+    np.add.at(d, (rows, rule.indices.ravel()), rule.weights[1].ravel())
+    if not rule.periodic:
+        return d, np.zeros(n)
+    laps = (np.arange(n)[:, None] + rule.offsets - rule.indices) // n
+    return d, np.sum(rule.weights[1] * laps, axis=1)
 
 
-def _first_derivative(values, rule: Rule, axis: int, translation: float = 0.0):
-    """FD-q first derivative along one tensor axis (interpolate.py:249-268)."""
-    w = rule.weights[1]
-    if axis == 1:
-        return np.einsum("zij,ij->zi", values[:, rule.indices], w)
-    sampled = values[rule.indices, :]
-    if rule.periodic and translation != 0.0:
-        rows = np.arange(rule.n)[:, None]
-        wraps = (rows + rule.offsets - rule.indices) // rule.n
-        sampled = sampled + wraps[:, :, None] * translation
-    return np.einsum("izj,iz->ij", sampled, w)
+def check_prepared_fields(src_grid, src_base, grid, base, y_rule: Rule, z_rule: Rule,
+                          period: float, y_old, z_old) -> float:
+    """Checks on an interpolated case; returns the smallest grid Jacobian.
 
-
-def validate_interpolated(src_grid, src_base, grid, base, y_rule: Rule, z_rule: Rule,
-                          period: float) -> float:
-    """Positivity, corner preservation and a positive grid Jacobian
-    (interpolate.py:271-337); returns the minimum Jacobian."""
-    if not (np.all(np.isfinite(grid)) and np.all(np.isfinite(base))):
-        raise PrepareError("interpolated grid and baseflow must be finite")
-    if np.any(base[..., 0].real <= 0.0):
-        raise PrepareError("interpolated density is not strictly positive")
-    if np.any(base[..., 4].real <= 0.0):
-        raise PrepareError("interpolated temperature is not strictly positive")
-    for src, tgt, name in ((src_grid, grid, "grid"), (src_base, base, "baseflow")):
-        sc = np.asarray([src[0, 0], src[0, -1], src[-1, 0], src[-1, -1]])
-        tc = np.asarray([tgt[0, 0], tgt[0, -1], tgt[-1, 0], tgt[-1, -1]])
-        scale = max(1.0, float(np.max(np.abs(sc))))
-        err = float(np.max(np.abs(tc - sc)))
-        if err > 2e-11 * scale:
-            raise PrepareError(f"{name} corner preservation failed: error={err:.3e}")
-    py, pz = grid[..., 1].real, grid[..., 2].real
-    jac = (_first_derivative(py, y_rule, 1) * _first_derivative(pz, z_rule, 0, period)
-           - _first_derivative(py, z_rule, 0) * _first_derivative(pz, y_rule, 1))
+    * every value finite, density and temperature positive;
+    * wherever a target node coincides with a source node (the wall and the
+      far field, and any shared spanwise station) the source value is kept,
+      within 2e-11 of the field's scale;
+    * the Jacobian y_xi z_eta - y_eta z_xi of the target grid, from the
+      FD-q first-derivative rules, is finite and positive everywhere."""
+    fields = {"grid": (src_grid, grid), "baseflow": (src_base, base)}
+    for name, (_, tgt) in fields.items():
+        if not np.all(np.isfinite(tgt)):
+            raise PrepareError(f"the interpolated {name} has non-finite values")
+    for comp, label in ((0, "density"), (4, "temperature")):
+        if np.any(base[..., comp].real <= 0.0):
+            raise PrepareError(f"the interpolated {label} is not positive everywhere")
+    sy = [(int(j), int(np.argmin(np.abs(np.asarray(y_old) - v))))
+          for j, v in enumerate(y_rule.nodes)
+          if np.min(np.abs(np.asarray(y_old) - v)) <= 1e-14]
+    sz = [(int(k), int(np.argmin(np.abs(np.asarray(z_old) - v))))
+          for k, v in enumerate(z_rule.nodes)
+          if np.min(np.abs(np.asarray(z_old) - v)) <= 1e-14]
+    if sy and sz:
+        (tj, sj), (tk, sk) = zip(*sy), zip(*sz)
+        tj, sj, tk, sk = list(tj), list(sj), list(tk), list(sk)
+        for name, (src, tgt) in fields.items():
+            a = tgt[np.ix_(tk, tj)]
+            b = src[np.ix_(sk, sj)]
+            scale = max(1.0, float(np.max(np.abs(b))))
+            dev = float(np.max(np.abs(a - b)))
+            if dev > 2e-11 * scale:
+                raise PrepareError(f"the interpolated {name} moved a source node value by "
+                                   f"{dev:.3e}")
+    y, z = grid[..., 1].real, grid[..., 2].real      # [nz, ny]
+    dxi, _ = _d1_operator(y_rule)
+    deta, laps = _d1_operator(z_rule)
+    y_xi, z_xi = y @ dxi.T, z @ dxi.T
+    y_eta = deta @ y
+    z_eta = deta @ z + laps[:, None] * period
+    jac = y_xi * z_eta - y_eta * z_xi
     if not np.all(np.isfinite(jac)):
-        raise PrepareError("interpolated grid Jacobian contains non-finite values")
+        raise PrepareError("the interpolated grid's Jacobian has non-finite values")
     jmin = float(np.min(jac))
     if jmin <= 0.0:
-        raise PrepareError(f"interpolated grid Jacobian must be strictly positive; "
-                           f"minimum={jmin:.6e}")
+        raise PrepareError(f"the interpolated grid's Jacobian is not positive "
+                           f"(smallest value {jmin:.6e})")
     return jmin
 
 
@@ -234,9 +216,10 @@ def prepare_sample(path: str | Path, q_y: int = 10, q_z: int = 6,
     z_rule = load_rule(nz, q_z, periodic=True)
     y_old = np.linspace(-1.0, 1.0, ny)
     z_old = -1.0 + 2.0 * np.arange(nz) / nz
-    g = _interpolate(grid, z_old, y_old, z_rule.nodes, y_rule.nodes, [0.0, 0.0, period])
-    b = _interpolate(base, z_old, y_old, z_rule.nodes, y_rule.nodes)
-    validate_interpolated(grid, base, g, b, y_rule, z_rule, period)
+    g = tensor_interpolate(z_old, y_old, grid, z_rule.nodes, y_rule.nodes, 2.0,
+                           np.array([0.0, 0.0, period]))
+    b = tensor_interpolate(z_old, y_old, base, z_rule.nodes, y_rule.nodes, 2.0)
+    check_prepared_fields(grid, base, g, b, y_rule, z_rule, period, y_old, z_old)
     return Case(ny, nz, q_y, q_z, y_rule, z_rule, period, _interleave(g), _interleave(b),
                 physics or Physics())
 

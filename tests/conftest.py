@@ -1,3 +1,4 @@
+import os
 import sys
 from pathlib import Path
 
@@ -5,6 +6,11 @@ import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
 sys.path.insert(0, str(ROOT))
+
+# A checkout of the reference project, for the tests that read its own files
+# (rule caches, the shipped sample, its prepared case): the TAILOR_REFERENCE
+# environment variable names it; those tests skip when it is unset.
+REFERENCE = Path(os.environ["TAILOR_REFERENCE"]) if os.environ.get("TAILOR_REFERENCE") else None
 
 
 def pytest_configure(config):

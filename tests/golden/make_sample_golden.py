@@ -6,9 +6,15 @@ case/data/FD-q/fdq_sample_qy10_qz6.h5 (201 x 50 nodes, Re 32500, Mach 6,
 alpha 2.43, nev 8 nearest lambda = 0).  Run in a checkout that has the
 reference project:
 
-    python tests/golden/make_sample_golden.py /path/to/reference
+    python tests/golden/make_sample_golden.py /path/to/reference [--fields-only]
 
 Writes
+    sample_201x50_source.npz  the structured source sample (grid [Nz][Ny][3]
+                              and base flow [Nz][Ny][5], real parts; the
+                              imaginary parts are zero, checked) and its
+                              spanwise period, so the interpolation can be
+                              checked against the reference's prepared file
+                              without the reference checkout
     sample_201x50_fields.npz  the prepared grid [N][3] and base flow [N][5]
                               read from the reference's prepared file (all
                               imaginary parts are zero there, checked), so
@@ -37,11 +43,17 @@ def main() -> None:
 
     ref = Path(sys.argv[1])
     cfg = config.load_config(ref / "case" / "config.yaml", require_input=True)
+    grid, base, _, _, period = prepare.read_structured_sample(cfg.source_file)
+    assert np.all(grid.imag == 0) and np.all(base.imag == 0)
+    np.savez_compressed(HERE / "sample_201x50_source.npz", grid=grid.real, baseflow=base.real,
+                        spanwise_period=np.float64(period))
     case = prepare.load_prepared(cfg.input_file, cfg.q_y, cfg.q_z, cfg.physics)
     assert np.all(case.grid[..., 1] == 0) and np.all(case.baseflow[..., 1] == 0)
     np.savez_compressed(HERE / "sample_201x50_fields.npz", grid=case.grid[..., 0],
                         baseflow=case.baseflow[..., 0],
                         spanwise_period=np.float64(case.spanwise_period))
+    if "--fields-only" in sys.argv:
+        return
     t = time.time()
     o = Oracle()
     r = o.full(case)

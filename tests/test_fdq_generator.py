@@ -19,6 +19,8 @@ import pytest
 from tailor_gb300 import build as tb
 from tailor_gb300 import rules
 
+from conftest import REFERENCE
+
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
@@ -155,10 +157,10 @@ def test_load_or_create_uses_and_rebuilds_the_cache(tmp_path):
     assert np.array_equal(r3.nodes, r1.nodes) and rules.load_rule_file(path).n == 21
 
 
-@pytest.mark.skipif(not Path("/root/reference/fdqNodes/N200_q10.h5").is_file(),
-                    reason="reference checkout not present")
+@pytest.mark.skipif(REFERENCE is None or not (REFERENCE / "fdqNodes" / "N200_q10.h5").is_file(),
+                    reason="TAILOR_REFERENCE (a reference checkout) not set")
 def test_reference_rule_caches_load():
-    ref = Path("/root/reference/fdqNodes")
+    ref = REFERENCE / "fdqNodes"
     r = rules.load_rule_file(ref / "N200_q10.h5")
     g = rules.generate_rule(201, 10, False)
     assert np.max(np.abs(r.nodes - g.nodes)) < 1e-14

@@ -17,10 +17,12 @@ import pytest
 from tailor_gb300 import config, h5, output, prepare, rules
 from tailor_gb300.case import Physics, make_case
 
-REF = Path("/root/reference")
+from conftest import REFERENCE
+
+REF = REFERENCE
 GOLDEN = Path(__file__).resolve().parent / "golden"
-needs_ref = pytest.mark.skipif(not (REF / "case" / "config.yaml").is_file(),
-                               reason="reference checkout not present")
+needs_ref = pytest.mark.skipif(REF is None or not (REF / "case" / "config.yaml").is_file(),
+                               reason="TAILOR_REFERENCE (a reference checkout) not set")
 
 
 def test_writer_reader_round_trip(tmp_path):
@@ -85,6 +87,30 @@ def test_interpolation_matches_reference_prepared_file():
         assert np.max(np.abs(a - b) / scale) < 1e-13
     assert np.array_equal(ours.eta.weights, ref.eta.weights)
     assert np.max(np.abs(ours.xi.nodes - ref.xi.nodes)) < 1e-14
+
+
+def test_interpolation_matches_reference_prepared_fixture(tmp_path):
+    """The shipped sample's source fields (a fixture read from the
+    reference's sample.h5) interpolated here agree with the reference's own
+    prepared fields (a fixture read from its prepared file) to 1e-13
+    relative per component; no reference checkout needed."""
+    src = np.load(GOLDEN / "sample_201x50_source.npz")
+    prepared = np.load(GOLDEN / "sample_201x50_fields.npz")
+    nz, ny = src["grid"].shape[:2]
+    w = h5.Writer()
+    w.attrs.update({"Ny": ny, "Nz": nz, "spanwise_periodic": 1,
+                    "spanwise_period": float(src["spanwise_period"])})
+    w.dataset("grid", np.stack((src["grid"], np.zeros_like(src["grid"])), axis=-1))
+    w.dataset("baseflow", np.stack((src["baseflow"], np.zeros_like(src["baseflow"])), axis=-1))
+    path = tmp_path / "sample.h5"
+    w.write(path)
+    ours = prepare.prepare_sample(path, 10, 6)
+    assert (ours.ny, ours.nz) == (ny, nz)
+    assert ours.spanwise_period == float(prepared["spanwise_period"])
+    for a, b in ((ours.grid, prepared["grid"]), (ours.baseflow, prepared["baseflow"])):
+        assert np.all(a[..., 1] == 0.0)
+        scale = np.maximum(np.max(np.abs(b), axis=0), 1e-300)
+        assert np.max(np.abs(a[..., 0] - b) / scale) < 1e-13
 
 
 @needs_ref
@@ -253,8 +279,7 @@ def test_periodic_complex_field_and_affine_translation():
 
     z_new = -1.0 + 2.0 * np.arange(48) / 48
     y_new = np.linspace(-1.0, 1.0, 13)
-    got = prepare.periodic_quintic_spline(z_old, y_old, field(zg, yg), z_new, y_new,
-                                          value_translation=tr)
+    got = prepare.tensor_interpolate(z_old, y_old, field(zg, yg), z_new, y_new, shift=tr)
     zt, yt = np.meshgrid(z_new, y_new, indexing="ij")
     np.testing.assert_allclose(got, field(zt, yt), rtol=2e-6, atol=5e-6)
 
@@ -262,14 +287,17 @@ def test_periodic_complex_field_and_affine_translation():
 def test_periodic_spline_rejections():
     y = np.linspace(-1.0, 1.0, 8)
     z = np.linspace(-1.0, 1.0, 12)  # repeats the periodic endpoint
-    with pytest.raises(prepare.PrepareError, match="uniformly spaced"):
-        prepare.periodic_quintic_spline(z, y, np.zeros((12, 8)), z[:-1], y)
+    with pytest.raises(prepare.PrepareError, match="repeat the wrap-around node"):
+        prepare.tensor_interpolate(z, y, np.zeros((12, 8)), z[:-1], y)
+    zu = np.array([-1.0, -0.7, -0.5, 0.0, 0.2, 0.5, 0.7])
+    with pytest.raises(prepare.PrepareError, match="not uniformly spaced"):
+        prepare.tensor_interpolate(zu, y, np.zeros((7, 8)), zu, y)
     zp = -1.0 + 2.0 * np.arange(5) / 5
-    with pytest.raises(prepare.PrepareError, match="at least 6"):
-        prepare.periodic_quintic_spline(zp, y, np.zeros((5, 8)), zp, y)
+    with pytest.raises(prepare.PrepareError, match="6 or more source nodes"):
+        prepare.tensor_interpolate(zp, y, np.zeros((5, 8)), zp, y)
     zp = -1.0 + 2.0 * np.arange(12) / 12
-    with pytest.raises(prepare.PrepareError, match="values must have shape"):
-        prepare.periodic_quintic_spline(zp, y, np.zeros((8, 12)), zp, y)
+    with pytest.raises(prepare.PrepareError, match="the source grid needs"):
+        prepare.tensor_interpolate(zp, y, np.zeros((8, 12)), zp, y)
 
 
 def _write_source(path, ny=8, nz=12, period=6.0):
@@ -409,9 +437,13 @@ def test_malformed_prepared_file(tmp_path, mutate, message):
         prepare.load_prepared(bad, 10, 6)
 
 
-def test_quintic_tensor_spline_polynomial_exactness():
-    """interpolate.py's bounded spline reproduces degree-5 tensor polynomials
-    (tests/Python/test_interpolate.py:23-47, 8e-14)."""
+def test_bounded_quintic_spline_polynomial_exactness():
+    """The not-a-knot quintic operator reproduces degree-5 tensor
+    polynomials (the reference's bounded-spline test,
+    tests/Python/test_interpolate.py:23-47, 8e-14), and agrees with
+    SciPy's interpolating spline in the same space to rounding."""
+    from scipy.interpolate import make_interp_spline
+    from tailor_gb300 import spline
     z_old = np.linspace(-1.0, 1.0, 8)
     y_old = np.linspace(-1.0, 1.0, 9)
     zg, yg = np.meshgrid(z_old, y_old, indexing="ij")
@@ -421,15 +453,37 @@ def test_quintic_tensor_spline_polynomial_exactness():
 
     z_new = np.sort(np.linspace(-1.0, 1.0, 13) ** 3)
     y_new = np.sort(np.linspace(-1.0, 1.0, 14) ** 3)
-    got = prepare.quintic_tensor_spline(z_old, y_old, f(zg, yg), z_new, y_new)
+    got = spline.tensor_apply(spline.bounded_matrix(z_old, z_new), f(zg, yg),
+                              spline.bounded_matrix(y_old, y_new))
     zt, yt = np.meshgrid(z_new, y_new, indexing="ij")
     np.testing.assert_allclose(got, f(zt, yt), rtol=0.0, atol=8e-14)
-    with pytest.raises(prepare.PrepareError, match="at least 6"):
-        prepare.quintic_tensor_spline(np.linspace(-1, 1, 5), np.linspace(-1, 1, 6),
-                                      np.zeros((5, 6)), [-1.0, 1.0], [-1.0, 1.0])
-    with pytest.raises(prepare.PrepareError, match="values must have shape"):
-        prepare.quintic_tensor_spline(np.linspace(-1, 1, 6), np.linspace(-1, 1, 7),
-                                      np.zeros((7, 6)), [-1.0, 1.0], [-1.0, 1.0])
+    rng = np.random.default_rng(3)
+    x = np.sort(rng.uniform(-1.0, 1.0, 40))
+    v = rng.standard_normal((40, 3))
+    xn = np.linspace(x[0], x[-1], 97)
+    ref = make_interp_spline(x, v, k=5, axis=0)(xn)
+    assert np.max(np.abs(spline.bounded_matrix(x, xn) @ v - ref)) < 1e-12 * np.max(np.abs(ref))
+    with pytest.raises(spline.SplineError, match="6 or more"):
+        spline.bounded_matrix(np.linspace(-1, 1, 5), [-1.0, 1.0])
+    with pytest.raises(spline.SplineError, match="increase strictly"):
+        spline.bounded_matrix(np.array([0.0, 1.0, 1.0, 2.0, 3.0, 4.0]), [0.5])
+
+
+def test_periodic_quintic_operator_matches_the_periodic_spline():
+    """The circulant periodic operator equals SciPy's periodic quintic
+    interpolating spline on uniform nodes, and is exact at the nodes."""
+    from scipy.interpolate import make_interp_spline
+    from tailor_gb300 import spline
+    rng = np.random.default_rng(5)
+    for n in (6, 7, 32, 50):
+        v = rng.standard_normal((n, 2))
+        ph = rng.uniform(-1.5, 2.5, 41)
+        x = np.arange(n + 1) / n
+        ref = make_interp_spline(x, np.concatenate((v, v[:1])), k=5, bc_type="periodic",
+                                 axis=0)(np.mod(ph, 1.0))
+        w = spline.periodic_matrix(n, ph)
+        assert np.max(np.abs(w @ v - ref)) < 1e-13 * np.max(np.abs(ref))
+        assert np.max(np.abs(spline.periodic_matrix(n, np.arange(n) / n) - np.eye(n))) < 1e-14
 
 
 def test_stage_report_format(tmp_path):
