@@ -1,30 +1,57 @@
 """Benchmark: converged eigenpairs per second on one GB300.
 
-Workload (one "step"): the full BiGlobal pass of the C2 configuration --
-Ny = 200 (FD-q q=10) x Nz = 128 (periodic q=6) wavy-wall boundary layer,
-bump 0.08, Re 1000, Mach 0.5, alpha 1.8, nev 16, search centre
-omega = 0.3 + 0.01i (lambda target 0.01 - 0.3i), tol 1e-10: metrics,
-base-flow derivatives, assembly of M_Gamma and L, wall/far-field rows,
-factorisation of A - sigma B and shift-and-invert Krylov-Schur, with every
-reported eigenpair checked at relative residual <= 1e-10.  Only eigenpairs
-passing that check count.
+Headline workload: the neutral-curve sweep at the largest grid -- Ny = 300
+(FD-q q=10) x Nz = 192 (periodic q=6), 288 000 complex unknowns per point,
+wavy-wall boundary layer (bump 0.05), Mach 0.7, nev 8 nearest lambda = 0,
+tol 1e-10, points on the 8 x 4 grid of alpha in [0.5, 3.5] and Re in
+[800, 2400], visited in snake order (alpha up on one Re row, down on the
+next) so that consecutive points are neighbours.  One "step" is one point:
+metrics, base-flow derivatives, assembly of M_Gamma and L at the point's
+(alpha, Re), wall and far-field rows, factorisation of A - sigma B and the
+shift-and-invert Krylov-Schur solve, on one persistent context.
 
-value: device-resident (grid and base flow already in HBM), CUDA events on
-the context's stream around the step.  e2e: the same step through the
-public API from pinned host buffers (host->device copy of the inputs and
-device->host read of eigenvalues and residuals inside the timed region).
-Inputs and factors are far larger than L2 (the operator alone is 788 MB),
-so no flush is needed.
+The combined form (the line's value) is
+  * mixed: complex64 multifrontal factor with tensor-core Schur updates,
+    every K^-1 application refined in FP64 against the FP64 operator;
+  * batched: one context for the whole sweep (one symbolic analysis, captured
+    solve graphs), and block Krylov-Schur (8 vectors per operator
+    application: one triangular solve reads the factor once for all 8);
+  * learned: the first point of the run starts from the learned proposal
+    (an MLP trained, before the timed region, on eigenpairs the solver
+    computed at 60 x 32 over the sweep's parameter range, its start vector
+    carried to 300 x 192 by the spline operators); every later point starts
+    from its predecessor's 8 Ritz vectors.
+The plain FP64 form (complex128 factor, single-vector Krylov-Schur from a
+pseudo-random start, the reference's EigenSolver) solves a stated subset of
+the same points in the same run.
 
---impl reference times the reference algorithm's CPU path (the CPU oracle:
-C restatement of the assembly, LAPACK zggev boundary rows, SuperLU +
-ARPACK shift-invert) on the host cores, on a bounded sample of the same
-workload family (a 60 x 32 grid, same physics, nev and target).
+An eigenpair counts only if its relative residual ||Ax - lambda Bx|| /
+(|lambda| ||x||) <= 1e-10 and |dlambda| / |lambda| <= 1e-8 against the FP64
+reference eigenvalues of its point (tests/golden/c5_300x192_plain_eigs.txt,
+the plain FP64 form's, which is pinned to the CPU oracle at 100 x 50 and
+200 x 128).
+
+value: device-resident (grid and base flow in HBM), CUDA events on the
+context's stream around the K timed steps.  e2e: the next K points through
+the public API from pinned host buffers (host->device copy of the grid and
+base flow and device->host read of eigenvalues and residuals inside the
+timed region).  The operator (1.8 GB) and the factor (10 GB) are far larger
+than L2, so no flush is needed.
+
+Sub-records: c2 (200 x 128, nev 16, target 0.01 - 0.3i, alpha 1.8; mixed
+vs plain FP64, every eigenvalue against the CPU oracle's) and sweep_c3 (64
+instances on three grid classes, mixed + batched vs plain FP64).
+
+--impl reference: the reference algorithm's CPU path (the CPU oracle: C
+restatement of the assembly, LAPACK zggev boundary rows, SuperLU + ARPACK)
+cannot solve one 300 x 192 point within the step budget; it prints the
+reason and a measured CPU figure on a smaller grid, and no value.
 """
 from __future__ import annotations
 
 import argparse
 import ctypes
+import dataclasses
 import json
 import os
 import subprocess
@@ -38,12 +65,19 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "eigenpairs/s at resid<=1e-10"
+METRIC = "eigenpairs/s at resid<=1e-10 and |dlambda|/|lambda|<=1e-8"
 UNIT = "eigenpairs/s"
+RESID_TOL = 1e-10
+DLAM_TOL = 1e-8
+# combined form on the neutral-curve sweep
+C5_NEV = 8
+C5_BLOCK = 8
+C5_NCV = 48
+PLAIN_NCV = 32
+# C2: mixed vs plain FP64 at 200 x 128
 C2 = dict(ny=200, nz=128, amplitude=0.08, alpha=1.8, omega=complex(0.3, 0.01), nev=16)
-# Krylov-Schur basis size for both forms (the reference leaves it to SLEPc's
-# runtime -eps_ncv; 4 nev needs 3 restarts here instead of 13 at 2 nev)
-NCV = 64
+C2_NCV = 64
+GOLDEN = ROOT / "tests" / "golden"
 
 
 def c2_case(ny=None, nz=None):
@@ -114,14 +148,101 @@ class Events:
         return p
 
 
-def one_pass(prob, api, precision):
-    api.Metrics(prob).compute()
-    api.BaseFlowDerivatives(prob).compute()
-    op = api.GlobalOperator(prob).assemble()
-    api.BoundaryConditions(prob).apply()
-    sol = api.EigenSolver(prob).solve(precision=precision, ncv=NCV)
-    good = int(np.sum(sol.residual <= 1e-10))
-    return good, sol, op
+# ------------------------------------------------------- parity bookkeeping
+def load_c5_reference():
+    """{(alpha, Re): FP64 eigenvalues} of the sweep's points, or None."""
+    f = GOLDEN / "c5_300x192_plain_eigs.txt"
+    if not f.exists():
+        return None
+    ref = {}
+    for row in np.loadtxt(f, ndmin=2):
+        lam = row[2::3] + 1j * row[3::3]
+        ref[(round(row[0], 9), round(row[1], 6))] = lam
+    return ref
+
+
+def count_pairs(lam, res, ref_lam):
+    """(pairs passing both bars, largest |dlambda|/|lambda| against ref).
+    Without reference eigenvalues only the residual bar is applied and the
+    deviation is None."""
+    if ref_lam is None or len(ref_lam) == 0:
+        return int(np.sum(np.asarray(res) <= RESID_TOL)), None
+    good, worst = 0, 0.0
+    for l, r in zip(lam, res):
+        d = float(np.min(np.abs(ref_lam - l)) / abs(l))
+        worst = max(worst, d)
+        if r <= RESID_TOL and d <= DLAM_TOL:
+            good += 1
+    return good, worst
+
+
+# ------------------------------------------------------------ learned start
+def train_proposal(api, learned, points, grid=(60, 32)):
+    """The learned start proposal for the sweep: solver eigenpairs at a
+    coarse grid over the sweep's parameter box (alpha in [0.5, 3.5], Re
+    log-uniform in [800, 2400], Mach 0.7), an MLP fitted on the GPU by the
+    library's kernels.  Returns (proposal, seconds)."""
+    from tailor_gb300.neutral_sweep import c5_case
+    t = time.perf_counter()
+    rng = np.random.default_rng(7)
+    train = [(float(rng.uniform(0.5, 3.5)), float(10 ** rng.uniform(np.log10(800), np.log10(2400))),
+              0.7) for _ in range(48)]
+    case = c5_case(*grid, nev=C5_NEV)
+    with api.Problem(case) as prob:
+        samples = learned.generate(prob, train, nev=C5_NEV, precision=1)
+    prop = learned.Proposal.fit(samples, 0j, epochs=2000, batch=48, lr=1e-3)
+    prop.grid = grid
+    return prop, time.perf_counter() - t
+
+
+# ------------------------------------------------------------- C5 headline
+def c5_step(api, prob, point, first, proposal):
+    """One sweep point in the combined form; returns (lam, residual, diag)."""
+    _, alpha, re = point
+    prob.set_physics(dataclasses.replace(prob.case.physics, alpha=alpha, reynolds=re))
+    api.run_pipeline(prob)
+    kw = dict(nev=C5_NEV, ncv=C5_NCV, precision=1, block=C5_BLOCK)
+    if first:
+        start = proposal.start_on(prob.case, (alpha, re, prob.case.physics.mach)) \
+            if proposal is not None else None
+        sol = api.EigenSolver(prob).solve(start=start, **kw)
+    else:
+        sol = api.EigenSolver(prob).solve(warm_start=True, **kw)
+    return sol.lam, sol.residual, sol.diag
+
+
+def plain_step(api, prob, point):
+    _, alpha, re = point
+    prob.set_physics(dataclasses.replace(prob.case.physics, alpha=alpha, reynolds=re))
+    api.run_pipeline(prob)
+    sol = api.EigenSolver(prob).solve(nev=C5_NEV, ncv=PLAIN_NCV, precision=0)
+    return sol.lam, sol.residual, sol.diag
+
+
+def run_c2(api, ref_file=GOLDEN / "c2_200x128_eigs.txt"):
+    """C2: mixed (single-vector, the bench's earlier headline form) vs plain
+    FP64, one pass each after a warm-up, eigenvalues against the oracle."""
+    ref = None
+    if ref_file.exists():
+        r = np.loadtxt(ref_file, ndmin=2)
+        ref = r[:, 0] + 1j * r[:, 1]
+    case = c2_case()
+    out = {"workload": "C2: 200x128, nev 16, target 0.01-0.3i, alpha 1.8", "oracle": ref is not None}
+    with api.Problem(case) as prob:
+        for name, kw in (("mixed", dict(precision=1)), ("plain_fp64", dict(precision=0))):
+            api.run_pipeline(prob)
+            api.EigenSolver(prob).solve(nev=C2["nev"], ncv=C2_NCV, **kw)  # warm-up
+            t = time.perf_counter()
+            api.run_pipeline(prob)
+            sol = api.EigenSolver(prob).solve(nev=C2["nev"], ncv=C2_NCV, **kw)
+            wall = time.perf_counter() - t
+            good, worst = count_pairs(sol.lam, sol.residual, ref) if ref is not None else \
+                (int(np.sum(sol.residual <= RESID_TOL)), None)
+            out[name] = {"value": good / wall, "unit": UNIT, "wall_s": wall, "eigenpairs": good,
+                         "max_dlambda_rel": worst, "factor_ms": sol.diag["factor_ms"],
+                         "krylov_ms": sol.diag["krylov_ms"]}
+    out["mixed_vs_plain"] = out["mixed"]["value"] / max(out["plain_fp64"]["value"], 1e-300)
+    return out
 
 
 # batched alpha-sweep: 64 instances, grids (60,32), (100,50), (150,64) drawn
@@ -143,83 +264,99 @@ def run_c3(api, npoints=64):
     """The sweep in the plain FP64 form (one instance at a time, CUDA-core
     FP64 fronts) and in the mixed + batched form (complex64 fronts with
     tensor-core Schur updates and FP64 refinement, eight concurrent instances,
-    autotuned kernels): eigenpairs at resid <= 1e-10 per wall second.  With
+    autotuned kernels): eigenpairs at resid <= 1e-10 per wall second; the
+    mixed eigenvalues are compared with the plain ones point by point.  With
     several ranks the points are dealt round-robin to the GPUs (replicas) and
     the wall time is the slowest rank's."""
     from tailor_gb300 import replicas
     cases, points = c3_sweep_inputs(npoints)
-    out = {}
+    out, lam = {}, {}
     for name, kw in (("plain_fp64", dict(precision=0, workers=1, autotune=False)),
                      ("mixed_batched", dict(precision=1, workers=8, autotune=True))):
         replicas.barrier()
         t = time.perf_counter()
         r = replicas.sweep(cases, points, nev=8, ncv=32, raise_on_error=False, **kw)
         wall, _ = replicas.reduce_timing(time.perf_counter() - t, 0)
-        good = int(np.sum((r["residual"] >= 0) & (r["residual"] <= 1e-10)))
+        lam[name] = (r["lam"], r["residual"])
+        good = int(np.sum((r["residual"] >= 0) & (r["residual"] <= RESID_TOL)))
         d0 = next(d for d in r["rank_diag"] if d)
         out[name] = {"value": good / wall, "unit": UNIT, "wall_s": wall, "eigenpairs": good,
                      "failed_points": int(np.sum(r["status"] != 0)),
                      "workers": d0["workers"], "ranks": r["world"],
                      "solve_block": d0["solve_block"],
                      "tensor_core_schur": [1 - c for c in d0["cuda_core_schur"]]}
+    # mixed pairs count only where they match the plain FP64 eigenvalues
+    (lp, rp), (lm, rm) = lam["plain_fp64"], lam["mixed_batched"]
+    good, worst = 0, 0.0
+    for i in range(len(points)):
+        g, w = count_pairs(lm[i], rm[i], lp[i][rp[i] >= 0])
+        good, worst = good + g, max(worst, w if w is not None else 0.0)
+    out["mixed_batched"]["eigenpairs_matching_plain"] = good
+    out["mixed_batched"]["max_dlambda_rel_vs_plain"] = worst
     out["points"] = npoints
     out["grids"] = C3_GRIDS
     return out
 
 
-def cpu_reference_sample(steps=1, threads=None):
-    """The CPU path on a bounded sample (60 x 32 grid, C2 physics)."""
+def cpu_oracle_sample():
+    """The CPU path on a bounded sample: one 60 x 32 point of the sweep's
+    physics (Mach 0.7, alpha 2.21, Re 800, nev 8)."""
     from oracle.oracle import Oracle, boundary_rows, eigen_oracle, to_complex_blocks
-    case = c2_case(60, 32)
-    o = Oracle()
-    sigma = complex(C2["omega"].imag, -C2["omega"].real)
-    times, good = [], 0
-    for _ in range(steps):
-        t = time.perf_counter()
-        r = o.full(case)
-        A, B, _ = boundary_rows(case, r["metrics"], r["row_ptr"], r["col"],
-                                to_complex_blocks(r["mass"]), to_complex_blocks(r["spatial"]))
-        lam, _, res = eigen_oracle(r["row_ptr"], r["col"], A, B, case.nodes, sigma,
-                                   C2["nev"], tol=1e-12)
-        times.append(time.perf_counter() - t)
-        good = int(np.sum(res <= 1e-10))
-    return good, times, case
+    from tailor_gb300.neutral_sweep import c5_case
+    case = c5_case(60, 32, nev=C5_NEV)
+    case.physics = dataclasses.replace(case.physics, alpha=2.21, reynolds=800.0)
+    t = time.perf_counter()
+    r = Oracle().full(case)
+    A, B, _ = boundary_rows(case, r["metrics"], r["row_ptr"], r["col"],
+                            to_complex_blocks(r["mass"]), to_complex_blocks(r["spatial"]))
+    lam, _, res = eigen_oracle(r["row_ptr"], r["col"], A, B, case.nodes, 0j, C5_NEV, tol=1e-12)
+    sec = time.perf_counter() - t
+    return int(np.sum(res <= RESID_TOL)), sec
 
 
 def run_reference(args):
+    """The reference's CPU path cannot solve one point of the headline
+    workload within the step budget (its LU alone is 21.3 TFLOP at 300 x
+    192; the CPU oracle's 200 x 128 solve took 39 min on 8 cores), so this
+    arm prints no value, only the reason and a measured sample on a smaller
+    grid of the same physics, so that no ratio across different sizes is
+    formed."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    good, sec = cpu_oracle_sample()
     cores = os.cpu_count() or 1
-    good, times, case = cpu_reference_sample(steps=max(args.warmup, 0) and 1)
-    good, times, case = cpu_reference_sample(steps=args.steps)
-    sec = float(np.mean(times))
-    value = good / sec
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "impl": "reference",
+        "unavailable": "the CPU oracle (C assembly, zggev rows, SuperLU + ARPACK) cannot solve one "
+                       "300x192 point of the headline sweep within the step budget (21.3 TFLOP LU "
+                       "per point; its 200x128 solve took 39 min on 8 cores), so no value and no "
+                       "ratio; a 60x32 sample of the same physics is measured instead",
+        "metric": METRIC, "unit": UNIT, "higher_is_better": True,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-        "config": {"workload": "C2 family, bounded CPU sample 60x32 (nev 16, target 0.01-0.3i)",
-                   "ny": case.ny, "nz": case.nz},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "one 60x32 eigen solve per step: C oracle assembly, "
-                                   "zggev boundary rows, SuperLU+ARPACK"},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": {"workload": "C5 neutral-curve sweep, 300x192 (288000 unknowns) per point"},
+        "sample": {"value": good / sec, "unit": UNIT, "cores": cores, "kind": "port",
+                   "seconds": sec, "eigenpairs": good,
+                   "sample": "one 60x32 point of the sweep's physics (Mach 0.7, alpha 2.21, "
+                             "Re 800, nev 8): C oracle assembly, zggev boundary rows, SuperLU + "
+                             "ARPACK"},
     }
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", type=int, default=1, help="1 mixed (default), 0 FP64")
-    ap.add_argument("--plain", action="store_true", help="also time the plain FP64 form")
+    ap.add_argument("--plain-points", type=int, default=2,
+                    help="sweep points solved in the plain FP64 form for the comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-sweep", action="store_true", help="skip the 64-instance sweep")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the 64-instance C3 sweep")
+    ap.add_argument("--no-c2", action="store_true", help="skip the 200x128 record")
+    ap.add_argument("--no-learned", action="store_true", help="first point from a random start")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -232,110 +369,155 @@ def main():
         import torch.distributed as dist  # replicas only: barrier + max over ranks
         dist.init_process_group("gloo")
 
-    from tailor_gb300 import api
+    from tailor_gb300 import api, learned, replicas
     from tailor_gb300 import build as tb
+    from tailor_gb300.neutral_sweep import c5_case, c5_points
     tb.build()
-    case = c2_case()
+    ref = load_c5_reference()
+    pts = c5_points(snake=True)
+    # replicas: each rank walks the sweep from its own offset
+    off = (rank * len(pts)) // max(world, 1)
+    seq = [pts[(off + i) % len(pts)] for i in range(args.warmup + 3 * args.steps)]
+
+    proposal, train_s = (None, 0.0)
+    if not args.no_learned:
+        proposal, train_s = train_proposal(api, learned, pts)
+
+    case = c5_case()
     ev = Events()
     prob = api.Problem(case, device=local)
     stream = prob.lib.tlr_stream(prob.ctx)
-    for _ in range(args.warmup):
-        one_pass(prob, api, args.precision)
+    g = 0
+    for i in range(args.warmup):
+        c5_step(api, prob, seq[g], g == 0, proposal)
+        g += 1
 
     def barrier():
         if dist:
             dist.barrier()
 
-    # device-resident timing
+    # ---- device-resident timing
     clocks = ClockSampler()
     clocks.start()
     barrier()
     launches0 = prob.lib.tlr_kernel_launches()
     ev.record(ev.a, stream)
-    good_total, sols = 0, []
+    steps = []
     for _ in range(args.steps):
-        good, sol, op = one_pass(prob, api, args.precision)
-        good_total += good
-        sols.append(sol)
+        lam, res, diag = c5_step(api, prob, seq[g], g == 0, proposal)
+        steps.append((seq[g], lam, res, diag))
+        g += 1
     ev.record(ev.b, stream)
     ms = ev.elapsed_ms()
     launches = prob.lib.tlr_kernel_launches() - launches0
     barrier()
     clk = clocks.stop()
-    from tailor_gb300 import replicas
+    good_total, worst = 0, None
+    for (pt, lam, res, _) in steps:
+        rl = ref.get((round(pt[1], 9), round(pt[2], 6))) if ref else None
+        gd, w = count_pairs(lam, res, rl)
+        good_total = good_total + gd
+        worst = w if worst is None else (worst if w is None else max(worst, w))
     ms, good_total = replicas.reduce_timing(ms, good_total)  # slowest rank, all pairs
     value = good_total / (ms / 1e3)
 
-    # end to end through the public API with pinned host buffers
+    # ---- end to end through the public API with pinned host buffers
     gbytes, bbytes = case.grid.nbytes, case.baseflow.nbytes
     pg, pb = ev.pinned(gbytes), ev.pinned(bbytes)
     ctypes.memmove(pg, case.grid.ctypes.data, gbytes)
     ctypes.memmove(pb, case.baseflow.ctypes.data, bbytes)
     barrier()
     ev.record(ev.a, stream)
-    good_e2e = 0
+    e2e_steps = []
     for _ in range(args.steps):
         prob.check(prob.lib.tlr_load_fields(prob.ctx, pg, pb))
-        good, sol, _ = one_pass(prob, api, args.precision)
-        good_e2e += good
+        lam, res, _ = c5_step(api, prob, seq[g], False, proposal)
+        e2e_steps.append((seq[g], lam, res))
+        g += 1
     ev.record(ev.b, stream)
     ms_e2e = ev.elapsed_ms()
     barrier()
+    good_e2e = 0
+    for (pt, lam, res) in e2e_steps:
+        rl = ref.get((round(pt[1], 9), round(pt[2], 6))) if ref else None
+        good_e2e += count_pairs(lam, res, rl)[0]
     ms_e2e, good_e2e = replicas.reduce_timing(ms_e2e, good_e2e)
     e2e = good_e2e / (ms_e2e / 1e3)
-    d2h = C2["nev"] * (16 + 8)
+    d2h = C5_NEV * (16 + 8)
 
-    last = sols[-1].diag
+    # ---- plain FP64 on a stated subset of the same points (rank 0)
     plain = None
-    if args.plain and rank == 0:
-        t = time.perf_counter()
-        good, sol, _ = one_pass(prob, api, 0)
-        plain = {"value": good / (time.perf_counter() - t), "factor_ms": sol.diag["factor_ms"],
-                 "krylov_ms": sol.diag["krylov_ms"], "eigenpairs": good}
+    if rank == 0 and args.plain_points > 0:
+        sub = [s[0] for s in steps[:args.plain_points]]
+        ev.record(ev.a, stream)
+        pres = [plain_step(api, prob, pt) for pt in sub]
+        ev.record(ev.b, stream)
+        pms = ev.elapsed_ms()
+        pgood, pworst = 0, None
+        for pt, (lam, res, _) in zip(sub, pres):
+            rl = ref.get((round(pt[1], 9), round(pt[2], 6))) if ref else None
+            gd, w = count_pairs(lam, res, rl)
+            pgood = pgood + gd
+            pworst = w if pworst is None else (pworst if w is None else max(pworst, w))
+        pv = pgood / (pms / 1e3)
+        plain = {"value": pv, "unit": UNIT, "points": [[p[1], p[2]] for p in sub],
+                 "ms_per_point": pms / len(sub), "eigenpairs": pgood,
+                 "max_dlambda_rel": pworst,
+                 "factor_ms": [r[2]["factor_ms"] for r in pres],
+                 "krylov_ms": [r[2]["krylov_ms"] for r in pres],
+                 "combined_vs_plain": value / pv if pv > 0 else None}
+    last = steps[-1][3]
+    prob.close()
 
+    c2 = None if (args.no_c2 or rank != 0) else run_c2(api)
     sweep = None
     if not args.no_sweep:  # every rank takes its share of the points
         sweep = run_c3(api)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        g, times, c = cpu_reference_sample(steps=1)
-        cpu = {"value": g / times[0], "unit": UNIT, "cores": os.cpu_count() or 1,
-               "kind": "port",
-               "sample": "one 60x32 eigen solve (C2 physics, nev 16): C oracle assembly, "
-                         "zggev boundary rows, SuperLU+ARPACK, %.1f s" % times[0]}
-    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        gd, sec = cpu_oracle_sample()
+        cpu = {"value": gd / sec, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": "one 60x32 point of the sweep's physics (Mach 0.7, alpha 2.21, Re 800, "
+                         "nev 8): C oracle assembly, zggev boundary rows, SuperLU + ARPACK, "
+                         "%.1f s; a smaller grid than the headline" % sec}
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm = peaks.get("hbm_gbs", 6800.0)
-    # dominant kernel: the triangular solves (one CUDA graph per K^-1
-    # application), timed live with CUDA events around every graph replay.
-    csize = 8 if args.precision == 1 else 16
-    tri_bytes = last["factor_bytes"] + 2 * 5 * case.nodes * csize
-    tri_avg_ms = last["trisolve_ms"] / max(last["trisolves"], 1)
+    # dominant kernel: the multi-vector triangular solves (one CUDA graph per
+    # solve of the block's 8 vectors), CUDA events around every replay
+    nvec = last.get("block", 1)
+    tri_bytes = last["factor_bytes"] + 2 * nvec * 5 * case.nodes * 8
+    tri_ms = sum(s[3]["trisolve_ms"] for s in steps)
+    tri_n = sum(s[3]["trisolves"] for s in steps)
+    tri_avg_ms = tri_ms / max(tri_n, 1)
     achieved = tri_bytes / (tri_avg_ms * 1e-3) / 1e9 if tri_avg_ms > 0 else 0.0
     traffic = None
     tf = ROOT / "profiles" / "trisolve_traffic.json"
     if tf.exists():
-        t = json.loads(tf.read_text()).get("c64" if args.precision == 1 else "c128", {})
-        traffic = t.get("bytes_per_solve_c2")
+        traffic = json.loads(tf.read_text()).get("c64x8", {}).get("bytes_per_solve_c5")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c64 factor + c128 refinement" if args.precision == 1 else "c128",
-        "data": "synthetic",
-        "config": {"workload": "C2: 200x128 wavy-wall BL, nev 16, target 0.01-0.3i, alpha 1.8",
-                   "ny": case.ny, "nz": case.nz, "nev": C2["nev"],
-                   "form": "mixed" if args.precision == 1 else "plain-fp64", "ncv": NCV,
-                   "l2": "inputs and factors larger than L2 (no flush)",
+        "dtype": "c64 factor + c128 refinement", "data": "synthetic",
+        "config": {"workload": "C5 neutral-curve sweep: 300x192 (288000 unknowns), Mach 0.7, "
+                               "alpha x Re on 8x4 in [0.5,3.5]x[800,2400], snake order, one "
+                               "point per step, nev 8, target 0",
+                   "form": "learned + mixed + batched", "block": C5_BLOCK, "ncv": C5_NCV,
+                   "points": [[s[0][1], s[0][2]] for s in steps],
+                   "l2": "operator 1.8 GB and factor 10 GB per point, larger than L2 (no flush)",
                    "parallelism": "replicas" if world > 1 else "single"},
+        "parity": {"reference": "tests/golden/c5_300x192_plain_eigs.txt" if ref else None,
+                   "max_dlambda_rel": worst, "resid_tol": RESID_TOL, "dlambda_tol": DLAM_TOL},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": gbytes + bbytes,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,
-                     "kernel": "triangular solves (solve graph: k_blk_update, k_border_gemv, "
-                               "k_bwd_start, gathers)",
+                     "kernel": "8-vector triangular solves (solve graph: k_blk_update_m, "
+                               "k_border_gemv_m, k_bwd_start_m, k_sgather_m)",
                      "algorithmic_bytes": tri_bytes, "avg_ms": tri_avg_ms,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
         "factor": {"flops": last["factor_flops"], "ms": last["factor_ms"],
@@ -345,13 +527,15 @@ def main():
                                        "krylov_ms", "total_ms", "max_relative_error",
                                        "trisolve_ms", "trisolves", "ortho_ms", "dense_ms",
                                        "residual_ms")},
-        "cpu_baseline": cpu,
+        "learned": {"train_points": 48, "grid": [60, 32], "train_s": train_s}
+        if proposal is not None else None,
         "plain_fp64": plain,
+        "cpu_baseline": cpu,
+        "c2": c2,
         "sweep_c3": sweep,
     }
     if rank == 0:
         print(json.dumps(line))
-    prob.close()
     if dist:
         dist.destroy_process_group()
 

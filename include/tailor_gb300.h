@@ -193,9 +193,10 @@ typedef struct {
   double sigma_re, sigma_im; /* used when use_sigma != 0                    */
   int use_sigma;          /* 0: sigma = lambda target from omega            */
   const double *start;    /* optional complex [5N] host start vector        */
-  int cuda_core_schur;    /* mixed form: 0 (default) Schur updates on the
-                             tensor cores (tcgen05, 3xTF32); 1 on the CUDA
-                             cores (FP32 FMA)                                */
+  int cuda_core_schur;    /* 0 (default): Schur updates on the tensor cores
+                             (mixed form: tcgen05, 3xTF32; FP64 form: DMMA,
+                             mma.sync m8n8k4 f64); 1: on the CUDA cores
+                             (FP32 / FP64 FMA)                               */
   int solve_block;        /* mixed form: diagonal-block size of the
                              triangular solves, 128, 256 or 512 (0: 256)     */
   int refinement;         /* mixed form: 0 (default) classic iterative
@@ -220,6 +221,23 @@ typedef struct {
                              persistent cooperative launch with grid
                              barriers between steps (slower on GB300: 1.82
                              vs 1.23 ms per solve at 200 x 128)              */
+  int block;              /* Krylov block size: 0 or 1 (default) the single-
+                             vector Krylov-Schur of the reference's SLEPc
+                             solver; 2, 4 or 8 block Krylov-Schur, every
+                             operator application on `block` vectors at once
+                             (in the mixed form one triangular solve then
+                             reads the factor once for all of them).  ncv is
+                             rounded up to a multiple of block.  No
+                             counterpart in the reference.                  */
+  int nstart;             /* vectors in `start` ([nstart][5N] complex; 0:
+                             one when start is set); at most `block` are
+                             used, the rest of the start block is
+                             pseudo-random                                 */
+  int warm_start;         /* 1: without `start`, begin from the Ritz vectors
+                             of the previous solve on this context (a
+                             neighbouring point of a sweep), vector i of the
+                             start block the sum of Ritz vectors i, i +
+                             block, ...                                     */
 } tlr_solve_opts;
 
 typedef struct {
@@ -239,6 +257,8 @@ typedef struct {
   double residual_ms;     /* Ritz vectors and explicit residuals            */
   double refine_res[3];   /* mixed form: largest ||r|| / ||y|| seen after the
                              first solve, the first and the second correction */
+  int block;              /* Krylov block size used (vectors per triangular
+                             solve in the mixed form)                       */
 } tlr_eig_diag;
 
 /* lambda [nev] complex, residual [nev]; modes [nev][5N] complex or NULL. */
@@ -345,6 +365,14 @@ int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sweep_point *
  * k0 must be a multiple of w, w <= 64.  lbo/sbo: shared-memory descriptor
  * strides of the operand planes in bytes (0: the library's values).
  * Writes the updated front to out. */
+/* Test hook, no counterpart in the reference: x = K^-1 rhs through the
+ * context's complex64 factor (left by a mixed-form tlr_solve) for nvec
+ * host vectors rhs [nvec][5N] complex (rounded to complex64), written to
+ * out [nvec][5N].  multi = 1 solves all of them in one multi-vector solve
+ * (nvec 2, 4 or 8; every factor tile read once), multi = 0 one at a time;
+ * both give the same bits. */
+int tlr_factor_solve(tlr_ctx *ctx, int nvec, const double *rhs, double *out, int multi);
+
 int tlr_schur_update_c64(const float *front, int m, int p, int k0, int w, unsigned lbo,
                          unsigned sbo, float *out);
 

@@ -77,7 +77,8 @@ class SolveOpts(ctypes.Structure):
                 ("start", ctypes.c_void_p), ("cuda_core_schur", ctypes.c_int),
                 ("solve_block", ctypes.c_int), ("refinement", ctypes.c_int),
                 ("panel_width", ctypes.c_int), ("cluster_panel", ctypes.c_int),
-                ("persistent_solve", ctypes.c_int)]
+                ("persistent_solve", ctypes.c_int), ("block", ctypes.c_int),
+                ("nstart", ctypes.c_int), ("warm_start", ctypes.c_int)]
 
 
 class EigDiag(ctypes.Structure):
@@ -92,7 +93,8 @@ class EigDiag(ctypes.Structure):
                 ("solve_ms", ctypes.c_double), ("factor_bytes", ctypes.c_double),
                 ("trisolve_ms", ctypes.c_double), ("trisolves", ctypes.c_int),
                 ("ortho_ms", ctypes.c_double), ("dense_ms", ctypes.c_double),
-                ("residual_ms", ctypes.c_double), ("refine_res", ctypes.c_double * 3)]
+                ("residual_ms", ctypes.c_double), ("refine_res", ctypes.c_double * 3),
+                ("block", ctypes.c_int)]
 
 
 class GridClass(ctypes.Structure):
@@ -153,6 +155,7 @@ SIGNATURES = {
     "tlr_kernel_launches": ([], ctypes.c_longlong),
     "tlr_sweep": ([_P, _I, _P, _I, _P, _P, _P, _P, _P, _P], _I),
     "tlr_schur_update_c64": ([_P, _I, _I, _I, _I, ctypes.c_uint, ctypes.c_uint, _P], _I),
+    "tlr_factor_solve": ([_P, _I, _P, _P, _I], _I),
     "tlr_wait_selftest": ([_I, ctypes.c_uint, _P], _I),
     "tlr_pencil_create": ([_P, _I, _P, _P, _I, _P], _I),
     "tlr_fdq_rule": ([_I, _I, _I, ctypes.c_double, _P, _P, _P, _P, _P], _I),

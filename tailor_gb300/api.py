@@ -226,14 +226,21 @@ class EigenSolver:
               cuda_core_schur: bool = False, persistent_solve: bool = False,
               solve_block: int = 0, refinement: str = "ir",
               panel_width: int = 0, cluster_panel: int = 0,
-              fallback: bool = True) -> EigenSolution:
+              fallback: bool = True, block: int = 0,
+              warm_start: bool = False) -> EigenSolution:
         """With fallback, a mixed-form solve (precision 1) that fails to
         converge (or hits a singular pivot or a timed-out device wait) is
-        repeated in the plain FP64 form; diag["fallback"] is 1 then."""
+        repeated in the plain FP64 form; diag["fallback"] is 1 then.
+
+        start: one start vector [5N], or several [k][5N] (up to the block
+        size); block: Krylov block size (1, 2, 4 or 8; 0 = 1); warm_start:
+        without start, begin from the previous solve's Ritz vectors on this
+        problem."""
         kw = dict(nev=nev, ncv=ncv, tol=tol, max_it=max_it, sigma=sigma, start=start,
                   modes=modes, cuda_core_schur=cuda_core_schur,
                   persistent_solve=persistent_solve, solve_block=solve_block,
-                  refinement=refinement, panel_width=panel_width, cluster_panel=cluster_panel)
+                  refinement=refinement, panel_width=panel_width, cluster_panel=cluster_panel,
+                  block=block, warm_start=warm_start)
         if precision == 1 and fallback:
             try:
                 sol = self._solve(precision=1, **kw)
@@ -250,7 +257,7 @@ class EigenSolver:
 
     def _solve(self, nev, ncv, tol, max_it, precision, sigma, start, modes, cuda_core_schur,
                persistent_solve, solve_block, refinement, panel_width,
-               cluster_panel) -> EigenSolution:
+               cluster_panel, block=0, warm_start=False) -> EigenSolution:
         ph = self.p.case.physics
         k = nev or ph.nev
         opts = L.SolveOpts(nev, ncv, tol, max_it, precision,
@@ -259,12 +266,14 @@ class EigenSolver:
                            0 if sigma is None else 1, None, int(bool(cuda_core_schur)),
                            int(solve_block), 1 if refinement == "gmres" else 0,
                            int(panel_width), int(cluster_panel),
-                           int(bool(persistent_solve)))
+                           int(bool(persistent_solve)), int(block), 0,
+                           int(bool(warm_start)))
         if start is not None:
-            s = np.ascontiguousarray(np.stack([start.real, start.imag], -1),
-                                     dtype=np.float64)
+            st = np.atleast_2d(np.asarray(start, dtype=np.complex128))
+            s = np.ascontiguousarray(np.stack([st.real, st.imag], -1), dtype=np.float64)
             self.p._keep.append(s)
             opts.start = s.ctypes.data
+            opts.nstart = st.shape[0]
         lam = np.zeros((k, 2))
         res = np.zeros(k)
         vec = np.zeros((k, 5 * self.p.case.nodes, 2)) if modes else None
@@ -342,12 +351,15 @@ class SweepResult:
 def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
           autotune: bool = True, tol: float = 0.0, ncv: int = 0, max_it: int = 0,
           starts=None, device: int = 0, raise_on_error: bool = True,
-          fallback: bool = True) -> SweepResult:
+          fallback: bool = True, block: int = 0, warm_start: bool = False) -> SweepResult:
     """Batched alpha-sweep (tlr_sweep): points are (class index, alpha) or
     (class index, alpha, Re); each class is a Case (grid, base flow,
     physics) whose alpha (and Re when given) is overridden.  With fallback,
     points that fail in the mixed form are solved again, one at a time, in
-    the plain FP64 form (diag["fallback_points"] counts them)."""
+    the plain FP64 form (diag["fallback_points"] counts them).  block: the
+    Krylov block size of every solve; warm_start: each worker takes a
+    contiguous run of the points and starts every point but the run's first
+    from its predecessor's Ritz vectors (starts[i], when given, wins)."""
     lib = L.load()
     keep = []
     holder = Problem.__new__(Problem)  # reuse the rule marshalling
@@ -375,7 +387,7 @@ def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
         pts[i] = L.SweepPoint(int(c), complex(a).real, complex(a).imag, s, re_ov)
     k = nev or cases[0].physics.nev
     opts = L.SweepOpts(L.SolveOpts(k, ncv, tol, max_it, precision, 0.0, 0.0, 0, None, 0, 0, 0, 0,
-                                   0, 0),
+                                   0, 0, int(block), 0, int(bool(warm_start))),
                        workers, int(bool(autotune)), device)
     lam = np.zeros((max(npts, 1), k, 2))
     res = np.zeros((max(npts, 1), k))

@@ -71,7 +71,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         for s, log in zip(srcs, logs):
             print(f"== {s.name}\n{log}", file=sys.stderr)
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcublas", "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

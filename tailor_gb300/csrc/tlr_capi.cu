@@ -8,6 +8,7 @@
 #include <numeric>
 
 #include "tlr_internal.h"
+#include "tlr_lu.h"
 
 namespace tlr {
 
@@ -266,7 +267,6 @@ void tlr_ctx_destroy(tlr_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_factor(ctx);
   free_workspace(ctx);
-  free_blas(ctx);
   free_rule(ctx->xi);
   free_rule(ctx->eta);
   cudaFree(ctx->grid_c); cudaFree(ctx->base_c); cudaFree(ctx->base);
@@ -274,7 +274,7 @@ void tlr_ctx_destroy(tlr_ctx *ctx) {
   cudaFree(ctx->row_ptr); cudaFree(ctx->col); cudaFree(ctx->L); cudaFree(ctx->A);
   cudaFree(ctx->M); cudaFree(ctx->B); cudaFree(ctx->status); cudaFree(ctx->red);
   cudaFree(ctx->partial); cudaFree(ctx->bc_modes); cudaFree(ctx->bc_cond);
-  cudaFree(ctx->aff); cudaFree(ctx->wff);
+  cudaFree(ctx->aff); cudaFree(ctx->wff); cudaFree(ctx->wff_m);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -468,6 +468,38 @@ int tlr_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     return fail(ctx, TLR_ERR_WRONGSTATE,
                 "Boundary-constrained matrices are required before EPSSolve");
   return run_solve(ctx, opts, lambda, residual, modes, diag);
+}
+
+int tlr_factor_solve(tlr_ctx *ctx, int nvec, const double *rhs, double *out, int multi) {
+  if (!ctx || !rhs || !out || nvec < 1 || nvec > 8)
+    return ctx ? fail(ctx, TLR_ERR_ARG, "tlr_factor_solve: invalid arguments") : TLR_ERR_ARG;
+  Factor *F = ctx->factor;
+  if (!F || !F->factored || F->prec != 1)
+    return fail(ctx, TLR_ERR_WRONGSTATE,
+                "tlr_factor_solve needs a complex64 factorisation (a mixed-form tlr_solve)");
+  if (multi && nvec != 2 && nvec != 4 && nvec != 8)
+    return fail(ctx, TLR_ERR_ARG, "multi-vector solves take 2, 4 or 8 vectors");
+  cudaGetLastError();
+  const long long n = 5LL * ctx->nn;
+  std::vector<float2> h((size_t)nvec * n);
+  for (size_t i = 0; i < h.size(); ++i)
+    h[i] = make_float2((float)rhs[2 * i], (float)rhs[2 * i + 1]);
+  float2 *d = nullptr;
+  TLR_CUDA(ctx, cudaMalloc(&d, h.size() * sizeof(float2)));
+  int rc = cudaMemcpy(d, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice) ==
+                   cudaSuccess ? TLR_OK : TLR_ERR_CUDA;
+  if (!rc && multi) rc = F->solve_multi(ctx, d, nvec);
+  for (int v = 0; v < nvec && !rc && !multi; ++v) rc = F->solve(ctx, d + (size_t)v * n);
+  if (!rc && cudaMemcpy(h.data(), d, h.size() * sizeof(float2), cudaMemcpyDeviceToHost) !=
+                 cudaSuccess)
+    rc = TLR_ERR_CUDA;
+  cudaFree(d);
+  if (rc) return rc == TLR_ERR_CUDA ? fail(ctx, rc, "tlr_factor_solve: CUDA error") : rc;
+  for (size_t i = 0; i < h.size(); ++i) {
+    out[2 * i] = h[i].x;
+    out[2 * i + 1] = h[i].y;
+  }
+  return TLR_OK;
 }
 
 }  // extern "C"

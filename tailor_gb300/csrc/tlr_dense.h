@@ -98,18 +98,41 @@ inline void hessenberg(Mat &A, Mat &Z) {
 }
 
 // Hessenberg A -> upper triangular Schur form, Z <- Z Q.  Returns false
-// when an eigenvalue fails to converge in 60 iterations.
+// when the iteration does not converge (30 max(10, n) sweeps for one
+// deflation).  A subdiagonal entry is neglected by the conservative test
+// of Ahues and Tisseur (LAPACK Working Note 122, 1997), which keeps small
+// eigenvalues accurate next to large ones; projected matrices of shift-and-
+// invert hold both (theta of infinite eigenvalues is 0).
 inline bool schur(Mat &A, Mat &Z) {
   const int n = A.n;
-  const double eps = 2.220446049250313e-16;
-  int hi = n - 1, iter = 0, total = 0;
+  const double ulp = 2.220446049250313e-16;
+  const double smlnum = 2.2250738585072014e-308 * ((double)n / ulp);
+  auto c1 = [](cd z) { return std::abs(z.real()) + std::abs(z.imag()); };
+  const int itmax = 30 * std::max(10, n);
+  int hi = n - 1, iter = 0;
   while (hi > 0) {
     int l = hi;
     for (; l > 0; --l) {
-      const double s = std::abs(A(l - 1, l - 1)) + std::abs(A(l, l));
-      if (std::abs(A(l, l - 1)) <= eps * (s > 0 ? s : 1.0)) {
+      const double h21 = c1(A(l, l - 1));
+      if (h21 <= smlnum) {
         A(l, l - 1) = 0.0;
         break;
+      }
+      double tst = c1(A(l - 1, l - 1)) + c1(A(l, l));
+      if (tst == 0.0) {
+        if (l - 2 >= 0) tst += std::abs(A(l - 1, l - 2).real());
+        if (l + 1 <= hi) tst += std::abs(A(l + 1, l).real());
+      }
+      if (h21 <= ulp * tst) {
+        const double h12 = c1(A(l - 1, l));
+        const double ab = std::max(h21, h12), ba = std::min(h21, h12);
+        const double d1 = c1(A(l, l)), d2 = c1(A(l - 1, l - 1) - A(l, l));
+        const double aa = std::max(d1, d2), bb = std::min(d1, d2);
+        const double sum = aa + ab;
+        if (ba * (ab / sum) <= std::max(smlnum, ulp * (bb * (aa / sum)))) {
+          A(l, l - 1) = 0.0;
+          break;
+        }
       }
     }
     if (l == hi) {
@@ -117,7 +140,7 @@ inline bool schur(Mat &A, Mat &Z) {
       iter = 0;
       continue;
     }
-    if (++iter > 60 || ++total > 100 * n) return false;
+    if (++iter > itmax) return false;
     cd shift;
     if (iter % 10 == 0) {
       shift = A(hi, hi) + std::abs(A(hi, hi - 1));

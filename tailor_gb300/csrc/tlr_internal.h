@@ -100,8 +100,8 @@ struct tlr_ctx {
   // A_bc split into FP32 hi/lo pairs (re_hi, re_lo, im_hi, im_lo) for the
   // float-float refinement residual; rebuilt when the operator changes
   float4 *aff = nullptr, *wff = nullptr;  // wff: the iterate split the same way
+  float4 *wff_m = nullptr;                // the same for up to 8 iterates at once
   const tlr::Symbolic *shared_sym = nullptr;  // set by a sweep: reuse this analysis
-  void *blas = nullptr;                         // cuBLAS handle, created on first solve
   void *kws = nullptr;                          // Krylov workspace (tlr_krylov.cu)
   bool aff_valid = false;
   int *status = nullptr;     // [ST_COUNT]
@@ -145,10 +145,34 @@ int frobenius(tlr_ctx *ctx, const double2 *v, long long count, double *out);
 // FP32 pipe (about 48-bit significands); builds ctx->aff on first use.
 int residual_ff(tlr_ctx *ctx, const double2 *y, const double2 *w, double sr, double si,
                 double2 *r);
+// The same products on nr vectors at once (nr 1, 2, 4 or 8; vector v at
+// + v * 5 nn): each operator block is read once for all of them.
+int run_spmv_multi(tlr_ctx *ctx, int which, const double2 *x, double2 *y, int nr);
+int residual_ff_multi(tlr_ctx *ctx, const double2 *y, const double2 *w, double sr, double si,
+                      double2 *r, int nr);
+// allocate the buffers residual_ff_multi uses (outside any stream capture)
+int residual_ff_multi_prepare(tlr_ctx *ctx);
 // ||v||_2 into device memory out (scratch: ctx->partial_blocks doubles),
 // stream-ordered, no host synchronisation (capturable).
 int vec_norm_async(tlr_ctx *ctx, const double2 *v, long long count, double *scratch,
                    double *out);
+// Krylov basis primitives (tlr_kvec.cu), stream-ordered, results in device
+// memory.  V is column-major with leading dimension ldv; part holds
+// partial_blocks x nk complex partial sums, npart partial_blocks doubles.
+// h = V(:, 0:nk)^H w
+int kv_dot(tlr_ctx *ctx, long long n, const double2 *V, long long ldv, int nk,
+           const double2 *w, double2 *part, double2 *h);
+// w -= V(:, 0:nk) h; with norm, also *norm = ||w|| of the result
+int kv_update(tlr_ctx *ctx, long long n, const double2 *V, long long ldv, int nk,
+              const double2 *h, double2 *w, double *npart, double *norm);
+// out(:, 0:nl) = V(:, 0:nq) Y(0:nq, 0:nl); out must not overlap V
+int kv_combine(tlr_ctx *ctx, long long n, const double2 *V, long long ldv, int nq,
+               const double2 *Y, int ldy, int nl, double2 *out, long long ldo);
+// dst = src * s / *dnorm (dnorm null: dst = src * s; a zero norm gives zeros)
+int kv_scale(tlr_ctx *ctx, long long n, const double2 *src, const double *dnorm, double s,
+             double2 *dst);
+// y += a x
+int kv_axpy(tlr_ctx *ctx, long long n, double2 a, const double2 *x, double2 *y);
 // Launch the persistent solve's grid barrier on one CTA with a target it
 // cannot reach (bounded-wait self test).
 int grid_barrier_probe(unsigned *count, unsigned limit, int *err);
@@ -157,7 +181,6 @@ int prepare_ff(tlr_ctx *ctx);
 int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
               double *residual, double *modes, tlr_eig_diag *diag);
 void free_factor(tlr_ctx *ctx);
-void free_blas(tlr_ctx *ctx);
 void free_workspace(tlr_ctx *ctx);
 // Message returned by tlr_last_error(NULL) on the calling thread.
 void set_global_error(const std::string &msg);

@@ -13,8 +13,12 @@
 // precision 0 factors K in complex128; precision 1 factors it in complex64
 // and refines every application of K^-1 in FP64 against the FP64 operator
 // (r = y - A w + sigma B w) until ||r|| <= 1e-12 ||y||.
-#include <cublas_v2.h>
-
+//
+// No library on the path: Gram-Schmidt, basis combinations, norms and
+// scaling are this library's own kernels (tlr_kvec.cu).  An Arnoldi step
+// leaves its Gram-Schmidt coefficients and ||w|| in device memory and forms
+// the next basis vector on the device; the host reads the projected matrix
+// once per restart.
 #include <algorithm>
 #include <chrono>
 #include <climits>
@@ -77,15 +81,27 @@ struct Workspace {  // device buffers of the Krylov driver, owned by the context
   double2 *gv = nullptr;    // GMRES-IR: kGmresM + 1 basis vectors, kGmresM preconditioned
   double2 *zero = nullptr;  // a zero vector
   double *nscratch = nullptr;  // two norm reductions: 2 x (blocks + 1) doubles
-  double *hnorm = nullptr;     // pinned host copy of the two norms
-  double2 *hpin = nullptr;     // pinned: Gram-Schmidt coefficients (2 passes) and beta
-  double *ascratch = nullptr;  // norm reduction of the Arnoldi vector
+  double *hnorm = nullptr;     // pinned host copy of norms (4 doubles)
+  double2 *kpart = nullptr;    // per-CTA inner-product partials: blocks x (ncv + 1)
+  double *npart = nullptr;     // per-CTA norm partials: blocks
+  double2 *hd = nullptr;       // Gram-Schmidt coefficients, 2 passes x ncv x (ncv + 1)
+  double *betad = nullptr;     // ||w|| of every Arnoldi step: ncv + 1
+  double2 *ybuf = nullptr;     // restart / Ritz coefficients: ncv x ncv (device)
+  double *rnd = nullptr;       // eigen residual norms: ncv + 1 (device)
+  double2 *hpin = nullptr;     // pinned: 2 x ncv x (ncv + 1) coefficients, then betas
+  double2 *ypin = nullptr;     // pinned: ncv x ncv restart / Ritz coefficients
+  double *rnh = nullptr;       // pinned: ncv + 1 residual norms
+  int prev_ritz = 0;           // normalised Ritz vectors of the last solve left in tmp
+  // block operator buffers (up to Factor::kMaxRhs vectors each), on first use
+  double2 *blk = nullptr;      // W, Y, R, AW, BW blocks
+  float2 *blk32 = nullptr;
+  double *bnd = nullptr;       // 2 norms per vector (device)
+  double *bnh = nullptr;       // the same, pinned
 };
 
 struct Solver {
   tlr_ctx *ctx;
   Factor *F;
-  cublasHandle_t h = nullptr;
   long long n;
   double sr, si;
   double2 *V = nullptr, *w = nullptr, *y = nullptr, *r = nullptr, *aw = nullptr,
@@ -93,6 +109,16 @@ struct Solver {
   float2 *x32 = nullptr;
   double2 *gv = nullptr, *zero = nullptr;
   double *nscratch = nullptr, *hnorm = nullptr;
+  double2 *kpart = nullptr;
+  double *npart = nullptr;
+  // block operator: nb_rhs vectors per application
+  int nb_rhs = 1;
+  double2 *Wb = nullptr, *Yb = nullptr, *Rb = nullptr, *AWb = nullptr, *BWb = nullptr;
+  float2 *X32b = nullptr;
+  double *bnd = nullptr, *bnh = nullptr;
+  cudaGraphExec_t bref_exec = nullptr;
+  long long bref_kernels = 0;
+  cudaEvent_t brev[6] = {};
   bool gmres = false;  // GMRES-IR, or classic iterative refinement (default)
   int solves = 0, refine = 0;
   double refine_res[3] = {0, 0, 0};  // largest ||r|| / ||y|| after solve 1, 2, 3
@@ -100,10 +126,15 @@ struct Solver {
   int max_refine = 30;
 
 
+  // ||v|| on the host (one synchronisation); NaN when the device work failed
   double nrm(const double2 *v) {
-    double out = 0.0;
-    cublasDznrm2(h, (int)n, reinterpret_cast<const cuDoubleComplex *>(v), 1, &out);
-    return out;
+    const int nb = ctx->partial_blocks;
+    if (vec_norm_async(ctx, v, n, nscratch, nscratch + nb) ||
+        cudaMemcpyAsync(hnorm + 2, nscratch + nb, sizeof(double), cudaMemcpyDeviceToHost,
+                        ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+      return NAN;
+    return hnorm[2];
   }
 
   double solve_ms = 0.0;
@@ -155,7 +186,109 @@ struct Solver {
     for (cudaEvent_t e : evs) cudaEventDestroy(e);
     for (cudaEvent_t e : rev)
       if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : brev)
+      if (e) cudaEventDestroy(e);
     if (ref_exec) cudaGraphExecDestroy(ref_exec);
+    if (bref_exec) cudaGraphExecDestroy(bref_exec);
+  }
+
+  // The block refinement graph: nb_rhs right-hand sides Yb refined together
+  // into Wb (solve, two float-float corrections, FP64 residual and the two
+  // norms of every vector), each triangular solve one multi-vector solve
+  // that reads the factor once for all vectors.
+  int build_block_graph() {
+    cudaStream_t st = ctx->stream;
+    const int b = nb_rhs;
+    const long long bn = (long long)b * n;
+    const int blocks = blocks_for(bn, 256);
+    int rc = prepare_ff(ctx);
+    if (!rc) rc = F->solve_multi_prepare(ctx);
+    if (!rc) rc = residual_ff_multi_prepare(ctx);
+    if (rc) return rc;
+    for (auto &e : brev)
+      if (!e) TLR_CUDA(ctx, cudaEventCreate(&e));
+    TLR_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    {
+      CaptureScope cs;
+      k_to32<<<blocks, 256, 0, st>>>(bn, Yb, X32b);
+      rc = F->solve_multi(ctx, X32b, b, brev[0], brev[1], true);
+      if (!rc) rc = cudaMemsetAsync(Wb, 0, bn * sizeof(double2), st) == cudaSuccess ? 0 : TLR_ERR_CUDA;
+      if (!rc) k_add32<<<blocks, 256, 0, st>>>(bn, X32b, Wb);
+      for (int q = 1; q < 3 && !rc; ++q) {
+        rc = residual_ff_multi(ctx, Yb, Wb, sr, si, Rb, b);
+        if (rc) break;
+        k_to32<<<blocks, 256, 0, st>>>(bn, Rb, X32b);
+        rc = F->solve_multi(ctx, X32b, b, brev[2 * q], brev[2 * q + 1], true);
+        if (!rc) k_add32<<<blocks, 256, 0, st>>>(bn, X32b, Wb);
+      }
+      if (!rc) rc = run_spmv_multi(ctx, TLR_MAT_A, Wb, AWb, b);
+      if (!rc) rc = run_spmv_multi(ctx, TLR_MAT_B, Wb, BWb, b);
+      if (!rc) k_residual<<<blocks, 256, 0, st>>>(bn, Yb, AWb, BWb, sr, si, Rb);
+      const int nb = ctx->partial_blocks;
+      for (int v = 0; v < b && !rc; ++v) {
+        rc = vec_norm_async(ctx, Rb + (size_t)v * n, n, nscratch, bnd + 2 * v);
+        if (!rc) rc = vec_norm_async(ctx, Yb + (size_t)v * n, n, nscratch + nb + 1, bnd + 2 * v + 1);
+      }
+      if (!rc && cudaMemcpyAsync(bnh, bnd, sizeof(double) * 2 * b, cudaMemcpyDeviceToHost, st) !=
+                     cudaSuccess)
+        rc = TLR_ERR_CUDA;
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture (block refinement)");
+    size_t nn = 0;
+    bref_kernels = 0;
+    if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn > 0) {
+      std::vector<cudaGraphNode_t> nodes(nn);
+      if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+        for (size_t i = 0; i < nn; ++i) {
+          cudaGraphNodeType t;
+          if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+            ++bref_kernels;
+        }
+    }
+    const cudaError_t e2 = cudaGraphInstantiate(&bref_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaGraphInstantiate (block refinement)");
+    return TLR_OK;
+  }
+
+  // Wb = OP in for nb_rhs vectors in .. in + (nb_rhs - 1) n
+  int op_block(const double2 *in) {
+    const int b = nb_rhs;
+    int rc = run_spmv_multi(ctx, TLR_MAT_B, in, Yb, b);
+    if (rc) return rc;
+    if (F->prec == 0) {  // complex128 factor: one solve per vector
+      for (int v = 0; v < b; ++v)
+        if ((rc = apply_inverse(Yb + (size_t)v * n, Wb + (size_t)v * n))) return rc;
+      return TLR_OK;
+    }
+    if (!bref_exec && (rc = build_block_graph())) return rc;
+    TLR_CUDA(ctx, cudaGraphLaunch(bref_exec, ctx->stream));
+    count_launches(bref_kernels);
+    solves += 3 * b;
+    refine += 2 * b;
+    TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int q = 0; q < 3; ++q) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, brev[2 * q], brev[2 * q + 1]) == cudaSuccess) {
+        tri_ms += ms;
+        ++tri_n;
+      } else {
+        cudaGetLastError();  // not a failure of the solve: no timing this time
+      }
+    }
+    for (int v = 0; v < b; ++v) {
+      const double nr = bnh[2 * v], ny = bnh[2 * v + 1];
+      refine_res[2] = std::max(refine_res[2], nr / ny);
+      if (!(nr <= refine_tol * ny))  // rare: finish this vector on its own
+        if ((rc = refine_loop(Yb + (size_t)v * n, Wb + (size_t)v * n, ny))) return rc;
+    }
+    return TLR_OK;
   }
 
   int build_ref_graph(const double2 *in, double2 *out) {
@@ -251,9 +384,7 @@ struct Solver {
   int refine_gmres(const double2 *in, double2 *out, double ny) {
     cudaStream_t st = ctx->stream;
     double2 *Vg = gv, *Zg = gv + (size_t)(kGmresM + 1) * n;
-    auto Vj = [&](int j) { return reinterpret_cast<cuDoubleComplex *>(Vg + (size_t)j * n); };
     auto Zj = [&](int j) { return Zg + (size_t)j * n; };
-    const cuDoubleComplex one = {1.0, 0.0}, zero1 = {0.0, 0.0}, mone = {-1.0, 0.0};
     int rc;
     int inner = 0;
     for (int cycle = 0; inner < max_refine; ++cycle) {
@@ -265,9 +396,7 @@ struct Solver {
         beta = nrm(r);
         if (beta <= refine_tol * ny) return TLR_OK;
       }
-      const double inv = 1.0 / beta;
-      TLR_CUDA(ctx, cudaMemcpyAsync(Vg, r, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-      cublasZdscal(h, (int)n, &inv, Vj(0), 1);
+      if ((rc = kv_scale(ctx, n, r, nullptr, 1.0 / beta, Vg))) return rc;
       std::vector<cd> H((kGmresM + 1) * kGmresM, 0.0), g(kGmresM + 1, 0.0);
       std::vector<cd> cs(kGmresM), sn(kGmresM);
       g[0] = beta;
@@ -279,21 +408,17 @@ struct Solver {
         // caller's vector, so the product lives in aw
         double2 *kz = aw;
         if ((rc = residual_ff(ctx, zero, Zj(k), sr, si, kz))) return rc;
-        cublasZdscal(h, (int)n, &mone.x, reinterpret_cast<cuDoubleComplex *>(kz), 1);
+        if ((rc = kv_scale(ctx, n, kz, nullptr, -1.0, kz))) return rc;
         // two passes of classical Gram-Schmidt against V_0..V_k
         std::vector<double2> hc(k + 1), hc2(k + 1);
         for (int pass = 0; pass < 2; ++pass) {
-          cublasZgemv(h, CUBLAS_OP_C, (int)n, k + 1, &one, Vj(0), (int)n,
-                      reinterpret_cast<cuDoubleComplex *>(kz), 1, &zero1,
-                      reinterpret_cast<cuDoubleComplex *>(hv), 1);
-          cublasZgemv(h, CUBLAS_OP_N, (int)n, k + 1, &mone, Vj(0), (int)n,
-                      reinterpret_cast<cuDoubleComplex *>(hv), 1, &one,
-                      reinterpret_cast<cuDoubleComplex *>(kz), 1);
-          TLR_CUDA(ctx, cudaMemcpyAsync(pass ? hc2.data() : hc.data(), hv,
+          double2 *hk = hv + (size_t)pass * (kGmresM + 1);
+          if ((rc = kv_dot(ctx, n, Vg, n, k + 1, kz, kpart, hk))) return rc;
+          if ((rc = kv_update(ctx, n, Vg, n, k + 1, hk, kz, nullptr, nullptr))) return rc;
+          TLR_CUDA(ctx, cudaMemcpyAsync(pass ? hc2.data() : hc.data(), hk,
                                         sizeof(double2) * (k + 1), cudaMemcpyDeviceToHost, st));
         }
         const double hn = nrm(kz);
-        TLR_CUDA(ctx, cudaStreamSynchronize(st));
         for (int i = 0; i <= k; ++i)
           H[i * kGmresM + k] = cd(hc[i].x + hc2[i].x, hc[i].y + hc2[i].y);
         H[(k + 1) * kGmresM + k] = hn;
@@ -316,10 +441,7 @@ struct Solver {
           ++inner;
           break;
         }
-        const double hinv = 1.0 / hn;
-        TLR_CUDA(ctx, cudaMemcpyAsync(Vg + (size_t)(k + 1) * n, kz, n * sizeof(double2),
-                                      cudaMemcpyDeviceToDevice, st));
-        cublasZdscal(h, (int)n, &hinv, Vj(k + 1), 1);
+        if ((rc = kv_scale(ctx, n, kz, nullptr, 1.0 / hn, Vg + (size_t)(k + 1) * n))) return rc;
       }
       // x += Z y with H(0:k, 0:k) y = g(0:k)
       std::vector<cd> yk(k);
@@ -328,11 +450,9 @@ struct Solver {
         for (int j = i + 1; j < k; ++j) v -= H[i * kGmresM + j] * yk[j];
         yk[i] = v / H[i * kGmresM + i];
       }
-      for (int i = 0; i < k; ++i) {
-        const cuDoubleComplex c = {yk[i].real(), yk[i].imag()};
-        cublasZaxpy(h, (int)n, &c, reinterpret_cast<cuDoubleComplex *>(Zj(i)), 1,
-                    reinterpret_cast<cuDoubleComplex *>(out), 1);
-      }
+      for (int i = 0; i < k; ++i)
+        if ((rc = kv_axpy(ctx, n, make_double2(yk[i].real(), yk[i].imag()), Zj(i), out)))
+          return rc;
     }
     // out of iterations: report the final FP64 residual through the caller's
     // explicit eigen residual checks
@@ -450,16 +570,12 @@ void free_workspace(tlr_ctx *ctx) {
     cudaFree(ws->V); cudaFree(ws->w); cudaFree(ws->y); cudaFree(ws->r); cudaFree(ws->aw);
     cudaFree(ws->bw); cudaFree(ws->hv); cudaFree(ws->tmp); cudaFree(ws->x32);
     cudaFree(ws->gv); cudaFree(ws->zero); cudaFree(ws->nscratch); cudaFreeHost(ws->hnorm);
-    cudaFreeHost(ws->hpin); cudaFree(ws->ascratch);
+    cudaFree(ws->kpart); cudaFree(ws->npart); cudaFree(ws->hd); cudaFree(ws->betad);
+    cudaFree(ws->ybuf); cudaFree(ws->rnd); cudaFreeHost(ws->hpin); cudaFreeHost(ws->ypin);
+    cudaFreeHost(ws->rnh); cudaFree(ws->blk); cudaFree(ws->blk32); cudaFree(ws->bnd);
+    cudaFreeHost(ws->bnh);
     delete ws;
     ctx->kws = nullptr;
-  }
-}
-
-void free_blas(tlr_ctx *ctx) {
-  if (ctx && ctx->blas) {
-    cublasDestroy(static_cast<cublasHandle_t>(ctx->blas));
-    ctx->blas = nullptr;
   }
 }
 
@@ -483,15 +599,24 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   const double tol = o.tol > 0 ? o.tol : rcp.tol;
   const int max_it = o.max_it > 0 ? o.max_it : rcp.max_it;
   const long long n = 5LL * ctx->nn;
+  const int bsz = o.block == 2 || o.block == 4 || o.block == 8 ? o.block : 1;
+  if (o.block < 0 || o.block > 8 || (o.block > 1 && bsz == 1))
+    return fail(ctx, TLR_ERR_ARG, "Krylov block size must be 1, 2, 4 or 8");
   int ncv = o.ncv > 0 ? o.ncv : std::max(2 * nev, nev + 15);
-  ncv = (int)std::min<long long>(ncv, n - 1);
-  if (nev < 1 || nev >= ncv || !lambda || !residual)
+  if (bsz > 1) {  // a whole number of blocks, at least one beyond nev
+    ncv = std::max(ncv, nev + bsz);
+    ncv = (ncv + bsz - 1) / bsz * bsz;
+  }
+  ncv = (int)std::min<long long>(ncv, n - bsz);
+  if (nev < 1 || nev >= ncv || ncv % bsz || !lambda || !residual)
     return fail(ctx, TLR_ERR_ARG, "invalid eigen-solver dimensions");
   // lambda target = Im(omega) - i Re(omega)  (EigenSolver.cpp:46-48)
   const cd target(rcp.omega_im, -rcp.omega_re);
   const cd sigma = o.use_sigma ? cd(o.sigma_re, o.sigma_im) : target;
   const int prec = o.precision == 1 ? 1 : 0;
-  const bool tc = prec == 1 && !o.cuda_core_schur;
+  // Schur updates on the tensor cores: tcgen05 (3xTF32) for complex64
+  // fronts, DMMA (FP64 mma.sync) for complex128 fronts
+  const bool tc = !o.cuda_core_schur;
   const int sblock = prec == 0 ? 128
                      : (o.solve_block == 128 || o.solve_block == 512 ? o.solve_block : 256);
   const int pwidth =
@@ -553,19 +678,11 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   S.n = n;
   S.sr = sigma.real();
   S.si = sigma.imag();
-  if (!ctx->blas) {
-    cublasHandle_t hb = nullptr;
-    if (cublasCreate(&hb) != CUBLAS_STATUS_SUCCESS)
-      return fail(ctx, TLR_ERR_CUDA, "cublasCreate failed");
-    ctx->blas = hb;
-  }
-  S.h = static_cast<cublasHandle_t>(ctx->blas);
-  cublasSetStream(S.h, ctx->stream);
   const size_t vb = n * sizeof(double2);
   // Krylov workspace kept in the context: cudaFree synchronises the whole
   // device, which would serialise contexts that run concurrently
   Workspace *ws = static_cast<Workspace *>(ctx->kws);
-  if (ws && (ws->n != n || ws->ncv < ncv)) {
+  if (ws && (ws->n != n || ws->ncv < ncv || (bsz > 1 && !ws->blk))) {
     free_workspace(ctx);
     ws = nullptr;
   }
@@ -574,23 +691,41 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     ctx->kws = ws;
     ws->n = n;
     ws->ncv = ncv;
-    TLR_CUDA(ctx, cudaMalloc(&ws->V, vb * (ncv + 1)));
+    // ncv + block columns: the basis and the block of next vectors
+    TLR_CUDA(ctx, cudaMalloc(&ws->V, vb * (ncv + Factor::kMaxRhs)));
     TLR_CUDA(ctx, cudaMalloc(&ws->w, vb));
     TLR_CUDA(ctx, cudaMalloc(&ws->y, vb));
     TLR_CUDA(ctx, cudaMalloc(&ws->r, vb));
     TLR_CUDA(ctx, cudaMalloc(&ws->aw, vb));
     TLR_CUDA(ctx, cudaMalloc(&ws->bw, vb));
-    TLR_CUDA(ctx, cudaMalloc(&ws->hv, sizeof(double2) * (ncv + 1) * (ncv + 1)));
+    TLR_CUDA(ctx, cudaMalloc(&ws->hv, sizeof(double2) * 2 * (kGmresM + 1)));
     TLR_CUDA(ctx, cudaMalloc(&ws->tmp, vb * ncv));
     TLR_CUDA(ctx, cudaMalloc(&ws->x32, n * sizeof(float2)));
     TLR_CUDA(ctx, cudaMalloc(&ws->gv, vb * (2 * kGmresM + 1)));
     TLR_CUDA(ctx, cudaMalloc(&ws->zero, vb));
     TLR_CUDA(ctx, cudaMemset(ws->zero, 0, vb));
     TLR_CUDA(ctx, cudaMalloc(&ws->nscratch, sizeof(double) * 2 * (ctx->partial_blocks + 1)));
-    TLR_CUDA(ctx, cudaHostAlloc(&ws->hnorm, 2 * sizeof(double), cudaHostAllocDefault));
-    TLR_CUDA(ctx, cudaHostAlloc(&ws->hpin, sizeof(double2) * (2 * (ncv + 1) + 1),
+    TLR_CUDA(ctx, cudaHostAlloc(&ws->hnorm, 4 * sizeof(double), cudaHostAllocDefault));
+    const size_t hcount = (size_t)2 * ncv * (ncv + Factor::kMaxRhs);
+    TLR_CUDA(ctx, cudaMalloc(&ws->kpart,
+                             sizeof(double2) * ctx->partial_blocks * (ncv + Factor::kMaxRhs)));
+    if (bsz > 1) {
+      const size_t bv = (size_t)Factor::kMaxRhs * n;
+      TLR_CUDA(ctx, cudaMalloc(&ws->blk, sizeof(double2) * 5 * bv));
+      TLR_CUDA(ctx, cudaMalloc(&ws->blk32, sizeof(float2) * bv));
+      TLR_CUDA(ctx, cudaMalloc(&ws->bnd, sizeof(double) * 2 * Factor::kMaxRhs));
+      TLR_CUDA(ctx, cudaHostAlloc(&ws->bnh, sizeof(double) * 2 * Factor::kMaxRhs,
+                                  cudaHostAllocDefault));
+    }
+    TLR_CUDA(ctx, cudaMalloc(&ws->npart, sizeof(double) * ctx->partial_blocks));
+    TLR_CUDA(ctx, cudaMalloc(&ws->hd, sizeof(double2) * hcount));
+    TLR_CUDA(ctx, cudaMalloc(&ws->betad, sizeof(double) * (ncv + 1)));
+    TLR_CUDA(ctx, cudaMalloc(&ws->ybuf, sizeof(double2) * ncv * ncv));
+    TLR_CUDA(ctx, cudaMalloc(&ws->rnd, sizeof(double) * (ncv + 1)));
+    TLR_CUDA(ctx, cudaHostAlloc(&ws->hpin, sizeof(double2) * hcount + sizeof(double) * (ncv + 1),
                                 cudaHostAllocDefault));
-    TLR_CUDA(ctx, cudaMalloc(&ws->ascratch, sizeof(double) * (ctx->partial_blocks + 1)));
+    TLR_CUDA(ctx, cudaHostAlloc(&ws->ypin, sizeof(double2) * ncv * ncv, cudaHostAllocDefault));
+    TLR_CUDA(ctx, cudaHostAlloc(&ws->rnh, sizeof(double) * (ncv + 1), cudaHostAllocDefault));
   }
   S.V = ws->V;
   S.w = ws->w;
@@ -605,21 +740,66 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   S.zero = ws->zero;
   S.nscratch = ws->nscratch;
   S.hnorm = ws->hnorm;
+  S.kpart = ws->kpart;
+  S.npart = ws->npart;
   S.gmres = o.refinement == 1;
+  S.nb_rhs = bsz;
+  if (bsz > 1) {
+    const size_t bv = (size_t)Factor::kMaxRhs * n;
+    S.Wb = ws->blk;
+    S.Yb = ws->blk + bv;
+    S.Rb = ws->blk + 2 * bv;
+    S.AWb = ws->blk + 3 * bv;
+    S.BWb = ws->blk + 4 * bv;
+    S.X32b = ws->blk32;
+    S.bnd = ws->bnd;
+    S.bnh = ws->bnh;
+  }
 
-  std::vector<double2> v0(n);
-  if (o.start) {
-    for (long long i = 0; i < n; ++i) v0[i] = make_double2(o.start[2 * i], o.start[2 * i + 1]);
-  } else {
-    fill_start(v0, 0x5eed0001ull);
-  }
-  TLR_CUDA(ctx, cudaMemcpyAsync(S.V, v0.data(), vb, cudaMemcpyHostToDevice, ctx->stream));
+  // ---- start block: the caller's vectors, or the previous solve's Ritz
+  // vectors (warm start), completed with pseudo-random vectors, then
+  // orthonormalised in order (two passes of classical Gram-Schmidt)
   {
-    double nv = S.nrm(S.V);
-    if (!(nv > 0)) return fail(ctx, TLR_ERR_ARG, "start vector is zero");
-    const double inv = 1.0 / nv;
-    cublasZdscal(S.h, (int)n, &inv, reinterpret_cast<cuDoubleComplex *>(S.V), 1);
+    std::vector<double2> v0(n);
+    int have = 0;
+    const int given = o.start ? std::max(1, o.nstart) : 0;
+    for (int v = 0; v < bsz; ++v) {
+      double2 *dst = S.V + (size_t)v * n;
+      if (v < given) {
+        const double *src = o.start + (size_t)2 * n * v;
+        for (long long i = 0; i < n; ++i) v0[i] = make_double2(src[2 * i], src[2 * i + 1]);
+        TLR_CUDA(ctx, cudaMemcpy(dst, v0.data(), vb, cudaMemcpyHostToDevice));
+        ++have;
+      } else if (!given && o.warm_start && ws->prev_ritz > 0 && v < ws->prev_ritz) {
+        // vector v = sum of the previous Ritz vectors i with i = v (mod block)
+        TLR_CUDA(ctx, cudaMemcpyAsync(dst, S.tmp + (size_t)v * n, vb, cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+        for (int q = v + bsz; q < ws->prev_ritz; q += bsz) {
+          const int rc = kv_axpy(ctx, n, make_double2(1.0, 0.0), S.tmp + (size_t)q * n, dst);
+          if (rc) return rc;
+        }
+        ++have;
+      } else {
+        fill_start(v0, 0x5eed0001ull + (unsigned long long)v * 0x9E3779B97F4A7C15ull);
+        TLR_CUDA(ctx, cudaMemcpy(dst, v0.data(), vb, cudaMemcpyHostToDevice));
+      }
+    }
+    (void)have;
+    for (int v = 0; v < bsz; ++v) {
+      double2 *dst = S.V + (size_t)v * n;
+      int rc = TLR_OK;
+      for (int pass = 0; pass < 2 && v > 0 && !rc; ++pass) {
+        rc = kv_dot(ctx, n, S.V, n, v, dst, S.kpart, ws->hd);
+        if (!rc) rc = kv_update(ctx, n, S.V, n, v, ws->hd, dst, S.npart, nullptr);
+      }
+      if (rc) return rc;
+      const double nv = S.nrm(dst);
+      if (!(nv > 0) || !std::isfinite(nv))
+        return fail(ctx, TLR_ERR_ARG, "start vector is zero or not finite");
+      if ((rc = kv_scale(ctx, n, dst, nullptr, 1.0 / nv, dst))) return rc;
+    }
   }
+  ws->prev_ritz = 0;  // tmp is reused below
   double maxerr = 0.0;
   const int nout = nev;
   // Ritz vectors x_i = V Q y_i, lambda_i = sigma + 1/theta_i and explicit
@@ -639,81 +819,95 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
         yh[(size_t)i * ncv + q] = make_double2(sacc.real(), sacc.imag());
       }
     }
-    double2 *yd = nullptr;
-    TLR_CUDA(ctx, cudaMallocAsync(&yd, yh.size() * sizeof(double2), ctx->stream));
-    TLR_CUDA(ctx, cudaMemcpyAsync(yd, yh.data(), yh.size() * sizeof(double2),
+    // the host writes the pinned stage only after the stream has drained
+    // every earlier upload from it (the expansion's synchronisation)
+    std::copy(yh.begin(), yh.end(), ws->ypin);
+    TLR_CUDA(ctx, cudaMemcpyAsync(ws->ybuf, ws->ypin, yh.size() * sizeof(double2),
                                   cudaMemcpyHostToDevice, ctx->stream));
-    const cuDoubleComplex one1 = {1.0, 0.0}, zero1 = {0.0, 0.0};
-    cublasZgemm(S.h, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, nout, ncv, &one1,
-                reinterpret_cast<cuDoubleComplex *>(S.V), (int)n,
-                reinterpret_cast<cuDoubleComplex *>(yd), ncv, &zero1,
-                reinterpret_cast<cuDoubleComplex *>(S.tmp), (int)n);
-    cudaFreeAsync(yd, ctx->stream);
-    maxerr = 0.0;
+    int rc = kv_combine(ctx, n, S.V, n, ncv, ws->ybuf, ncv, nout, S.tmp, n);
+    if (rc) return rc;
+    const int nb = ctx->partial_blocks;
     for (int i = 0; i < nout; ++i) {
       double2 *x = S.tmp + (size_t)i * n;
-      const double nx = S.nrm(x);
-      const double inv = 1.0 / nx;
-      cublasZdscal(S.h, (int)n, &inv, reinterpret_cast<cuDoubleComplex *>(x), 1);
+      if ((rc = vec_norm_async(ctx, x, n, S.nscratch, S.nscratch + nb))) return rc;
+      if ((rc = kv_scale(ctx, n, x, S.nscratch + nb, 1.0, x))) return rc;
       const cd lam = sigma + 1.0 / Tq(i, i);
-      int rc = run_spmv(ctx, TLR_MAT_A, x, S.aw);
-      if (rc) return rc;
+      if ((rc = run_spmv(ctx, TLR_MAT_A, x, S.aw))) return rc;
       if ((rc = run_spmv(ctx, TLR_MAT_B, x, S.bw))) return rc;
       { k_axmy<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, S.aw, S.bw, lam.real(),
                                                           lam.imag(), S.r); count_launches(); }
-      const double res = S.nrm(S.r) / std::abs(lam);
+      if ((rc = vec_norm_async(ctx, S.r, n, S.nscratch, ws->rnd + i))) return rc;
+    }
+    TLR_CUDA(ctx, cudaMemcpyAsync(ws->rnh, ws->rnd, sizeof(double) * nout,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    maxerr = 0.0;
+    for (int i = 0; i < nout; ++i) {
+      const cd lam = sigma + 1.0 / Tq(i, i);
+      const double res = ws->rnh[i] / std::abs(lam);
       lambda[2 * i] = lam.real();
       lambda[2 * i + 1] = lam.imag();
-      residual[i] = res;
-      maxerr = std::max(maxerr, res);
+      residual[i] = std::isfinite(res) ? res : INFINITY;
+      maxerr = std::max(maxerr, residual[i]);
     }
     residual_ms += ms_since(tf);
     return TLR_OK;
   };
   double tol_int = tol;
   int tighten = 0;
-  dense::Mat H(ncv + 1, ncv);
+  // Krylov decomposition OP V(:, 0:k) = V(:, 0:k+bsz) H(0:k+bsz, 0:k); the
+  // projected matrix H is (ncv + bsz) x ncv, block upper Hessenberg with
+  // lower bandwidth bsz during an expansion
+  dense::Mat H(ncv + bsz, ncv);
   int k = 0, nconv = 0, it = 0, reason = 0;
-  std::vector<cd> theta(ncv);
-  std::vector<cd> hcol(ncv + 1), hcol2(ncv + 1);
-  const cuDoubleComplex one = {1.0, 0.0}, zero = {0.0, 0.0}, mone = {-1.0, 0.0};
-  auto Vc = [&](int j) { return reinterpret_cast<cuDoubleComplex *>(S.V + (size_t)j * n); };
+  // device coefficient columns: pass p, column j at hd + (p * ncv + j) * ldh
+  const int ldh = ncv + Factor::kMaxRhs;
+  auto hcol = [&](int pass, int j) { return ws->hd + ((size_t)pass * ncv + j) * ldh; };
   while (true) {
     ++it;
-    // Arnoldi expansion k .. ncv-1
-    for (int j = k; j < ncv; ++j) {
-      int rc = S.op(S.V + (size_t)j * n, S.w);
+    // block Arnoldi expansion of columns k .. ncv-1: OP on bsz vectors at
+    // once, then every new vector orthogonalised in order against all
+    // earlier ones (two passes of classical Gram-Schmidt); nothing comes
+    // back to the host until the expansion is complete
+    for (int j0 = k; j0 < ncv; j0 += bsz) {
+      int rc = bsz == 1 ? S.op(S.V + (size_t)j0 * n, S.w)
+                        : S.op_block(S.V + (size_t)j0 * n);
       if (rc) return rc;
       const auto to = clock::now();
-      // two passes of classical Gram-Schmidt; coefficients and ||w|| land in
-      // pinned memory and the host waits once
-      double2 *h1 = ws->hpin, *h2 = ws->hpin + (ncv + 1), *hb = ws->hpin + 2 * (ncv + 1);
-      for (int pass = 0; pass < 2; ++pass) {
-        cublasZgemv(S.h, CUBLAS_OP_C, (int)n, j + 1, &one, Vc(0), (int)n,
-                    reinterpret_cast<cuDoubleComplex *>(S.w), 1, &zero,
-                    reinterpret_cast<cuDoubleComplex *>(S.hv), 1);
-        cublasZgemv(S.h, CUBLAS_OP_N, (int)n, j + 1, &mone, Vc(0), (int)n,
-                    reinterpret_cast<cuDoubleComplex *>(S.hv), 1, &one,
-                    reinterpret_cast<cuDoubleComplex *>(S.w), 1);
-        TLR_CUDA(ctx, cudaMemcpyAsync(pass ? h2 : h1, S.hv, sizeof(double2) * (j + 1),
-                                      cudaMemcpyDeviceToHost, ctx->stream));
+      for (int i = 0; i < bsz && !rc; ++i) {
+        const int j = j0 + i, nk = j + bsz;
+        double2 *w = bsz == 1 ? S.w : S.Wb + (size_t)i * n;
+        for (int pass = 0; pass < 2 && !rc; ++pass) {
+          rc = kv_dot(ctx, n, S.V, n, nk, w, S.kpart, hcol(pass, j));
+          if (!rc)
+            rc = kv_update(ctx, n, S.V, n, nk, hcol(pass, j), w, S.npart,
+                           pass ? ws->betad + j : nullptr);
+        }
+        if (!rc) rc = kv_scale(ctx, n, w, ws->betad + j, 1.0, S.V + (size_t)nk * n);
       }
-      {
-        const int nb = ctx->partial_blocks;
-        int rc2 = vec_norm_async(ctx, S.w, n, ws->ascratch, ws->ascratch + nb);
-        if (rc2) return rc2;
-        TLR_CUDA(ctx, cudaMemcpyAsync(&hb->x, ws->ascratch + nb, sizeof(double),
-                                      cudaMemcpyDeviceToHost, ctx->stream));
-      }
+      if (rc) return rc;
+      ortho_ms += ms_since(to);
+    }
+    if (k < ncv) {
+      const auto to = clock::now();
+      const size_t stride = (size_t)ncv * ldh;
+      double *hbeta = reinterpret_cast<double *>(ws->hpin + 2 * stride);
+      for (int pass = 0; pass < 2; ++pass)
+        TLR_CUDA(ctx, cudaMemcpyAsync(ws->hpin + pass * stride + (size_t)k * ldh, hcol(pass, k),
+                                      sizeof(double2) * (ncv - k) * ldh, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+      TLR_CUDA(ctx, cudaMemcpyAsync(hbeta + k, ws->betad + k, sizeof(double) * (ncv - k),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
       TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-      const double beta = hb->x;
-      for (int i = 0; i <= j; ++i) H(i, j) = cd(h1[i].x + h2[i].x, h1[i].y + h2[i].y);
-      H(j + 1, j) = beta;
-      if (!(beta > 0)) return fail(ctx, TLR_ERR_NOT_CONVERGED, "Arnoldi breakdown");
-      const double inv = 1.0 / beta;
-      TLR_CUDA(ctx, cudaMemcpyAsync(S.V + (size_t)(j + 1) * n, S.w, vb,
-                                    cudaMemcpyDeviceToDevice, ctx->stream));
-      cublasZdscal(S.h, (int)n, &inv, Vc(j + 1), 1);
+      for (int j = k; j < ncv; ++j) {
+        const double2 *h1 = ws->hpin + (size_t)j * ldh;
+        const double2 *h2 = ws->hpin + stride + (size_t)j * ldh;
+        for (int i = 0; i < j + bsz; ++i) H(i, j) = cd(h1[i].x + h2[i].x, h1[i].y + h2[i].y);
+        for (int i = j + bsz; i < ncv + bsz; ++i) H(i, j) = 0.0;
+        H(j + bsz, j) = hbeta[j];
+        if (!(hbeta[j] > 0) || !std::isfinite(hbeta[j]))
+          return fail(ctx, TLR_ERR_NOT_CONVERGED, "Arnoldi breakdown");
+      }
       ortho_ms += ms_since(to);
     }
     // projected problem: Schur form, wanted first
@@ -732,26 +926,32 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
         if (std::abs(T(q, q)) > std::abs(T(best, best))) best = q;
       for (int q = best - 1; q >= pos; --q) dense::swap_adjacent(T, Q, q);
     }
-    const double beta = std::abs(H(ncv, ncv - 1));
-    std::vector<cd> b(ncv);
-    for (int i = 0; i < ncv; ++i) b[i] = beta * Q(ncv - 1, i);
+    // residual rows of the decomposition in the Schur basis: E Q, E =
+    // H(ncv : ncv + bsz, 0 : ncv)
+    dense::Mat EQ(bsz, ncv);
+    for (int r = 0; r < bsz; ++r)
+      for (int i = 0; i < ncv; ++i) {
+        cd acc = 0.0;
+        for (int q = 0; q < ncv; ++q) acc += H(ncv + r, q) * Q(q, i);
+        EQ(r, i) = acc;
+      }
     auto count_conv = [&](double tl) {
       int c = 0;
       for (int i = 0; i < ncv; ++i) {
         const auto yv = dense::tri_eigvec(T, i);
-        cd dot = 0.0;
-        double ny = 0.0;
-        for (int q = 0; q <= i; ++q) {
-          dot += b[q] * yv[q];
-          ny += std::norm(yv[q]);
+        double ny = 0.0, nr = 0.0;
+        for (int q = 0; q <= i; ++q) ny += std::norm(yv[q]);
+        for (int r = 0; r < bsz; ++r) {
+          cd dot = 0.0;
+          for (int q = 0; q <= i; ++q) dot += EQ(r, q) * yv[q];
+          nr += std::norm(dot);
         }
-        if (std::abs(dot) / std::sqrt(ny) <= tl * std::abs(T(i, i))) ++c;
+        if (std::sqrt(nr / ny) <= tl * std::abs(T(i, i))) ++c;
         else break;
       }
       return c;
     };
     nconv = count_conv(tol_int);
-    for (int i = 0; i < ncv; ++i) theta[i] = T(i, i);
     dense_ms += ms_since(td);
     bool done = false;
     if (nconv >= nev) {
@@ -775,31 +975,38 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
       done = true;
     }
     if (done) break;
-    // thick restart
+    // thick restart: keep l Schur vectors (half of the unconverged part, as
+    // SLEPc), with ncv - l a multiple of the block size
     int l = nconv + (ncv - nconv) / 2;
-    l = std::max(1, std::min(l, ncv - 2));
-    std::vector<double2> qh((size_t)ncv * l);
+    if (bsz == 1) {
+      l = std::max(1, std::min(l, ncv - 2));
+    } else {
+      const int d = std::max(bsz, ((ncv - l) / bsz) * bsz);
+      l = std::max(1, ncv - d);
+    }
+    // the pinned stage is free: the expansion's synchronisation drained the
+    // stream after its last upload
     for (int j = 0; j < l; ++j)
-      for (int i = 0; i < ncv; ++i) qh[(size_t)j * ncv + i] = make_double2(Q(i, j).real(), Q(i, j).imag());
-    double2 *qd = nullptr;
-    TLR_CUDA(ctx, cudaMallocAsync(&qd, qh.size() * sizeof(double2), ctx->stream));
-    TLR_CUDA(ctx, cudaMemcpyAsync(qd, qh.data(), qh.size() * sizeof(double2),
+      for (int i = 0; i < ncv; ++i)
+        ws->ypin[(size_t)j * ncv + i] = make_double2(Q(i, j).real(), Q(i, j).imag());
+    TLR_CUDA(ctx, cudaMemcpyAsync(ws->ybuf, ws->ypin, sizeof(double2) * ncv * l,
                                   cudaMemcpyHostToDevice, ctx->stream));
-    cublasZgemm(S.h, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, l, ncv, &one, Vc(0), (int)n,
-                reinterpret_cast<cuDoubleComplex *>(qd), ncv, &zero,
-                reinterpret_cast<cuDoubleComplex *>(S.tmp), (int)n);
+    {
+      const int rc = kv_combine(ctx, n, S.V, n, ncv, ws->ybuf, ncv, l, S.tmp, n);
+      if (rc) return rc;
+    }
     TLR_CUDA(ctx, cudaMemcpyAsync(S.V, S.tmp, vb * l, cudaMemcpyDeviceToDevice, ctx->stream));
-    TLR_CUDA(ctx, cudaMemcpyAsync(S.V + (size_t)l * n, S.V + (size_t)ncv * n, vb,
+    TLR_CUDA(ctx, cudaMemcpyAsync(S.V + (size_t)l * n, S.V + (size_t)ncv * n, vb * bsz,
                                   cudaMemcpyDeviceToDevice, ctx->stream));
-    cudaFreeAsync(qd, ctx->stream);
-    dense::Mat Hn(ncv + 1, ncv);
+    dense::Mat Hn(ncv + bsz, ncv);
     for (int j = 0; j < l; ++j) {
       for (int i = 0; i < l; ++i) Hn(i, j) = T(i, j);
-      Hn(l, j) = b[j];
+      for (int r = 0; r < bsz; ++r) Hn(l + r, j) = EQ(r, j);
     }
     H = Hn;
     k = l;
   }
+  ws->prev_ritz = nout;  // tmp holds the normalised Ritz vectors
   const auto t2 = clock::now();
   if (modes)
     for (int i = 0; i < nout; ++i)
@@ -836,6 +1043,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     d.dense_ms = dense_ms;
     d.residual_ms = residual_ms;
     for (int q = 0; q < 3; ++q) d.refine_res[q] = S.refine_res[q];
+    d.block = bsz;
     *diag = d;
   }
   if (reason != 1) {

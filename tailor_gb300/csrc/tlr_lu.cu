@@ -685,6 +685,106 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// FP64 trailing update on the FP64 tensor cores (DMMA: mma.sync m8n8k4
+// f64; tcgen05 has no FP64 kind).  Same 64x64 complex tiles and tile list as
+// k_gemm.  The panel's K columns are staged KC at a time as separate real
+// and imaginary planes in shared memory (rows padded to 68 doubles: the
+// fragment loads of a half-warp hit 16 distinct banks); warp (wr, wc) owns
+// rows 16 wr .. +15 and columns 32 wc .. +31 of the tile, i.e. 2 x 4 real
+// 8x8 accumulator tiles for each of Re and Im.  A complex product is four
+// real products: Cr += Ar Br - Ai Bi, Ci += Ar Bi + Ai Br.
+__device__ __forceinline__ void dmma(double &d0, double &d1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+               : "+d"(d0), "+d"(d1)
+               : "d"(a), "d"(b));
+}
+
+__global__ void __launch_bounds__(256)
+    k_gemm_dmma(const int *__restrict__ fl, const int *__restrict__ prefix, int nf, int s, int w,
+                double2 *__restrict__ pool, const DevFront *__restrict__ fr) {
+  constexpr int KC = 16, LD = kTile + 4;
+  __shared__ double Ar[KC][LD], Ai[KC][LD], Br[KC][LD], Bi[KC][LD];
+  const int t = blockIdx.x;
+  int lo = 0, hi = nf;  // find the front owning tile t
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) / 2;
+    if (prefix[mid] <= t) lo = mid; else hi = mid;
+  }
+  const DevFront f = fr[fl[lo]];
+  const int m = f.m, k0 = s * w, ww = min(w, f.p - k0);
+  const int base = k0 + ww, ext = m - base;
+  const int nt = (ext + kTile - 1) / kTile;
+  const int lt = t - prefix[lo];
+  const int R0 = base + (lt % nt) * kTile, C0 = base + (lt / nt) * kTile;
+  double2 *F = pool + f.off;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wr = warp & 3, wc = warp >> 2;
+  const int g = lane >> 2, q = lane & 3;  // fragment row / column group, k index
+  double cr[2][4][2], ci[2][4][2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) cr[i][j][0] = cr[i][j][1] = ci[i][j][0] = ci[i][j][1] = 0.0;
+  for (int kk = 0; kk < ww; kk += KC) {
+    for (int x = threadIdx.x; x < KC * kTile; x += 256) {
+      const int r = x % kTile, k = x / kTile;
+      const int gr = R0 + r;
+      const double2 a = (gr < m && kk + k < ww) ? F[(long long)(k0 + kk + k) * m + gr]
+                                                : make_double2(0.0, 0.0);
+      Ar[k][r] = a.x;
+      Ai[k][r] = a.y;
+      const int cc = x / KC, kb = x % KC;
+      const int gc = C0 + cc;
+      const double2 b = (gc < m && kk + kb < ww) ? F[(long long)gc * m + k0 + kk + kb]
+                                                 : make_double2(0.0, 0.0);
+      Br[kb][cc] = b.x;
+      Bi[kb][cc] = b.y;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k4 = 0; k4 < KC; k4 += 4) {
+      double ar[2], ai[2], br[4], bi[4];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        ar[i] = Ar[k4 + q][16 * wr + 8 * i + g];
+        ai[i] = Ai[k4 + q][16 * wr + 8 * i + g];
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        br[j] = Br[k4 + q][32 * wc + 8 * j + g];
+        bi[j] = Bi[k4 + q][32 * wc + 8 * j + g];
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          dmma(cr[i][j][0], cr[i][j][1], ar[i], br[j]);
+          dmma(cr[i][j][0], cr[i][j][1], -ai[i], bi[j]);
+          dmma(ci[i][j][0], ci[i][j][1], ar[i], bi[j]);
+          dmma(ci[i][j][0], ci[i][j][1], ai[i], br[j]);
+        }
+    }
+    __syncthreads();
+  }
+  // accumulator element (g, 2 q + e) of the 8x8 tile (i, j)
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int gr = R0 + 16 * wr + 8 * i + g;
+    if (gr >= m) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int gc = C0 + 32 * wc + 8 * j + 2 * q + e;
+        if (gc < m) {
+          double2 &d = F[(long long)gc * m + gr];
+          d.x -= cr[i][j][e];
+          d.y -= ci[i][j][e];
+        }
+      }
+  }
+}
+
 // FP32 trailing update: 128x64 tiles, 256 threads, 8x4 complex register
 // tile per thread (rows tx + 16 i, columns ty + 16 j), K staged 16 at a time
 // through double-buffered shared memory.  Per k step a thread issues 12
@@ -1233,6 +1333,211 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---- multi-RHS triangular solves (complex64) --------------------------------
+// The solve steps above on NR right-hand sides at once.  Every CTA loads its
+// factor (or D_b) tile into registers once and applies it to all NR vectors,
+// so one solve of NR vectors streams the factor from HBM once instead of NR
+// times.  Vector r of x lives at x + r * xs, of work / work2 at + r * ws, and
+// its border partial sums at partial + r * ps.  Per vector, the arithmetic
+// and its order are those of the single-vector kernels, so every vector's
+// result is bitwise the single-vector solve's.
+
+template <int NR>
+__global__ void k_sgather_m(const int *__restrict__ fl, const DevFront *__restrict__ fr,
+                            const int *__restrict__ nodes, const int *__restrict__ perm,
+                            const int2 *__restrict__ cinv, const float2 *__restrict__ b,
+                            long long xs, float2 *__restrict__ work, long long ws) {
+  pdl_launch_dependents();
+  pdl_wait();
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= f.m) return;
+  long long src = -1;
+  if (i < f.p) {
+    const int q = perm[f.toff + i];
+    src = (long long)nodes[f.node_off + q / 5] * 5 + q % 5;
+  }
+  const int2 c = cinv[f.toff + i];
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const float2 *br = b + r * xs;
+    float2 *wr = work + r * ws;
+    float2 v = src >= 0 ? br[src] : czero<float2>();
+    if (c.x >= 0) v = cadd(v, wr[c.x]);
+    if (c.y >= 0) v = cadd(v, wr[c.y]);
+    wr[f.toff + i] = v;
+  }
+}
+
+template <int SW, int NR>
+__global__ void __launch_bounds__(256)
+    k_blk_update_m(const int *__restrict__ fl, int b, int backward, const float2 *__restrict__ pool,
+                   const DevFront *__restrict__ fr, float2 *__restrict__ work, long long ws,
+                   const int *__restrict__ nodes, float2 *__restrict__ x, long long xs) {
+  using C = float2;
+  __shared__ __align__(16) C vs[NR][SW];
+  __shared__ C red[NR][8][32];
+  pdl_launch_dependents();
+  const DevFront f = fr[fl[blockIdx.y]];
+  const int b0 = b * SW, b1 = min(f.p, b0 + SW), nb = b1 - b0;
+  const int lo = backward ? 0 : b1, hi = backward ? b0 : f.m;
+  const int r0 = lo + blockIdx.x * 32;
+  if (nb <= 0 || r0 >= hi) return;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int r = r0 + lane;
+  const C *F = pool + f.off + (long long)b0 * f.m;
+  constexpr int kQ = SW / 8;
+  const int q0 = wp * kQ;
+  const bool full = q0 + kQ <= nb;
+  C fv[kQ];
+  if (full && r < hi) {
+    const C *Fp = F + (long long)q0 * f.m + r;
+#pragma unroll
+    for (int k = 0; k < kQ; ++k, Fp += f.m) fv[k] = *Fp;
+  } else {
+#pragma unroll
+    for (int k = 0; k < kQ; ++k)
+      fv[k] = (r < hi && q0 + k < nb) ? F[(long long)(q0 + k) * f.m + r] : czero<C>();
+  }
+  pdl_wait();
+  for (int t = threadIdx.x; t < NR * nb; t += blockDim.x) {
+    const int v = t / nb, q = t - v * nb;
+    vs[v][q] = work[v * ws + f.toff + b0 + q];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int v = 0; v < NR; ++v) red[v][wp][lane] = dot_cols<C, kQ>(fv, vs[v] + q0, full, nb - q0);
+  __syncthreads();
+  if (r < hi)
+    for (int v = wp; v < NR; v += 8) {  // warp v finishes vector v
+      C *t = work + v * ws + f.toff;
+      C acc = t[r];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) acc = csub(acc, red[v][k][lane]);
+      t[r] = acc;
+      if (backward && r >= b0 - SW)
+        x[v * xs + (long long)nodes[f.node_off + r / 5] * 5 + r % 5] = acc;
+    }
+}
+
+template <int NR>
+__global__ void __launch_bounds__(256)
+    k_border_gemv_m(const int *__restrict__ fl, const float2 *__restrict__ pool,
+                    const DevFront *__restrict__ fr, const int *__restrict__ nodes,
+                    const float2 *__restrict__ x, long long xs, double2 *__restrict__ partial,
+                    long long ps, int nck, int pmax) {
+  using C = float2;
+  __shared__ __align__(16) C xsh[NR][kBC];
+  __shared__ C red[NR][8][32];
+  pdl_launch_dependents();
+  const int fq = blockIdx.z;
+  const DevFront f = fr[fl[fq]];
+  const int r0 = blockIdx.x * 32;
+  const int c0 = f.p + blockIdx.y * kBC;
+  if (r0 >= f.p || c0 >= f.m) return;
+  const int nc = min(kBC, f.m - c0);
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int r = r0 + lane;
+  constexpr int kQ = kBC / 8;
+  const int ka = wp * kQ;
+  const bool full = ka + kQ <= nc;
+  const C *F = pool + f.off + (long long)c0 * f.m + r;
+  C fv[kQ];
+  if (full && r < f.p) {
+    const C *Fp = F + (long long)ka * f.m;
+#pragma unroll
+    for (int k = 0; k < kQ; ++k, Fp += f.m) fv[k] = *Fp;
+  } else {
+#pragma unroll
+    for (int k = 0; k < kQ; ++k)
+      fv[k] = (r < f.p && ka + k < nc) ? F[(long long)(ka + k) * f.m] : czero<C>();
+  }
+  pdl_wait();
+  for (int t = threadIdx.x; t < NR * nc; t += blockDim.x) {
+    const int v = t / nc, k = t - v * nc;
+    const int c = c0 + k;
+    xsh[v][k] = x[v * xs + (long long)nodes[f.node_off + c / 5] * 5 + c % 5];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int v = 0; v < NR; ++v)
+    red[v][wp][lane] = r < f.p ? dot_cols<C, kQ>(fv, xsh[v] + ka, full, nc - ka) : czero<C>();
+  __syncthreads();
+  if (r < f.p)
+    for (int v = wp; v < NR; v += 8) {
+      C acc = czero<C>();
+#pragma unroll
+      for (int k = 0; k < 8; ++k) acc = cadd(acc, red[v][k][lane]);
+      partial[v * ps + ((long long)fq * nck + blockIdx.y) * pmax + r] = to64(acc);
+    }
+}
+
+template <int SW, int NR>
+__global__ void __launch_bounds__(256)
+    k_bwd_start_m(const int *__restrict__ fl, const DevFront *__restrict__ fr,
+                  const long long *__restrict__ inv_off, const float2 *__restrict__ dmat,
+                  const float2 *__restrict__ work, float2 *__restrict__ work2, long long ws,
+                  const double2 *__restrict__ partial, long long ps, int nck, int pmax,
+                  const int *__restrict__ nodes, float2 *__restrict__ x, long long xs) {
+  using C = float2;
+  static_assert(NR <= 8, "one warp per right-hand side finishes the rows");
+  __shared__ __align__(16) C zs[NR][SW];
+  __shared__ C red[NR][8][32];
+  pdl_launch_dependents();
+  const int fq = blockIdx.y, fid = fl[fq];
+  const DevFront f = fr[fid];
+  const int blk = blockIdx.x / (SW / 32), quarter = blockIdx.x % (SW / 32);
+  const int b0 = blk * SW, nb = min(SW, f.p - b0);
+  const int rr0 = quarter * 32;
+  if (nb <= 0 || rr0 >= nb) return;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int rr = rr0 + lane;
+  const C *Dm = dmat + inv_off[fid] + (long long)blk * SW * SW;
+  constexpr int kQ = SW / 8;
+  const int q0 = wp * kQ;
+  const bool full = q0 + kQ <= nb;
+  C dv[kQ];
+  if (full && rr < nb) {
+    const C *Dp = Dm + (long long)q0 * nb + rr;
+#pragma unroll
+    for (int k = 0; k < kQ; ++k, Dp += nb) dv[k] = *Dp;
+  } else {
+#pragma unroll
+    for (int k = 0; k < kQ; ++k)
+      dv[k] = (rr < nb && q0 + k < nb) ? Dm[(long long)(q0 + k) * nb + rr] : czero<C>();
+  }
+  pdl_wait();
+  const int r = b0 + rr;
+  // warp v (< NR) sums vector v's border partials for its rows, in chunk order
+  double2 s = make_double2(0, 0);
+  if (wp < NR && rr < nb) {
+    const int nchf = f.m > f.p ? (f.m - f.p + kBC - 1) / kBC : 0;
+    const double2 *pv = partial + wp * ps;
+#pragma unroll 4
+    for (int k = 0; k < nchf; ++k) {
+      const double2 p = pv[((long long)fq * nck + k) * pmax + r];
+      s.x += p.x;
+      s.y += p.y;
+    }
+  }
+  for (int t = threadIdx.x; t < NR * nb; t += blockDim.x) {
+    const int v = t / nb, q = t - v * nb;
+    zs[v][q] = work[v * ws + f.toff + b0 + q];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int v = 0; v < NR; ++v) red[v][wp][lane] = dot_cols<C, kQ>(dv, zs[v] + q0, full, nb - q0);
+  __syncthreads();
+  if (wp < NR && rr < nb) {
+    C w = czero<C>();
+#pragma unroll
+    for (int k = 0; k < 8; ++k) w = cadd(w, red[wp][k][lane]);
+    w = csub(w, from64<C>(s));
+    work2[wp * ws + f.toff + r] = w;
+    if (b0 + SW >= f.p) x[wp * xs + (long long)nodes[f.node_off + r / 5] * 5 + r % 5] = w;
+  }
+}
+
 // ---- persistent solve ------------------------------------------------------
 // The whole triangular solve as one cooperative launch: every phase of the
 // graph above (gather of a level, one block step, border product, backward
@@ -1656,6 +1961,7 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int pa
       (rc = alloc((void **)&d_inv_blocks, inv_blocks.size() * sizeof(int2))) ||
       (rc = alloc(&vec_a, (size_t)ctx->nn * 5 * csize)))
     return rc;
+  partial_stride = std::max(partial_elems, 1LL);
   TLR_CUDA(ctx, cudaMemcpy(d_inv_off, inv_off.data(), nf * sizeof(long long),
                            cudaMemcpyHostToDevice));
   TLR_CUDA(ctx, cudaMemcpy(d_ltiles, ltiles.data(), ltiles.size() * sizeof(int4),
@@ -1786,6 +2092,14 @@ void Factor::release() {
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   graph_exec = nullptr;
   pool = work = work2 = vec_a = nullptr;
+  for (auto &g : graph_m) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  cudaFree(work_m); cudaFree(work2_m); cudaFree(vec_m); cudaFree(partial_m);
+  work_m = work2_m = vec_m = nullptr;
+  partial_m = nullptr;
+  multi_cap = 0;
 }
 
 template <class C, int SW>
@@ -1873,6 +2187,9 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
               { k_gemm32<<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w,
                                                 reinterpret_cast<float2 *>(P), d_fronts); count_launches(); }
           }
+          else if (tensor_cores)
+            { k_gemm_dmma<<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w,
+                                                  reinterpret_cast<double2 *>(P), d_fronts); count_launches(); }
           else
             { k_gemm<C><<<S.tiles, 256, 0, st>>>(fl, d_sched + S.prefix_off, S.nf, s, w, P,
                                                d_fronts); count_launches(); }
@@ -2096,6 +2413,153 @@ int Factor::solve(tlr_ctx *ctx, void *x) {
   ev_used += 2;
   count_launches(graph_kernels);
   TLR_CUDA(ctx, cudaMemcpyAsync(x, vec_a, bytes, cudaMemcpyDeviceToDevice, st));
+  return TLR_OK;
+}
+
+// ---- multi-RHS solve (host) ---------------------------------------------------
+template <int SW, int NR>
+int Factor::solve_impl_m(tlr_ctx *ctx) {
+  cudaStream_t st = ctx->stream;
+  const float2 *P = static_cast<const float2 *>(pool);
+  float2 *W = static_cast<float2 *>(work_m);
+  float2 *W2 = static_cast<float2 *>(work2_m);
+  float2 *x = static_cast<float2 *>(vec_m);
+  const long long xs = (long long)sym.nn * 5, ws = sym.work_elems, ps = partial_stride;
+  for (size_t h = 0; h < levels.size(); ++h) {
+    const Level &L = levels[h];
+    const int *fl = d_sched + L.fronts_off;
+    TLR_CUDA(ctx, launch_pdl(h > 0, k_sgather_m<NR>, dim3(blocks_for(L.max_m, 128), L.nfronts),
+                             dim3(128), st, fl, (const DevFront *)d_fronts, (const int *)d_nodes,
+                             (const int *)d_perm, (const int2 *)d_cinv, (const float2 *)x, xs, W,
+                             ws));
+    count_launches();
+    for (int b = 0; b < (int)L.blk_nf.size(); ++b) {
+      const int rows = L.fwd_rows[b];
+      if (rows > 0) {
+        TLR_CUDA(ctx, launch_pdl(true, k_blk_update_m<SW, NR>,
+                                 dim3(blocks_for(rows, 32), L.blk_nf[b]), dim3(256), st, fl, b, 0,
+                                 P, (const DevFront *)d_fronts, W, ws, (const int *)d_nodes, x,
+                                 xs));
+        count_launches();
+      }
+    }
+  }
+  for (int h = (int)levels.size() - 1; h >= 0; --h) {
+    const Level &L = levels[h];
+    const int *fl = d_sched + L.fronts_off;
+    if (L.bmax > 0) {
+      const dim3 g(blocks_for(L.pmax, 32), L.nck_b, L.nfronts);
+      TLR_CUDA(ctx, launch_pdl(true, k_border_gemv_m<NR>, g, dim3(256), st, fl, P,
+                               (const DevFront *)d_fronts, (const int *)d_nodes, (const float2 *)x,
+                               xs, partial_m, ps, L.nck_b, L.pmax));
+      count_launches();
+    }
+    TLR_CUDA(ctx, launch_pdl(true, k_bwd_start_m<SW, NR>,
+                             dim3((unsigned)L.blk_nf.size() * (SW / 32), L.nfronts), dim3(256), st,
+                             fl, (const DevFront *)d_fronts, (const long long *)d_inv_off,
+                             static_cast<const float2 *>(dmat), (const float2 *)W, W2, ws,
+                             (const double2 *)partial_m, ps, L.nck_b, L.pmax,
+                             (const int *)d_nodes, x, xs));
+    count_launches();
+    for (int b = (int)L.blk_nf.size() - 1; b >= 1; --b) {
+      TLR_CUDA(ctx, launch_pdl(true, k_blk_update_m<SW, NR>,
+                               dim3(blocks_for(b * SW, 32), L.blk_nf[b]), dim3(256), st, fl, b, 1,
+                               P, (const DevFront *)d_fronts, W2, ws, (const int *)d_nodes, x, xs));
+      count_launches();
+    }
+  }
+  TLR_CUDA(ctx, cudaGetLastError());
+  return TLR_OK;
+}
+
+int Factor::solve_impl_m_dispatch(tlr_ctx *ctx, int nr) {
+  switch (sw * 16 + nr) {
+    case 128 * 16 + 2: return solve_impl_m<128, 2>(ctx);
+    case 128 * 16 + 4: return solve_impl_m<128, 4>(ctx);
+    case 128 * 16 + 8: return solve_impl_m<128, 8>(ctx);
+    case 256 * 16 + 2: return solve_impl_m<256, 2>(ctx);
+    case 256 * 16 + 4: return solve_impl_m<256, 4>(ctx);
+    case 256 * 16 + 8: return solve_impl_m<256, 8>(ctx);
+    default:
+      return fail(ctx, TLR_ERR_ARG,
+                  "multi-vector solves need 2, 4 or 8 vectors and diagonal blocks of 128 or 256");
+  }
+}
+
+int Factor::solve_multi_prepare(tlr_ctx *ctx) {
+  if (multi_cap >= kMaxRhs) return TLR_OK;
+  // buffers for up to kMaxRhs vectors, allocated once per factor
+  const size_t cs = sizeof(float2);
+  const size_t we = (size_t)std::max<long long>(sym.work_elems, 1);
+  TLR_CUDA(ctx, cudaMalloc(&work_m, (size_t)kMaxRhs * we * cs));
+  TLR_CUDA(ctx, cudaMalloc(&work2_m, (size_t)kMaxRhs * we * cs));
+  TLR_CUDA(ctx, cudaMalloc(&vec_m, (size_t)kMaxRhs * sym.nn * 5 * cs));
+  TLR_CUDA(ctx, cudaMalloc(&partial_m, (size_t)kMaxRhs * partial_stride * sizeof(double2)));
+  multi_cap = kMaxRhs;
+  return TLR_OK;
+}
+
+int Factor::solve_multi(tlr_ctx *ctx, void *x, int nr, cudaEvent_t a, cudaEvent_t b,
+                        bool capture) {
+  if (prec != 1 || nr < 2 || nr > kMaxRhs || persistent)
+    return fail(ctx, TLR_ERR_ARG, "multi-vector solves run on complex64 graph solves only");
+  if (multi_cap < kMaxRhs) {
+    if (capture) return fail(ctx, TLR_ERR_ARG, "multi-vector buffers must exist before capture");
+    const int rc = solve_multi_prepare(ctx);
+    if (rc) return rc;
+  }
+  const size_t bytes = (size_t)nr * sym.nn * 5 * sizeof(float2);
+  cudaStream_t st = ctx->stream;
+  TLR_CUDA(ctx, cudaMemcpyAsync(vec_m, x, bytes, cudaMemcpyDeviceToDevice, st));
+  if (capture) {  // inside the caller's capture: enqueue the kernels directly
+    if (a) TLR_CUDA(ctx, cudaEventRecordWithFlags(a, st, cudaEventRecordExternal));
+    const int rc = solve_impl_m_dispatch(ctx, nr);
+    if (rc) return rc;
+    if (b) TLR_CUDA(ctx, cudaEventRecordWithFlags(b, st, cudaEventRecordExternal));
+  } else {
+    if (!graph_m[nr]) {
+      TLR_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      int rc;
+      {
+        CaptureScope cs;
+        rc = solve_impl_m_dispatch(ctx, nr);
+      }
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(st, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture (multi solve)");
+      size_t nn = 0;
+      graph_m_kernels[nr] = 0;
+      if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn > 0) {
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+          for (size_t i = 0; i < nn; ++i) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+              ++graph_m_kernels[nr];
+          }
+      }
+      const cudaError_t e2 = cudaGraphInstantiate(&graph_m[nr], g, 0);
+      cudaGraphDestroy(g);
+      if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaGraphInstantiate (multi solve)");
+    }
+    if (ev_used + 2 > ev_pool.size()) {
+      cudaEvent_t e0, e1;
+      TLR_CUDA(ctx, cudaEventCreate(&e0));
+      TLR_CUDA(ctx, cudaEventCreate(&e1));
+      ev_pool.push_back(e0);
+      ev_pool.push_back(e1);
+    }
+    TLR_CUDA(ctx, cudaEventRecord(ev_pool[ev_used], st));
+    TLR_CUDA(ctx, cudaGraphLaunch(graph_m[nr], st));
+    TLR_CUDA(ctx, cudaEventRecord(ev_pool[ev_used + 1], st));
+    ev_used += 2;
+    count_launches(graph_m_kernels[nr]);
+  }
+  TLR_CUDA(ctx, cudaMemcpyAsync(x, vec_m, bytes, cudaMemcpyDeviceToDevice, st));
   return TLR_OK;
 }
 

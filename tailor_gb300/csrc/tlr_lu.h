@@ -41,7 +41,9 @@ struct Phase {
 struct Factor {
   Symbolic sym;
   int prec = 0;  // 0: complex128 fronts, 1: complex64 fronts
-  bool tensor_cores = true;  // complex64 Schur updates on tcgen05 (3xTF32)
+  // Schur updates on the tensor cores: tcgen05 (3xTF32) for complex64
+  // fronts, DMMA (FP64 mma.sync) for complex128 fronts; else CUDA cores
+  bool tensor_cores = true;
   // panel steps with at least this many fully summed rows left run over an
   // 8-CTA cluster (INT_MAX: never)
   int cluster_rows = kClusterPanelRows;
@@ -81,6 +83,26 @@ struct Factor {
   double take_solve_time(int *count);
   bool factored = false;
   double sigma_re = 0.0, sigma_im = 0.0;
+
+  // Multi-RHS solves (complex64 factors): nr vectors at once, every factor
+  // tile read once for all of them.  Buffers sized for multi_cap vectors,
+  // allocated on first use; one captured graph per vector count.
+  static constexpr int kMaxRhs = 8;
+  int multi_cap = 0;
+  long long partial_stride = 0;   // border partial sums of one vector
+  void *work_m = nullptr, *work2_m = nullptr, *vec_m = nullptr;
+  double2 *partial_m = nullptr;
+  cudaGraphExec_t graph_m[kMaxRhs + 1] = {};
+  long long graph_m_kernels[kMaxRhs + 1] = {};
+  // In-place x <- K^-1 x for nr vectors at x + r * 5 nn (complex64 only,
+  // 2 <= nr <= kMaxRhs; events a/b, when given, bracket the triangular
+  // solve and mark a capture into the caller's graph: no graph of our own).
+  int solve_multi(tlr_ctx *ctx, void *x, int nr, cudaEvent_t a = nullptr,
+                  cudaEvent_t b = nullptr, bool capture = false);
+  // allocate the multi-vector buffers (outside any stream capture)
+  int solve_multi_prepare(tlr_ctx *ctx);
+  template <int SW, int NR> int solve_impl_m(tlr_ctx *ctx);
+  int solve_impl_m_dispatch(tlr_ctx *ctx, int nr);
 
   int setup(tlr_ctx *ctx, int precision, int leaf, int solve_block = 0, int panel_width = 0);
   void release();

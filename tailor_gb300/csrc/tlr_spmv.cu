@@ -208,6 +208,151 @@ __global__ void __launch_bounds__(32 * kRowsPerCta)
   }
 }
 
+// The two products above on NR vectors at once (vector v at + v * n, n the
+// operator's scalar rows): each block of the operator is loaded once and
+// applied to all NR vectors.  Per vector, arithmetic and order are those of
+// the single-vector kernels.
+template <int NR>
+__global__ void __launch_bounds__(32 * kRowsPerCta)
+    k_bsr_spmv_m(int nrows, const int *__restrict__ row_ptr, const int *__restrict__ col,
+                 const double2 *__restrict__ val, const double2 *__restrict__ x,
+                 double2 *__restrict__ y, long long n) {
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * kRowsPerCta + (threadIdx.x >> 5);
+  if (row >= nrows) return;
+  const int c = lane % 5;
+  const bool active = lane < 25;
+  double ar[NR], ai[NR];
+#pragma unroll
+  for (int v = 0; v < NR; ++v) ar[v] = ai[v] = 0.0;
+  const int k0 = row_ptr[row], k1 = row_ptr[row + 1];
+  int k = k0;
+  for (; k + 4 <= k1; k += 4) {
+    double2 a[4];
+    int cc[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      cc[u] = col[k + u];
+      a[u] = active ? __ldcs(val + (size_t)(k + u) * 25 + lane) : make_double2(0, 0);
+    }
+#pragma unroll
+    for (int v = 0; v < NR; ++v) {
+      double2 xv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        xv[u] = active ? x[v * n + (size_t)cc[u] * 5 + c] : make_double2(0, 0);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        ar[v] = fma(a[u].x, xv[u].x, ar[v]);
+        ar[v] = fma(-a[u].y, xv[u].y, ar[v]);
+        ai[v] = fma(a[u].x, xv[u].y, ai[v]);
+        ai[v] = fma(a[u].y, xv[u].x, ai[v]);
+      }
+    }
+  }
+  for (; k < k1; ++k) {
+    const int cc = col[k];
+    const double2 a = active ? __ldcs(val + (size_t)k * 25 + lane) : make_double2(0, 0);
+#pragma unroll
+    for (int v = 0; v < NR; ++v) {
+      const double2 xv = active ? x[v * n + (size_t)cc * 5 + c] : make_double2(0, 0);
+      ar[v] = fma(a.x, xv.x, ar[v]);
+      ar[v] = fma(-a.y, xv.y, ar[v]);
+      ai[v] = fma(a.x, xv.y, ai[v]);
+      ai[v] = fma(a.y, xv.x, ai[v]);
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NR; ++v) {
+    double sr = ar[v], si = ai[v];
+#pragma unroll
+    for (int d = 1; d < 5; ++d) {
+      sr += __shfl_down_sync(0xffffffffu, ar[v], d);
+      si += __shfl_down_sync(0xffffffffu, ai[v], d);
+    }
+    if (active && c == 0) y[v * n + (size_t)row * 5 + lane / 5] = make_double2(sr, si);
+  }
+}
+
+template <int NR>
+__global__ void __launch_bounds__(32 * kRowsPerCta)
+    k_residual_ff_m(int nrows, const int *__restrict__ row_ptr, const int *__restrict__ col,
+                    const float4 *__restrict__ aff, const double2 *__restrict__ B,
+                    const float4 *__restrict__ wff, const double2 *__restrict__ w,
+                    const double2 *__restrict__ y, double sr, double si, double2 *__restrict__ r,
+                    long long n) {
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * kRowsPerCta + (threadIdx.x >> 5);
+  if (row >= nrows) return;
+  const int c = lane % 5;
+  const bool active = lane < 25;
+  float rh[NR], rl[NR], ih[NR], il[NR];
+#pragma unroll
+  for (int v = 0; v < NR; ++v) rh[v] = rl[v] = ih[v] = il[v] = 0.f;
+  const int k0 = row_ptr[row], k1 = row_ptr[row + 1];
+  constexpr int kU = NR >= 4 ? 2 : 4;
+  for (int k = k0; k < k1; k += kU) {
+    float4 a[kU];
+    int cc[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const bool ok = active && k + u < k1;
+      cc[u] = ok ? col[k + u] : 0;
+      a[u] = ok ? __ldcs(aff + (size_t)(k + u) * 25 + lane) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int v = 0; v < NR; ++v) {
+      float4 xv[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u)
+        xv[u] = (active && k + u < k1) ? wff[v * n + (size_t)cc[u] * 5 + c]
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        ff_mac(rh[v], rl[v], a[u].x, a[u].y, xv[u].x, xv[u].y);
+        ff_mac(rh[v], rl[v], -a[u].z, -a[u].w, xv[u].z, xv[u].w);
+        ff_mac(ih[v], il[v], a[u].x, a[u].y, xv[u].z, xv[u].w);
+        ff_mac(ih[v], il[v], a[u].z, a[u].w, xv[u].x, xv[u].y);
+      }
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NR; ++v) {
+#pragma unroll
+    for (int d = 1; d < 5; ++d) {
+      const float h1 = __shfl_down_sync(0xffffffffu, rh[v], d);
+      const float l1 = __shfl_down_sync(0xffffffffu, rl[v], d);
+      const float h2 = __shfl_down_sync(0xffffffffu, ih[v], d);
+      const float l2 = __shfl_down_sync(0xffffffffu, il[v], d);
+      if (c == 0) {
+        ff_add(rh[v], rl[v], h1, l1);
+        ff_add(ih[v], il[v], h2, l2);
+      }
+    }
+  }
+  if (active && c == 0) {
+    const int rr = lane / 5;
+    const size_t i = (size_t)row * 5 + rr;
+    const double2 *Bb = B + (size_t)row * 25 + rr * 5;
+#pragma unroll
+    for (int v = 0; v < NR; ++v) {
+      double bx = 0.0, by = 0.0;
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {
+        const double2 b = Bb[q], wv = w[v * n + (size_t)row * 5 + q];
+        bx = fma(b.x, wv.x, bx);
+        bx = fma(-b.y, wv.y, bx);
+        by = fma(b.x, wv.y, by);
+        by = fma(b.y, wv.x, by);
+      }
+      const double ax = (double)rh[v] + (double)rl[v], ay = (double)ih[v] + (double)il[v];
+      const double2 yy = y[v * n + i];
+      r[v * n + i] =
+          make_double2(yy.x - (ax - (sr * bx - si * by)), yy.y - (ay - (sr * by + si * bx)));
+    }
+  }
+}
+
 }  // namespace
 
 int prepare_ff(tlr_ctx *ctx) {
@@ -249,6 +394,62 @@ int frobenius(tlr_ctx *ctx, const double2 *v, long long count, double *out) {
   TLR_CUDA(ctx, cudaMemcpyAsync(out, ctx->partial + blocks, sizeof(double),
                                 cudaMemcpyDeviceToHost, ctx->stream));
   TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TLR_OK;
+}
+
+int run_spmv_multi(tlr_ctx *ctx, int which, const double2 *x, double2 *y, int nr) {
+  const int nrows = ctx->nn;
+  const long long n = 5LL * ctx->nn;
+  const double2 *val;
+  const int *rp = ctx->row_ptr, *cl = ctx->col;
+  switch (which) {
+    case TLR_MAT_L: val = ctx->L; break;
+    case TLR_MAT_A: val = ctx->A; break;
+    case TLR_MAT_M: val = ctx->M; cl = nullptr; break;
+    case TLR_MAT_B: val = ctx->B; cl = nullptr; break;
+    default: return fail(ctx, TLR_ERR_ARG, "unknown matrix selector");
+  }
+  if (cl == nullptr) {
+    rp = ctx->row_ptr + (ctx->nn + 1);
+    cl = rp + (ctx->nn + 1);
+  }
+  const dim3 g(blocks_for(nrows, kRowsPerCta)), b(32 * kRowsPerCta);
+  switch (nr) {
+    case 1: k_bsr_spmv<<<g, b, 0, ctx->stream>>>(nrows, rp, cl, val, x, y); break;
+    case 2: k_bsr_spmv_m<2><<<g, b, 0, ctx->stream>>>(nrows, rp, cl, val, x, y, n); break;
+    case 4: k_bsr_spmv_m<4><<<g, b, 0, ctx->stream>>>(nrows, rp, cl, val, x, y, n); break;
+    case 8: k_bsr_spmv_m<8><<<g, b, 0, ctx->stream>>>(nrows, rp, cl, val, x, y, n); break;
+    default: return fail(ctx, TLR_ERR_ARG, "multi-vector products take 1, 2, 4 or 8 vectors");
+  }
+  count_launches();
+  TLR_CUDA(ctx, cudaGetLastError());
+  return TLR_OK;
+}
+
+int residual_ff_multi_prepare(tlr_ctx *ctx) {
+  int rc = prepare_ff(ctx);
+  if (rc) return rc;
+  if (!ctx->wff_m)
+    TLR_CUDA(ctx, cudaMalloc(&ctx->wff_m, (size_t)8 * 5 * ctx->nn * sizeof(float4)));
+  return TLR_OK;
+}
+
+int residual_ff_multi(tlr_ctx *ctx, const double2 *y, const double2 *w, double sr, double si,
+                      double2 *r, int nr) {
+  if (nr == 1) return residual_ff(ctx, y, w, sr, si, r);
+  if (!ctx->aff || !ctx->wff_m || !ctx->aff_valid)
+    return fail(ctx, TLR_ERR_ARG, "float-float residual buffers not prepared");
+  const long long n = 5LL * ctx->nn;
+  { k_split_ff<<<blocks_for(nr * n, 256), 256, 0, ctx->stream>>>(nr * n, w, ctx->wff_m); count_launches(); }
+  const dim3 g(blocks_for(ctx->nn, kRowsPerCta)), b(32 * kRowsPerCta);
+  switch (nr) {
+    case 2: k_residual_ff_m<2><<<g, b, 0, ctx->stream>>>(ctx->nn, ctx->row_ptr, ctx->col, ctx->aff, ctx->B, ctx->wff_m, w, y, sr, si, r, n); break;
+    case 4: k_residual_ff_m<4><<<g, b, 0, ctx->stream>>>(ctx->nn, ctx->row_ptr, ctx->col, ctx->aff, ctx->B, ctx->wff_m, w, y, sr, si, r, n); break;
+    case 8: k_residual_ff_m<8><<<g, b, 0, ctx->stream>>>(ctx->nn, ctx->row_ptr, ctx->col, ctx->aff, ctx->B, ctx->wff_m, w, y, sr, si, r, n); break;
+    default: return fail(ctx, TLR_ERR_ARG, "multi-vector residuals take 1, 2, 4 or 8 vectors");
+  }
+  count_launches();
+  TLR_CUDA(ctx, cudaGetLastError());
   return TLR_OK;
 }
 

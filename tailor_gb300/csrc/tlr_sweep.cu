@@ -5,7 +5,8 @@
 // Each grid class gets one symbolic analysis (computed once, copied into
 // every context of the class).  Worker threads each own one context per
 // class (its own CUDA stream, factor buffers, captured solve graph and
-// cuBLAS handle) and take points from a shared queue, so the kernels of
+// Krylov workspace) and take points from a shared queue (or, with warm
+// starts, a contiguous run of neighbouring points each), so the kernels of
 // several instances overlap on the GPU while each instance's Krylov-Schur
 // driver runs on its own host thread.  With autotuning on, the first
 // context of a class times the factorisation with both Schur-update kernels
@@ -207,11 +208,18 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
   std::atomic<int> next{0};
   std::atomic<int> failed{0};
   std::vector<std::string> point_err(npoints);
+  // warm starts: worker w takes the contiguous run of points
+  // [w npoints / workers, (w + 1) npoints / workers) in order, so each
+  // point starts from its predecessor's Ritz vectors on the same context;
+  // otherwise the workers share one queue
+  const bool runs = base.warm_start != 0;
   auto work = [&](int w) {
     cudaSetDevice(opts->device);
+    const int run_end = (int)((long long)(w + 1) * npoints / workers);
+    int run_next = (int)((long long)w * npoints / workers);
     while (true) {
-      const int i = next.fetch_add(1);
-      if (i >= npoints) break;
+      const int i = runs ? run_next++ : next.fetch_add(1);
+      if (i >= (runs ? run_end : npoints)) break;
       const tlr_sweep_point &pt = points[i];
       const int c = pt.grid_class;
       tlr_ctx *&ctx = ctxs[w][c];
@@ -232,6 +240,7 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
         so.cuda_core_schur = cs[c].cuda_core_schur;
         so.solve_block = cs[c].solve_block;
         so.start = pt.start;
+        so.nstart = pt.start ? 1 : 0;
         // concurrent contexts replay solve graphs: a cooperative grid per
         // worker could not count on having the GPU's SMs to itself
         if (workers > 1) so.persistent_solve = 0;

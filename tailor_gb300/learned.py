@@ -18,8 +18,8 @@ Two ways to use it:
   start vector close to the wanted invariant subspace lets the first
   Krylov basis hold it, so fewer restarts (operator applications) are
   needed.
-* shift: factor A - sigma' B at sigma' = centroid of the predicted
-  eigenvalues, ask for nev + extra eigenpairs around sigma' and keep the
+* shift: factor A - sigma' B at sigma' = the predicted eigenvalue nearest
+  the target, ask for nev + extra eigenpairs around sigma' and keep the
   nev nearest the target.  Accepted only when it provably equals the plain
   answer: every eigenvalue within R of the target (R = distance of the
   farthest kept one) lies inside the disk around sigma' that the solve
@@ -168,6 +168,7 @@ class Proposal:
     target: complex
     n_lam: int = N_SHIFTS          # predicted eigenvalues per point
     history: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    grid: tuple = ()               # (Ny, Nz) of the training solves, when known
 
     @classmethod
     def fit(cls, samples: list[Sample], target: complex, epochs=3000, batch=256, lr=1e-3,
@@ -198,6 +199,7 @@ class Proposal:
                             y_std=self.y_std, basis=self.basis,
                             target=np.array([self.target.real, self.target.imag]),
                             n_lam=np.array(self.n_lam), history=self.history,
+                            grid=np.array(self.grid, dtype=np.int64),
                             sha256=np.array(hashlib.sha256(params.tobytes()).hexdigest()))
 
     @classmethod
@@ -213,8 +215,9 @@ class Proposal:
             raise ValueError(f"{path}: {params.size} parameters for a network of {mlp.n_params}")
         mlp.set_params(params)
         t = z["target"]
+        grid = tuple(int(v) for v in z["grid"]) if "grid" in z else ()
         return cls(mlp, z["x_mean"], z["x_std"], z["y_mean"], z["y_std"], z["basis"],
-                   complex(t[0], t[1]), int(z["n_lam"]), z["history"])
+                   complex(t[0], t[1]), int(z["n_lam"]), z["history"], grid)
 
     def predict(self, points, bf16=True):
         X = np.array([features(*p) for p in points])
@@ -225,10 +228,38 @@ class Proposal:
         return lam, c
 
     def propose(self, point, nev):
+        """(sigma', start vector, predicted eigenvalues): sigma' is the
+        predicted eigenvalue nearest the target."""
         lam, c = self.predict([point])
-        sigma = complex(np.mean(lam[0, :nev]))
+        pred = lam[0, :nev]
+        sigma = complex(pred[int(np.argmin(np.abs(pred - self.target)))])
         start = self.basis @ c[0]
         return sigma, start, lam[0]
+
+    def start_on(self, case, point) -> np.ndarray:
+        """The predicted start vector at `point` on `case`'s grid.  When that
+        grid differs from the training grid, the vector is carried over by
+        the quintic spline operators of case preparation (tailor_gb300.
+        spline): not-a-knot along the wall-normal index, periodic along the
+        spanwise index, on the index coordinates that both synthetic grids
+        share (y = f(j / (Ny - 1)), z = L k / Nz)."""
+        _, start, _ = self.propose(point, self.n_lam)
+        if not self.grid or tuple(self.grid) == (case.ny, case.nz):
+            return start
+        return transfer_vector(start, self.grid, (case.ny, case.nz))
+
+
+def transfer_vector(v: np.ndarray, src: tuple, dst: tuple) -> np.ndarray:
+    """A natural-order vector [Nz][Ny][5] on the grid src = (Ny, Nz) onto
+    dst = (Ny', Nz') by quintic spline interpolation in the index
+    coordinates (wall-normal j / (Ny - 1) on [0, 1], spanwise k / Nz
+    periodic)."""
+    from . import spline
+    (ny0, nz0), (ny1, nz1) = src, dst
+    w_y = spline.bounded_matrix(np.linspace(0.0, 1.0, ny0), np.linspace(0.0, 1.0, ny1))
+    w_z = spline.periodic_matrix(nz0, np.arange(nz1) / nz1)
+    out = spline.tensor_apply(w_z, np.asarray(v).reshape(nz0, ny0, 5), w_y)
+    return np.ascontiguousarray(out.reshape(-1))
 
 
 def learned_solve(problem: api.Problem, proposal: Proposal, nev: int, precision=1,

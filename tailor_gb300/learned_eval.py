@@ -42,7 +42,11 @@ def main() -> None:
     ap.add_argument("--nev", type=int, default=8)
     ap.add_argument("--precision", type=int, default=1)
     ap.add_argument("--epochs", type=int, default=3000)
+    ap.add_argument("--modes", default="start,shift",
+                    help="learned modes to evaluate (comma-separated: start, shift)")
+    ap.add_argument("--out", default="", help="also write the JSON result to this file")
     a = ap.parse_args()
+    modes = [m for m in a.modes.split(",") if m]
     base = Physics(alpha=2.43, omega=0j, nev=a.nev)
     case = make_case(a.ny, a.nz, physics=base)
     tgt = target_lambda(base.omega)
@@ -57,7 +61,8 @@ def main() -> None:
                                     lr=1e-3, width=256, depth=4)
         out["fit_s"] = time.perf_counter() - t
         out["final_loss"] = float(prop.history[-1])
-        tot = {k: {"iterations": 0, "solves": 0, "wall_s": 0.0} for k in ("plain", "start", "shift")}
+        tot = {k: {"iterations": 0, "solves": 0, "wall_s": 0.0, "factorizations": 0}
+               for k in ["plain"] + modes}
         accepted = 0
         maxdev = 0.0
         for pt in draw(a.eval, 12):
@@ -67,13 +72,19 @@ def main() -> None:
             tot["plain"]["wall_s"] += time.perf_counter() - t
             tot["plain"]["iterations"] += plain.diag["iterations"]
             tot["plain"]["solves"] += plain.diag["solves"]
-            for mode in ("start", "shift"):
+            tot["plain"]["factorizations"] += 1
+            for mode in modes:
                 t = time.perf_counter()
                 sol, used, st = learned.learned_solve(prob, prop, a.nev, a.precision,
                                                       shift=(mode == "shift"))
                 tot[mode]["wall_s"] += time.perf_counter() - t
                 tot[mode]["iterations"] += st.get("iterations", 0) + st.get("iterations_plain", 0)
                 tot[mode]["solves"] += st.get("solves", 0) + st.get("solves_plain", 0)
+                # start mode factors once at the target, like the plain solve;
+                # shift mode factors at sigma' and, when rejected, again at
+                # the target
+                tot[mode]["factorizations"] += (1 if mode == "start" else
+                                                (1 if used else 2))
                 if mode == "shift":
                     accepted += int(used)
                 for lam in sol.lam:
@@ -81,9 +92,18 @@ def main() -> None:
         out["modes"] = tot
         out["shift_accepted"] = accepted
         out["max_rel_deviation_from_plain"] = maxdev
-    out["iterations_saved_start"] = tot["plain"]["iterations"] - tot["start"]["iterations"]
-    out["solves_saved_start"] = tot["plain"]["solves"] - tot["start"]["solves"]
+    for mode in modes:
+        out[f"iterations_saved_{mode}"] = tot["plain"]["iterations"] - tot[mode]["iterations"]
+        out[f"solves_saved_{mode}"] = tot["plain"]["solves"] - tot[mode]["solves"]
+    if "shift" in modes:
+        # a point solved by the plain method needs one factorisation at the
+        # target; shift mode needs one at sigma' and, on fallback, a second
+        out["refactorizations_saved_shift"] = (tot["plain"]["factorizations"]
+                                               - tot["shift"]["factorizations"])
     print(json.dumps(out))
+    if a.out:
+        with open(a.out, "w") as f:
+            json.dump(out, f, indent=1)
 
 
 if __name__ == "__main__":

@@ -24,6 +24,28 @@ from . import api
 from .case import Physics, make_case
 
 
+C5_GRID = (300, 192)
+
+
+def c5_case(ny: int = C5_GRID[0], nz: int = C5_GRID[1], nev: int = 8) -> "Case":
+    """The neutral-curve case: wavy wall (bump 0.05), Mach 0.7, target
+    lambda 0, nev 8, tol 1e-10 (alpha and Re are set per point)."""
+    ph = Physics(alpha=1.0, mach=0.7, omega=0j, nev=nev, tol=1e-10)
+    return make_case(ny, nz, amplitude=0.05, physics=ph)
+
+
+def c5_points(snake: bool = False):
+    """The 8 x 4 (alpha, Re) grid as (class 0, alpha, Re) points, Re-major.
+    snake: alpha runs up on even Re rows and down on odd ones, so that
+    consecutive points are neighbours (warm starts)."""
+    alphas = [float(a) for a in np.linspace(0.5, 3.5, 8)]
+    pts = []
+    for r, re in enumerate(np.linspace(800, 2400, 4)):
+        row = alphas if (not snake or r % 2 == 0) else alphas[::-1]
+        pts += [(0, a, float(re)) for a in row]
+    return pts
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ny", type=int, default=300)
@@ -33,10 +55,8 @@ def main() -> None:
     ap.add_argument("--plain-points", type=int, default=2)
     ap.add_argument("--ncv", type=int, default=32)
     a = ap.parse_args()
-    ph = Physics(alpha=1.0, mach=0.7, omega=0j, nev=a.nev, tol=1e-10)
-    case = make_case(a.ny, a.nz, amplitude=0.05, physics=ph)
-    points = [(0, float(al), float(re)) for re in np.linspace(800, 2400, 4)
-              for al in np.linspace(0.5, 3.5, 8)]
+    case = c5_case(a.ny, a.nz, a.nev)
+    points = c5_points()
     out = {"grid": [a.ny, a.nz], "points": len(points), "nev": a.nev, "ncv": a.ncv,
            "mach": 0.7}
     t = time.perf_counter()

@@ -1,6 +1,9 @@
-"""The CPU reference arm of bench.py: one bounded 60 x 32 sample through the
-oracle's CPU path (C assembly, LAPACK boundary rows, SuperLU + ARPACK), and
-the JSON line it prints.  Needs no GPU."""
+"""The CPU reference arm of bench.py.  The reference's CPU path cannot solve
+one point of the headline workload (300 x 192) within the step budget, so
+the arm prints the reason and no value (the driver then forms no ratio),
+with one measured 60 x 32 sample of the same physics through the oracle's
+CPU path (C assembly, LAPACK boundary rows, SuperLU + ARPACK).  Needs no
+GPU."""
 import json
 import os
 import subprocess
@@ -28,15 +31,13 @@ def test_reference_arm_line():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference"
-    assert d["metric"] == "eigenpairs/s at resid<=1e-10" and d["unit"] == "eigenpairs/s"
+    assert "300x192" in d["unavailable"] and "value" not in d
+    assert d["metric"].startswith("eigenpairs/s at resid<=1e-10") and d["unit"] == "eigenpairs/s"
     assert d["higher_is_better"] is True and d["steps"] == 1 and d["n_gpus"] == 1
-    assert d["value"] > 0 and d["ms_per_step"] > 0
-    cb = d["cpu_baseline"]
-    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
-    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}
+    smp = d["sample"]
+    assert smp["kind"] == "port" and smp["cores"] >= 1 and smp["value"] > 0
     # every pair of the 60 x 32 sample converged to the residual bar
-    assert d["value"] * d["ms_per_step"] / 1e3 == pytest.approx(16, rel=1e-9)
+    assert smp["eigenpairs"] == 8
 
 
 def test_reference_arm_other_ranks_are_silent():
