@@ -13,14 +13,14 @@ shift-and-invert Krylov-Schur solve, on one persistent context.
 The combined form (the line's value) is
   * mixed: complex64 multifrontal factor with tensor-core Schur updates,
     every K^-1 application refined in FP64 against the FP64 operator;
-  * batched: one context for the whole sweep (one symbolic analysis, captured
-    solve graphs), and block Krylov-Schur (8 vectors per operator
-    application: one triangular solve reads the factor once for all 8);
+  * batched: one context for the whole sweep (one symbolic analysis, one
+    set of factor buffers, captured solve and refinement graphs);
   * learned: the first point of the run starts from the learned proposal
     (an MLP trained, before the timed region, on eigenpairs the solver
     computed at 60 x 32 over the sweep's parameter range, its start vector
     carried to 300 x 192 by the spline operators); every later point starts
-    from its predecessor's 8 Ritz vectors.
+    from its predecessor's Ritz vectors (their sum: the wanted modes of the
+    neighbouring point).
 The plain FP64 form (complex128 factor, single-vector Krylov-Schur from a
 pseudo-random start, the reference's EigenSolver) solves a stated subset of
 the same points in the same run.
@@ -69,10 +69,12 @@ METRIC = "eigenpairs/s at resid<=1e-10 and |dlambda|/|lambda|<=1e-8"
 UNIT = "eigenpairs/s"
 RESID_TOL = 1e-10
 DLAM_TOL = 1e-8
-# combined form on the neutral-curve sweep
+# combined form on the neutral-curve sweep (block Krylov-Schur, --block,
+# needs more operator applications than it saves on this clustered
+# spectrum, so the default is the single-vector method)
 C5_NEV = 8
-C5_BLOCK = 8
-C5_NCV = 48
+C5_BLOCK = 1
+C5_NCV = 64
 PLAIN_NCV = 32
 # C2: mixed vs plain FP64 at 200 x 128
 C2 = dict(ny=200, nz=128, amplitude=0.08, alpha=1.8, omega=complex(0.3, 0.01), nev=16)
@@ -196,12 +198,16 @@ def train_proposal(api, learned, points, grid=(60, 32)):
 
 
 # ------------------------------------------------------------- C5 headline
-def c5_step(api, prob, point, first, proposal):
+def c5_ncv(block):
+    return C5_NCV if block == 1 else max(C5_NCV, 6 * block)
+
+
+def c5_step(api, prob, point, first, proposal, block=C5_BLOCK):
     """One sweep point in the combined form; returns (lam, residual, diag)."""
     _, alpha, re = point
     prob.set_physics(dataclasses.replace(prob.case.physics, alpha=alpha, reynolds=re))
     api.run_pipeline(prob)
-    kw = dict(nev=C5_NEV, ncv=C5_NCV, precision=1, block=C5_BLOCK)
+    kw = dict(nev=C5_NEV, ncv=c5_ncv(block), precision=1, block=block)
     if first:
         start = proposal.start_on(prob.case, (alpha, re, prob.case.physics.mach)) \
             if proposal is not None else None
@@ -357,6 +363,8 @@ def main():
     ap.add_argument("--no-sweep", action="store_true", help="skip the 64-instance C3 sweep")
     ap.add_argument("--no-c2", action="store_true", help="skip the 200x128 record")
     ap.add_argument("--no-learned", action="store_true", help="first point from a random start")
+    ap.add_argument("--block", type=int, default=C5_BLOCK, choices=[1, 2, 4, 8],
+                    help="Krylov block size of the combined form")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -389,7 +397,7 @@ def main():
     stream = prob.lib.tlr_stream(prob.ctx)
     g = 0
     for i in range(args.warmup):
-        c5_step(api, prob, seq[g], g == 0, proposal)
+        c5_step(api, prob, seq[g], g == 0, proposal, args.block)
         g += 1
 
     def barrier():
@@ -404,7 +412,7 @@ def main():
     ev.record(ev.a, stream)
     steps = []
     for _ in range(args.steps):
-        lam, res, diag = c5_step(api, prob, seq[g], g == 0, proposal)
+        lam, res, diag = c5_step(api, prob, seq[g], g == 0, proposal, args.block)
         steps.append((seq[g], lam, res, diag))
         g += 1
     ev.record(ev.b, stream)
@@ -431,7 +439,7 @@ def main():
     e2e_steps = []
     for _ in range(args.steps):
         prob.check(prob.lib.tlr_load_fields(prob.ctx, pg, pb))
-        lam, res, _ = c5_step(api, prob, seq[g], False, proposal)
+        lam, res, _ = c5_step(api, prob, seq[g], False, proposal, args.block)
         e2e_steps.append((seq[g], lam, res))
         g += 1
     ev.record(ev.b, stream)
@@ -484,8 +492,8 @@ def main():
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
         if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm = peaks.get("hbm_gbs", 6800.0)
-    # dominant kernel: the multi-vector triangular solves (one CUDA graph per
-    # solve of the block's 8 vectors), CUDA events around every replay
+    # dominant kernel: the triangular solves (one CUDA graph per solve of the
+    # block's vectors), CUDA events around every replay
     nvec = last.get("block", 1)
     tri_bytes = last["factor_bytes"] + 2 * nvec * 5 * case.nodes * 8
     tri_ms = sum(s[3]["trisolve_ms"] for s in steps)
@@ -495,7 +503,10 @@ def main():
     traffic = None
     tf = ROOT / "profiles" / "trisolve_traffic.json"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get("c64x8", {}).get("bytes_per_solve_c5")
+        # ncu DRAM bytes / algorithmic bytes of the same solve graph measured
+        # on a 100 x 50 capture, applied to this solve's algorithmic bytes
+        ratio = json.loads(tf.read_text()).get("c64", {}).get("ratio")
+        traffic = ratio * tri_bytes if ratio else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -504,7 +515,8 @@ def main():
         "config": {"workload": "C5 neutral-curve sweep: 300x192 (288000 unknowns), Mach 0.7, "
                                "alpha x Re on 8x4 in [0.5,3.5]x[800,2400], snake order, one "
                                "point per step, nev 8, target 0",
-                   "form": "learned + mixed + batched", "block": C5_BLOCK, "ncv": C5_NCV,
+                   "form": "learned + mixed + batched", "block": args.block,
+                   "ncv": c5_ncv(args.block),
                    "points": [[s[0][1], s[0][2]] for s in steps],
                    "l2": "operator 1.8 GB and factor 10 GB per point, larger than L2 (no flush)",
                    "parallelism": "replicas" if world > 1 else "single"},
@@ -516,8 +528,8 @@ def main():
         "clocks": clk,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,
-                     "kernel": "8-vector triangular solves (solve graph: k_blk_update_m, "
-                               "k_border_gemv_m, k_bwd_start_m, k_sgather_m)",
+                     "kernel": "triangular solves (solve graph: k_blk_update, k_border_gemv_pf, "
+                               "k_bwd_start, k_sgather; their _m variants for blocks)",
                      "algorithmic_bytes": tri_bytes, "avg_ms": tri_avg_ms,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
         "factor": {"flops": last["factor_flops"], "ms": last["factor_ms"],

@@ -5,8 +5,10 @@
 
 --stage assemble runs metrics, derivatives and --repeat assemblies;
 --stage bc adds the boundary rows; --stage spmv adds --repeat SpMVs of A_bc;
---stage solve adds one shift-and-invert eigen solve (nev from --nev).
-Prints one JSON line with the stage timings reported by the library.
+--stage solve adds one shift-and-invert eigen solve (nev from --nev,
+Krylov basis --ncv, block size --block); with --warm the solve is repeated
+at alpha + 0.43 from the first solve's Ritz vectors (a neighbouring sweep
+point).  Prints one JSON line with the stage timings reported by the library.
 """
 from __future__ import annotations
 
@@ -30,8 +32,15 @@ def main() -> None:
     ap.add_argument("--alpha", type=float, default=2.43)
     ap.add_argument("--omega-re", type=float, default=0.0)
     ap.add_argument("--omega-im", type=float, default=0.0)
+    ap.add_argument("--mach", type=float, default=0.5)
+    ap.add_argument("--reynolds", type=float, default=1000.0)
+    ap.add_argument("--ncv", type=int, default=0)
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--cuda-core-schur", action="store_true")
+    ap.add_argument("--warm", action="store_true")
     a = ap.parse_args()
-    case = make_case(a.ny, a.nz, physics=Physics(alpha=a.alpha, nev=a.nev,
+    case = make_case(a.ny, a.nz, physics=Physics(alpha=a.alpha, nev=a.nev, mach=a.mach,
+                                                 reynolds=a.reynolds,
                                                  omega=complex(a.omega_re, a.omega_im)))
     out = {"ny": a.ny, "nz": a.nz, "stage": a.stage}
     with api.Problem(case) as p:
@@ -46,10 +55,17 @@ def main() -> None:
             for _ in range(a.repeat):
                 p.spmv(api.TLR_MAT_A, x)
         if a.stage == "solve":
-            sol = api.EigenSolver(p).solve(precision=a.precision)
-            out["solve"] = {k: sol.diag[k] for k in ("factor_ms", "krylov_ms", "solves",
-                                                     "iterations", "max_relative_error",
-                                                     "solve_ms", "factor_bytes", "factor_flops")}
+            keys = ("factor_ms", "krylov_ms", "solves", "iterations", "max_relative_error",
+                    "solve_ms", "factor_bytes", "factor_flops", "trisolve_ms", "trisolves")
+            kw = dict(precision=a.precision, ncv=a.ncv, block=a.block,
+                      cuda_core_schur=a.cuda_core_schur)
+            sol = api.EigenSolver(p).solve(**kw)
+            out["solve"] = {k: sol.diag[k] for k in keys}
+            if a.warm:
+                p.set_alpha(a.alpha + 0.43)
+                api.run_pipeline(p)
+                sol = api.EigenSolver(p).solve(warm_start=True, **kw)
+                out["warm_solve"] = {k: sol.diag[k] for k in keys}
     print(json.dumps(out))
 
 
