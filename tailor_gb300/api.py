@@ -223,7 +223,7 @@ class EigenSolver:
     def solve(self, nev: int = 0, ncv: int = 0, tol: float = 0.0,
               max_it: int = 0, precision: int = 0, sigma: complex | None = None,
               start: np.ndarray | None = None, modes: bool = False,
-              cuda_core_schur: bool = False, persistent_solve: bool = False,
+              cuda_core_schur: int = 0, persistent_solve: bool = False,
               solve_block: int = 0, refinement: str = "ir",
               panel_width: int = 0, cluster_panel: int = 0,
               fallback: bool = True, block: int = 0,
@@ -263,7 +263,9 @@ class EigenSolver:
         opts = L.SolveOpts(nev, ncv, tol, max_it, precision,
                            0.0 if sigma is None else complex(sigma).real,
                            0.0 if sigma is None else complex(sigma).imag,
-                           0 if sigma is None else 1, None, int(bool(cuda_core_schur)),
+                           0 if sigma is None else 1, None,
+                           # False/True, or 2: tile-staged tcgen05 update
+                           int(cuda_core_schur),
                            int(solve_block), 1 if refinement == "gmres" else 0,
                            int(panel_width), int(cluster_panel),
                            int(bool(persistent_solve)), int(block), 0,

@@ -199,6 +199,15 @@ struct CaptureScope {  // suppresses counting on this thread during capture
 
 struct DevFront;
 // Tensor-core Schur update of one panel step (tlr_tc.cu).
+// The same update with the operands converted once per panel step into
+// TF32 plane images (planes: (atiles + btiles) x ceil(w / 8) x 16 KB of
+// scratch) and streamed into shared memory by bulk copies; pa / pb are the
+// per-front prefixes of the step's 128-row L21 tiles and 64-column U12 tiles.
+int launch_gemm_tc_bulk(tlr_ctx *ctx, const int *fl, const int *prefix, const int *pa,
+                        const int *pb, int nf, int s, int w, float2 *pool, const DevFront *fr,
+                        int tiles, int atiles, int btiles, unsigned char *planes, int *err,
+                        cudaStream_t st);
+size_t tc_chunk_image_bytes();
 int launch_gemm_tc(tlr_ctx *ctx, const int *fl, const int *prefix, int nf, int s, int w,
                    float2 *pool, const DevFront *fr, int tiles, int *err, cudaStream_t st,
                    uint32_t lbo = 128, uint32_t sbo = 256);

@@ -616,7 +616,10 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   const int prec = o.precision == 1 ? 1 : 0;
   // Schur updates on the tensor cores: tcgen05 (3xTF32) for complex64
   // fronts, DMMA (FP64 mma.sync) for complex128 fronts
-  const bool tc = !o.cuda_core_schur;
+  const bool tc = o.cuda_core_schur != 1;
+  // complex64: 0 streams pre-split operand planes by bulk copies, 2 stages
+  // them per tile (the earlier kernel)
+  const bool tc_bulk = o.cuda_core_schur != 2;
   const int sblock = prec == 0 ? 128
                      : (o.solve_block == 128 || o.solve_block == 512 ? o.solve_block : 256);
   const int pwidth =
@@ -627,7 +630,8 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   // factorisation (reused when sigma, precision and Schur kernel are unchanged)
   Factor *F = ctx->factor;
   if (F && (F->prec != prec || F->sigma_re != sigma.real() || F->sigma_im != sigma.imag() ||
-            F->tensor_cores != tc || F->sw != sblock || F->w != pwidth || !F->factored)) {
+            F->tensor_cores != tc || F->tc_bulk != tc_bulk || F->sw != sblock || F->w != pwidth ||
+            !F->factored)) {
     if (F->prec != prec || F->sw != sblock || F->w != pwidth) {
       free_factor(ctx);
       F = nullptr;
@@ -650,6 +654,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
                     : (o.cluster_panel < 0 ? INT_MAX : kClusterPanelRows);
   if (F->cluster_rows != crows) F->factored = false;
   F->tensor_cores = tc;
+  F->tc_bulk = tc_bulk;
   F->cluster_rows = crows;
   F->persistent = o.persistent_solve != 0;
   if (!F->factored) {

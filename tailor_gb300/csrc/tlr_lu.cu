@@ -1822,6 +1822,7 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int pa
   }
   // schedules: per level, fronts sorted by p descending; per step prefix
   std::vector<int> sched;
+  long long max_plane_tiles = 0;  // largest atiles + btiles of a panel step
   levels.clear();
   for (size_t h = 0; h < sym.levels.size(); ++h) {
     Level L;
@@ -1877,6 +1878,22 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int pa
       }
       sched.push_back(acc);
       st.tiles = acc;
+      if (prec == 1) {  // the operand tiles of the bulk-copy Schur update
+        for (int pass = 0; pass < 2; ++pass) {
+          (pass ? st.pb_off : st.pa_off) = (int)sched.size();
+          int tot = 0;
+          for (int q = 0; q < st.nf; ++q) {
+            const FrontInfo &f = sym.fronts[fl[q]];
+            const int ww = std::min(w, f.p - s * w);
+            const int ext = f.m - s * w - ww;
+            sched.push_back(tot);
+            tot += (ext + (pass ? kTN32 : kTM32) - 1) / (pass ? kTN32 : kTM32);
+          }
+          sched.push_back(tot);
+          (pass ? st.btiles : st.atiles) = tot;
+        }
+        max_plane_tiles = std::max(max_plane_tiles, (long long)st.atiles + st.btiles);
+      }
       L.steps.push_back(st);
     }
     levels.push_back(L);
@@ -1960,6 +1977,10 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int pa
       (rc = alloc((void **)&d_inv_off, nf * sizeof(long long))) ||
       (rc = alloc((void **)&d_inv_blocks, inv_blocks.size() * sizeof(int2))) ||
       (rc = alloc(&vec_a, (size_t)ctx->nn * 5 * csize)))
+    return rc;
+  if (prec == 1 &&
+      (rc = alloc((void **)&tc_planes, (size_t)max_plane_tiles * ((w + 7) / 8) *
+                                           tc_chunk_image_bytes())))
     return rc;
   partial_stride = std::max(partial_elems, 1LL);
   TLR_CUDA(ctx, cudaMemcpy(d_inv_off, inv_off.data(), nf * sizeof(long long),
@@ -2081,7 +2102,8 @@ void Factor::release() {
   cudaFree(d_cinv); cudaFree(work2); cudaFree(d_sched); cudaFree(d_partial); cudaFree(d_pert); cudaFree(d_tc_err);
   cudaFree(vec_a); cudaFree(linv); cudaFree(uinv); cudaFree(dmat);
   cudaFree(d_inv_off); cudaFree(d_inv_blocks); cudaFree(d_ltiles); cudaFree(d_utiles);
-  cudaFree(d_phases); cudaFree(d_barrier); cudaFree(d_solve_err);
+  cudaFree(d_phases); cudaFree(d_barrier); cudaFree(d_solve_err); cudaFree(tc_planes);
+  tc_planes = nullptr;
   d_phases = nullptr;
   d_barrier = nullptr;
   d_solve_err = nullptr;
@@ -2178,7 +2200,13 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
                                                                                  d_fronts); count_launches(); }
         if (S.tiles > 0) {
           if constexpr (sizeof(C) == sizeof(float2)) {
-            if (tensor_cores) {
+            if (tensor_cores && tc_bulk) {
+              const int rc = launch_gemm_tc_bulk(
+                  ctx, fl, d_sched + S.prefix_off, d_sched + S.pa_off, d_sched + S.pb_off, S.nf,
+                  s, w, reinterpret_cast<float2 *>(P), d_fronts, S.tiles, S.atiles, S.btiles,
+                  tc_planes, d_tc_err, st);
+              if (rc) return rc;
+            } else if (tensor_cores) {
               const int rc = launch_gemm_tc(ctx, fl, d_sched + S.prefix_off, S.nf, s, w,
                                             reinterpret_cast<float2 *>(P), d_fronts, S.tiles,
                                             d_tc_err, st);

@@ -19,6 +19,9 @@ constexpr int kClusterPanelRows = 256;
 
 struct Step {  // one panel step of one level
   int nf, max_m, max_b, max_ext, prefix_off, tiles;
+  // complex64: per-front prefixes (nf + 1 each, in the schedule) of the
+  // step's 128-row L21 tiles and 64-column U12 tiles, and their totals
+  int pa_off = 0, pb_off = 0, atiles = 0, btiles = 0;
 };
 
 struct Level {
@@ -48,6 +51,10 @@ struct Factor {
   // 8-CTA cluster (INT_MAX: never)
   int cluster_rows = kClusterPanelRows;
   int *d_tc_err = nullptr;   // set by a tensor-core kernel whose wait timed out
+  // complex64 Schur updates: operand plane images of one panel step, read
+  // by bulk copies (tc_bulk), else staged by every tile's own threads
+  bool tc_bulk = true;
+  unsigned char *tc_planes = nullptr;
   int w = 32;    // panel width
   int sw = 128;  // rows of a diagonal block of the solves (128 or 256)
   std::vector<Level> levels;

@@ -116,6 +116,12 @@ __global__ void k_mbar_timeout_probe(unsigned limit, int *err) {
         "=r"(r[13]), "=r"(r[14]), "=r"(r[15])                                                    \
       : "r"(taddr))
 
+#define TLR_TC_LD8(taddr, r)                                                                    \
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"        \
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),        \
+                 "=r"(r[6]), "=r"(r[7])                                                         \
+               : "r"(taddr))
+
 __global__ void __launch_bounds__(256)
     k_gemm_tc(const int *__restrict__ fl, const int *__restrict__ prefix, int nf, int s, int w,
               float2 *__restrict__ pool, const DevFront *__restrict__ fr, int *__restrict__ err,
@@ -298,9 +304,302 @@ __global__ void __launch_bounds__(256)
                  "r"(kTmemCols));
 }
 
+// ---- operand planes in global memory, bulk-copy Schur update -------------
+// The update above converts every operand chunk into TF32 hi/lo planes once
+// per output tile, so each row tile of L21 is converted once per column
+// tile and vice versa, and the global loads feeding that conversion stall
+// the warps.  Here the conversion runs once per panel step: k_tc_split
+// writes, for every 128-row tile of L21 and every 64-column tile of U12 of
+// every front of the step, each K chunk as a 16 KB image [hi plane | lo
+// plane] in exactly the shared-memory layout the MMA descriptors expect.
+// k_gemm_tc_bulk then streams those images into a three-stage shared
+// memory ring with cp.async.bulk (one thread issues the copies and the
+// MMAs; completion by mbarrier transaction counts), while the other
+// threads prefetch the F22 tile into registers for the epilogue.
+constexpr int kChunkImg = 2 * kPlane;  // one operand chunk: hi + lo planes
+constexpr int kBulkStages = 3;
+
+__device__ __forceinline__ int find_front(const int *__restrict__ prefix, int nf, int t) {
+  int lo = 0, hi = nf;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) / 2;
+    if (prefix[mid] <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// grid (atiles + btiles, nchmax): blockIdx.x < atiles is A tile
+// (front, 128-row tile), else B tile (front, 64-column tile); blockIdx.y is
+// the K chunk.  pa / pb: per-front prefix of A / B tiles (nf + 1 each).
+__global__ void __launch_bounds__(256)
+    k_tc_split(const int *__restrict__ fl, const int *__restrict__ pa, const int *__restrict__ pb,
+               int nf, int s, int w, const float2 *__restrict__ pool,
+               const DevFront *__restrict__ fr, unsigned char *__restrict__ planes, int atiles,
+               int nchmax) {
+  const int tid = threadIdx.x, c = blockIdx.y;
+  const bool is_a = (int)blockIdx.x < atiles;
+  const int t = is_a ? blockIdx.x : blockIdx.x - atiles;
+  const int lo = find_front(is_a ? pa : pb, nf, t);
+  const DevFront f = fr[fl[lo]];
+  const int m = f.m, k0 = s * w, ww = min(w, f.p - k0);
+  const int base = k0 + ww;
+  if (c * kTcKC >= ww) return;  // this front has fewer chunks
+  const float2 *F = pool + f.off;
+  unsigned char *img = planes + ((long long)blockIdx.x * nchmax + c) * kChunkImg;
+  auto split4 = [](const float *x, uint4 &hi4, uint4 &lo4) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      h[j] = to_tf32(x[j]);
+      l[j] = to_tf32(x[j] - __uint_as_float(h[j]));
+    }
+    hi4 = make_uint4(h[0], h[1], h[2], h[3]);
+    lo4 = make_uint4(l[0], l[1], l[2], l[3]);
+  };
+  uint4 h, l;
+  if (is_a) {
+    // rows R0 + ar, complex columns 4 aq .. 4 aq + 3 of the chunk
+    const int R0 = base + (t - pa[lo]) * kTcM;
+    const int ar = tid & (kTcM - 1), aq = tid >> 7;
+    float re[4], im[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int kc = c * kTcKC + 4 * aq + j;
+      const float2 v = (R0 + ar < m && kc < ww) ? F[(long long)(k0 + kc) * m + R0 + ar]
+                                                 : make_float2(0.f, 0.f);
+      re[j] = v.x;
+      im[j] = v.y;
+    }
+    split4(re, h, l);
+    *reinterpret_cast<uint4 *>(img + plane_off(ar, 4 * aq)) = h;
+    *reinterpret_cast<uint4 *>(img + kPlane + plane_off(ar, 4 * aq)) = l;
+    split4(im, h, l);
+    *reinterpret_cast<uint4 *>(img + plane_off(ar, 8 + 4 * aq)) = h;
+    *reinterpret_cast<uint4 *>(img + kPlane + plane_off(ar, 8 + 4 * aq)) = l;
+  } else if (tid < 128) {
+    // columns C0 + bn, K rows 4 bq .. 4 bq + 3 of the chunk:
+    // Cr row bn: [Ur ; -Ui]; Ci row 64 + bn: [Ui ; Ur]
+    const int C0 = base + (t - pb[lo]) * kTcN;
+    const int bn = tid & 63, bq = tid >> 6;
+    float ur[4], ui[4], nui[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int kb = c * kTcKC + 4 * bq + j;
+      const float2 v = (C0 + bn < m && kb < ww) ? F[(long long)(C0 + bn) * m + k0 + kb]
+                                                 : make_float2(0.f, 0.f);
+      ur[j] = v.x;
+      ui[j] = v.y;
+      nui[j] = -v.y;
+    }
+    unsigned char *bh = img, *bl = img + kPlane;
+    split4(ur, h, l);
+    *reinterpret_cast<uint4 *>(bh + plane_off(bn, 4 * bq)) = h;
+    *reinterpret_cast<uint4 *>(bl + plane_off(bn, 4 * bq)) = l;
+    *reinterpret_cast<uint4 *>(bh + plane_off(64 + bn, 8 + 4 * bq)) = h;
+    *reinterpret_cast<uint4 *>(bl + plane_off(64 + bn, 8 + 4 * bq)) = l;
+    split4(nui, h, l);
+    *reinterpret_cast<uint4 *>(bh + plane_off(bn, 8 + 4 * bq)) = h;
+    *reinterpret_cast<uint4 *>(bl + plane_off(bn, 8 + 4 * bq)) = l;
+    split4(ui, h, l);
+    *reinterpret_cast<uint4 *>(bh + plane_off(64 + bn, 4 * bq)) = h;
+    *reinterpret_cast<uint4 *>(bl + plane_off(64 + bn, 4 * bq)) = l;
+  }
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// global -> shared bulk copy of `bytes` (16-byte aligned addresses, size a
+// multiple of 16), completing `bytes` transactions on bar
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__global__ void __launch_bounds__(256, 2)
+    k_gemm_tc_bulk(const int *__restrict__ fl, const int *__restrict__ prefix,
+                   const int *__restrict__ pa, const int *__restrict__ pb, int nf, int s, int w,
+                   float2 *__restrict__ pool, const DevFront *__restrict__ fr,
+                   const unsigned char *__restrict__ planes_a,
+                   const unsigned char *__restrict__ planes_b, int nchmax, int *__restrict__ err,
+                   uint32_t lbo, uint32_t sbo) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  __shared__ __align__(8) uint64_t full[kBulkStages], empty[kBulkStages];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int wait_ok;
+  unsigned char *ring = tc_smem + ((1024 - (smem_addr(tc_smem) & 1023)) & 1023);
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  const int t = blockIdx.x;
+  const int lo = find_front(prefix, nf, t);
+  const DevFront f = fr[fl[lo]];
+  const int m = f.m, k0 = s * w, ww = min(w, f.p - k0);
+  const int base = k0 + ww, ext = m - base;
+  const int ntm = (ext + kTcM - 1) / kTcM;
+  const int lt = t - prefix[lo];
+  const int rt = lt % ntm, ct = lt / ntm;
+  const int R0 = base + rt * kTcM, C0 = base + ct * kTcN;
+  float2 *F = pool + f.off;
+  const int nch = (ww + kTcKC - 1) / kTcKC;
+  const unsigned char *ga = planes_a + (long long)(pa[lo] + rt) * nchmax * kChunkImg;
+  const unsigned char *gb = planes_b + (long long)(pb[lo] + ct) * nchmax * kChunkImg;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(&tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int q = 0; q < kBulkStages; ++q) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full[q])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty[q])));
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  auto issue = [&](int c) {  // chunk c into stage c % kBulkStages
+    unsigned char *st = ring + (c % kBulkStages) * kStage;
+    uint64_t *bar = &full[c % kBulkStages];
+    mbar_expect_tx(bar, 2 * kChunkImg);
+    bulk_g2s(st, ga + (long long)c * kChunkImg, kChunkImg, bar);
+    bulk_g2s(st + kChunkImg, gb + (long long)c * kChunkImg, kChunkImg, bar);
+  };
+  int issued = 0;
+  if (tid == 0)
+    for (; issued < nch && issued < kBulkStages; ++issued) issue(issued);
+
+  // the F22 entries of the epilogue: warp w owns tile rows 32 (w % 4) + lane
+  // and the 32 columns 32 (w / 4) .. +31.  Warps 1..7 fetch theirs while the
+  // operands stream in; warp 0, whose first thread drives the copies and
+  // MMAs, fetches after them (keeping its registers free for that loop).
+  const int q4 = warp & 3, h2 = warp >> 2;
+  const int row = 32 * q4 + (tid & 31);
+  const bool row_ok = R0 + row < m;
+  float2 f22[32];
+  auto fetch_f22 = [&]() {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int n = 32 * h2 + j;
+      f22[j] = (row_ok && C0 + n < m) ? F[(long long)(C0 + n) * m + R0 + row]
+                                      : make_float2(0.f, 0.f);
+    }
+  };
+  if (warp != 0) fetch_f22();
+
+  if (tid == 0) {
+    bool ok = true;
+    int done = 0;  // chunks whose MMAs were issued
+    for (int c = 0; c < nch && ok; ++c) {
+      const int sb = c % kBulkStages;
+      if (!mbar_wait(&full[sb], (c / kBulkStages) & 1)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a_hi = smem_addr(ring + sb * kStage), a_lo = a_hi + kPlane;
+      const uint32_t b_hi = a_hi + 2 * kPlane, b_lo = a_hi + 3 * kPlane;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const uint32_t o = j * 4096;
+        const uint32_t acc0 = (c > 0 || j > 0) ? 1u : 0u;
+        mma_tf32(tmem, smem_desc(a_lo + o, lbo, sbo), smem_desc(b_hi + o, lbo, sbo), acc0);
+        mma_tf32(tmem, smem_desc(a_hi + o, lbo, sbo), smem_desc(b_lo + o, lbo, sbo), 1u);
+        mma_tf32(tmem, smem_desc(a_hi + o, lbo, sbo), smem_desc(b_hi + o, lbo, sbo), 1u);
+      }
+      mma_commit(&empty[sb]);
+      done = c + 1;
+      if (issued < nch) {  // refill this stage once its MMAs have read it
+        if (!mbar_wait(&empty[sb], (c / kBulkStages) & 1)) {
+          ok = false;
+          break;
+        }
+        issue(issued++);
+      }
+    }
+    // the last commit covers every MMA issued before it
+    bool fine = ok && done == nch &&
+                (nch == 0 || mbar_wait(&empty[(nch - 1) % kBulkStages],
+                                       ((nch - 1) / kBulkStages) & 1));
+    if (!fine) {
+      atomicExch(err, 1);
+      // let copies and MMAs still in flight land before the memory is
+      // released: every issued chunk's copy, then the last commit
+      for (int c = done; c < issued; ++c)
+        mbar_wait(&full[c % kBulkStages], (c / kBulkStages) & 1);
+      if (done > 0)
+        mbar_wait(&empty[(done - 1) % kBulkStages], ((done - 1) / kBulkStages) & 1);
+    }
+    wait_ok = fine;
+  }
+  __syncthreads();
+  const bool ok = wait_ok != 0;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0) fetch_f22();
+  if (ok) {
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * q4) << 16);
+#pragma unroll
+    for (int part = 0; part < 4; ++part) {
+      uint32_t cr[8], ci[8];
+      const int n0 = 32 * h2 + 8 * part;
+      TLR_TC_LD8(lane_addr + n0, cr);
+      TLR_TC_LD8(lane_addr + 64 + n0, ci);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row_ok) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int n = n0 + j;
+          if (C0 + n < m) {
+            float2 d = f22[8 * part + j];
+            d.x -= __uint_as_float(cr[j]);
+            d.y -= __uint_as_float(ci[j]);
+            F[(long long)(C0 + n) * m + R0 + row] = d;
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols));
+}
+
 }  // namespace
 
 size_t gemm_tc_smem() { return 2 * kStage + 1024; }
+
+size_t gemm_tc_bulk_smem() { return kBulkStages * kStage + 1024; }
+size_t tc_chunk_image_bytes() { return kChunkImg; }
+
+int launch_gemm_tc_bulk(tlr_ctx *ctx, const int *fl, const int *prefix, const int *pa,
+                        const int *pb, int nf, int s, int w, float2 *pool, const DevFront *fr,
+                        int tiles, int atiles, int btiles, unsigned char *planes, int *err,
+                        cudaStream_t st) {
+  const int nchmax = (w + kTcKC - 1) / kTcKC;
+  if (atiles + btiles > 0)
+    { k_tc_split<<<dim3(atiles + btiles, nchmax), 256, 0, st>>>(fl, pa, pb, nf, s, w, pool, fr,
+                                                               planes, atiles, nchmax); count_launches(); }
+  TLR_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tc_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)gemm_tc_bulk_smem()));
+  const unsigned char *pbp = planes + (long long)atiles * nchmax * kChunkImg;
+  { k_gemm_tc_bulk<<<tiles, 256, gemm_tc_bulk_smem(), st>>>(fl, prefix, pa, pb, nf, s, w, pool, fr,
+                                                            planes, pbp, nchmax, err, 128u, 256u); count_launches(); }
+  TLR_CUDA(ctx, cudaGetLastError());
+  return TLR_OK;
+}
 
 int launch_gemm_tc(tlr_ctx *ctx, const int *fl, const int *prefix, int nf, int s, int w,
                    float2 *pool, const DevFront *fr, int tiles, int *err, cudaStream_t st,

@@ -159,3 +159,18 @@ def test_fp64_tensor_core_schur_update_matches_cuda_cores(gpu_lib):
         assert np.all(tc.residual <= 1e-10) and np.all(cc.residual <= 1e-10)
         for lam in tc.lam:
             assert np.min(np.abs(cc.lam - lam)) <= 1e-10 * abs(lam)
+
+
+def test_bulk_copy_schur_update_is_bitwise_the_tile_staged_one(gpu_lib):
+    """The tcgen05 Schur update fed by bulk copies of operand planes split
+    once per panel step (the default) and the one whose tiles stage their
+    own operands run the same MMAs in the same order: identical factors,
+    hence identical eigenpairs."""
+    ph = Physics(alpha=1.9, omega=0j, nev=8, tol=1e-10)
+    with api.Problem(make_case(100, 50, physics=ph)) as p:
+        api.run_pipeline(p)
+        bulk = api.EigenSolver(p).solve(nev=8, precision=1, fallback=False)
+        tile = api.EigenSolver(p).solve(nev=8, precision=1, cuda_core_schur=2, fallback=False)
+        assert np.array_equal(bulk.lam, tile.lam)
+        assert np.array_equal(bulk.residual, tile.residual)
+        assert np.all(bulk.residual <= 1e-10)
