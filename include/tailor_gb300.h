@@ -193,13 +193,16 @@ typedef struct {
   double sigma_re, sigma_im; /* used when use_sigma != 0                    */
   int use_sigma;          /* 0: sigma = lambda target from omega            */
   const double *start;    /* optional complex [5N] host start vector        */
-  int cuda_core_schur;    /* 0 (default): Schur updates on the tensor cores
-                             (mixed form: tcgen05, 3xTF32, operands split
-                             once per panel step and streamed by bulk
-                             copies; FP64 form: DMMA, mma.sync m8n8k4 f64);
-                             1: on the CUDA cores (FP32 / FP64 FMA); 2:
-                             mixed form on tcgen05 with every tile staging
-                             its own operands (same bits as 0)               */
+  int cuda_core_schur;    /* Schur-update kernel.  0 (default): the fastest
+                             measured -- mixed form: tcgen05 (3xTF32) fed by
+                             bulk copies of operand planes split once per
+                             panel step; FP64 form: CUDA-core FP64 FMA.
+                             1: CUDA cores (FP32 / FP64 FMA).  2: mixed form
+                             on tcgen05 with every tile staging its own
+                             operands (the same bits as 0); FP64 form on the
+                             FP64 tensor cores (DMMA, mma.sync m8n8k4 f64;
+                             GB300's FP64 tensor rate is no higher than its
+                             FP64 FMA rate, and measured 13% slower)         */
   int solve_block;        /* mixed form: diagonal-block size of the
                              triangular solves, 128, 256 or 512 (0: 256)     */
   int refinement;         /* mixed form: 0 (default) classic iterative

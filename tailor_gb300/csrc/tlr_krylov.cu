@@ -616,9 +616,12 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   const int prec = o.precision == 1 ? 1 : 0;
   // Schur updates on the tensor cores: tcgen05 (3xTF32) for complex64
   // fronts, DMMA (FP64 mma.sync) for complex128 fronts
-  const bool tc = o.cuda_core_schur != 1;
-  // complex64: 0 streams pre-split operand planes by bulk copies, 2 stages
-  // them per tile (the earlier kernel)
+  // Schur-update kernel: 0 = the fastest measured one (complex64: tcgen05
+  // fed by bulk copies of pre-split operand planes; complex128: CUDA-core
+  // FP64, since GB300's DMMA rate is no higher and measured 13% slower);
+  // 1 = CUDA cores; 2 = the other tensor-core variant (complex64: tiles
+  // staging their own operands; complex128: DMMA)
+  const bool tc = prec == 1 ? o.cuda_core_schur != 1 : o.cuda_core_schur == 2;
   const bool tc_bulk = o.cuda_core_schur != 2;
   const int sblock = prec == 0 ? 128
                      : (o.solve_block == 128 || o.solve_block == 512 ? o.solve_block : 256);

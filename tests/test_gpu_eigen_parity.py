@@ -150,12 +150,13 @@ def test_sweep_with_warm_starts_and_blocks(gpu_lib):
 
 def test_fp64_tensor_core_schur_update_matches_cuda_cores(gpu_lib):
     """The plain FP64 form's Schur updates on the FP64 tensor cores (DMMA,
-    the default) and on the CUDA cores give the same eigenpairs."""
+    cuda_core_schur = 2) and on the CUDA cores (the default) give the same
+    eigenpairs."""
     ph = Physics(alpha=2.2, omega=0j, nev=8, tol=1e-10)
     with api.Problem(make_case(60, 32, physics=ph)) as p:
         api.run_pipeline(p)
-        tc = api.EigenSolver(p).solve(nev=8, precision=0)
-        cc = api.EigenSolver(p).solve(nev=8, precision=0, cuda_core_schur=True)
+        tc = api.EigenSolver(p).solve(nev=8, precision=0, cuda_core_schur=2)
+        cc = api.EigenSolver(p).solve(nev=8, precision=0)
         assert np.all(tc.residual <= 1e-10) and np.all(cc.residual <= 1e-10)
         for lam in tc.lam:
             assert np.min(np.abs(cc.lam - lam)) <= 1e-10 * abs(lam)
