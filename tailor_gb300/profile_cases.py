@@ -36,7 +36,8 @@ def main() -> None:
     ap.add_argument("--reynolds", type=float, default=1000.0)
     ap.add_argument("--ncv", type=int, default=0)
     ap.add_argument("--block", type=int, default=0)
-    ap.add_argument("--cuda-core-schur", action="store_true")
+    ap.add_argument("--schur-kernel", type=int, default=0,
+                    help="tlr_solve_opts.cuda_core_schur: 0 fastest, 1 CUDA cores, 2 other")
     ap.add_argument("--warm", action="store_true")
     a = ap.parse_args()
     case = make_case(a.ny, a.nz, physics=Physics(alpha=a.alpha, nev=a.nev, mach=a.mach,
@@ -58,7 +59,7 @@ def main() -> None:
             keys = ("factor_ms", "krylov_ms", "solves", "iterations", "max_relative_error",
                     "solve_ms", "factor_bytes", "factor_flops", "trisolve_ms", "trisolves")
             kw = dict(precision=a.precision, ncv=a.ncv, block=a.block,
-                      cuda_core_schur=a.cuda_core_schur)
+                      cuda_core_schur=a.schur_kernel)
             sol = api.EigenSolver(p).solve(**kw)
             out["solve"] = {k: sol.diag[k] for k in keys}
             if a.warm:
