@@ -270,15 +270,20 @@ def run_c3(api, npoints=64):
     """The sweep in the plain FP64 form (one instance at a time, CUDA-core
     FP64 fronts) and in the mixed + batched form (complex64 fronts with
     tensor-core Schur updates and FP64 refinement, eight concurrent instances,
-    autotuned kernels): eigenpairs at resid <= 1e-10 per wall second; the
+    autotuned kernels, each point warm-started from its neighbour in alpha):
+    eigenpairs at resid <= 1e-10 per wall second; the
     mixed eigenvalues are compared with the plain ones point by point.  With
     several ranks the points are dealt round-robin to the GPUs (replicas) and
     the wall time is the slowest rank's."""
     from tailor_gb300 import replicas
     cases, points = c3_sweep_inputs(npoints)
+    # ordered by grid class and alpha: with warm starts every worker walks a
+    # contiguous run of neighbouring points of one class
+    points = sorted(points)
     out, lam = {}, {}
     for name, kw in (("plain_fp64", dict(precision=0, workers=1, autotune=False)),
-                     ("mixed_batched", dict(precision=1, workers=8, autotune=True))):
+                     ("mixed_batched", dict(precision=1, workers=8, autotune=True,
+                                            warm_start=True))):
         replicas.barrier()
         t = time.perf_counter()
         r = replicas.sweep(cases, points, nev=8, ncv=32, raise_on_error=False, **kw)

@@ -4,9 +4,11 @@
 
 Grid Ny x Nz (FD-q q=10 / q=6), bump amplitude 0.05, Mach 0.7, target
 lambda_s = 0, nev 8, tol 1e-10; points on an 8 x 4 grid of alpha in
-[0.5, 3.5] and Re in [800, 2400].  The mixed + batched form (complex64
-fronts with tensor-core Schur updates and FP64 refinement, concurrent
-instances, autotuned kernels) solves every point; the plain FP64 form
+[0.5, 3.5] and Re in [800, 2400], in snake order.  The mixed + batched
+form (complex64 fronts with tensor-core Schur updates and FP64
+refinement, the sweep engine's shared symbolic analysis and autotuned
+kernels, every point warm-started from its predecessor's Ritz vectors)
+solves every point; the plain FP64 form
 solves the first --plain-points points one at a time, and their
 eigenvalues are compared.  Prints one JSON line with
 eigenpairs at resid <= 1e-10 per wall second for each form and the
@@ -51,17 +53,17 @@ def main() -> None:
     ap.add_argument("--ny", type=int, default=300)
     ap.add_argument("--nz", type=int, default=192)
     ap.add_argument("--nev", type=int, default=8)
-    ap.add_argument("--workers", type=int, default=3)
+    ap.add_argument("--workers", type=int, default=1)
     ap.add_argument("--plain-points", type=int, default=2)
-    ap.add_argument("--ncv", type=int, default=32)
+    ap.add_argument("--ncv", type=int, default=64)
     a = ap.parse_args()
     case = c5_case(a.ny, a.nz, a.nev)
-    points = c5_points()
+    points = c5_points(snake=True)
     out = {"grid": [a.ny, a.nz], "points": len(points), "nev": a.nev, "ncv": a.ncv,
            "mach": 0.7}
     t = time.perf_counter()
     r = api.sweep([case], points, nev=a.nev, ncv=a.ncv, precision=1, workers=a.workers,
-                  autotune=True, raise_on_error=False)
+                  autotune=True, raise_on_error=False, warm_start=True)
     wall = time.perf_counter() - t
     good = int(np.sum((r.residual >= 0) & (r.residual <= 1e-10)))
     fb = [d["factor_bytes"] for d in r.point_diag if d["factor_bytes"] > 0]
