@@ -295,6 +295,7 @@ def run_c3(api, npoints=64):
                      "failed_points": int(np.sum(r["status"] != 0)),
                      "workers": d0["workers"], "ranks": r["world"],
                      "solve_block": d0["solve_block"],
+                     "panel_width": d0.get("panel_width"),
                      "tensor_core_schur": [1 - c for c in d0["cuda_core_schur"]]}
     # mixed pairs count only where they match the plain FP64 eigenvalues
     (lp, rp), (lm, rm) = lam["plain_fp64"], lam["mixed_batched"]

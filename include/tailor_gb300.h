@@ -341,9 +341,10 @@ typedef struct {
 typedef struct {
   tlr_solve_opts solve;       /* shared solve options (start is ignored)      */
   int workers;                /* concurrent instances (0: 8)                  */
-  int autotune;               /* mixed form: time both Schur-update kernels
-                                 and both solve block sizes on each class's
-                                 first point and keep the fastest             */
+  int autotune;               /* mixed form: time both Schur-update kernels,
+                                 both solve block sizes and panels of 64 and
+                                 128 columns on each class's first point and
+                                 keep the fastest                             */
   int device;
 } tlr_sweep_opts;
 
@@ -355,6 +356,9 @@ typedef struct {
   int solve_block[16];        /* per grid class: chosen diagonal-block size   */
   double tune_factor_ms[16][2];   /* tensor cores, CUDA cores                 */
   double tune_trisolve_ms[16][2]; /* block 256, block 128                     */
+  int panel_width[16];        /* per grid class: chosen panel width (the
+                                 depth of the Schur-update tiles; 0: default) */
+  double tune_wide_factor_ms[16]; /* the chosen kernel with 128-wide panels   */
 } tlr_sweep_diag;
 
 /* lambda [npoints][nev] complex, residual [npoints][nev] (-1: not solved),

@@ -121,7 +121,8 @@ class SweepDiag(ctypes.Structure):
                 ("converged_pairs", ctypes.c_int),
                 ("cuda_core_schur", ctypes.c_int * 16), ("solve_block", ctypes.c_int * 16),
                 ("tune_factor_ms", (ctypes.c_double * 2) * 16),
-                ("tune_trisolve_ms", (ctypes.c_double * 2) * 16)]
+                ("tune_trisolve_ms", (ctypes.c_double * 2) * 16),
+                ("panel_width", ctypes.c_int * 16), ("tune_wide_factor_ms", ctypes.c_double * 16)]
 
 
 class SymbolicInfo(ctypes.Structure):

@@ -416,6 +416,8 @@ def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
             "solve_block": list(d.solve_block[:nc]),
             "tune_factor_ms": [list(d.tune_factor_ms[c]) for c in range(nc)],
             "tune_trisolve_ms": [list(d.tune_trisolve_ms[c]) for c in range(nc)],
+            "panel_width": list(d.panel_width[:nc]),
+            "tune_wide_factor_ms": list(d.tune_wide_factor_ms[:nc]),
             "fallback_points": fallbacks}
     return SweepResult(lam[:npts, :, 0] + 1j * lam[:npts, :, 1], res[:npts], st[:npts], diag,
                        point_diag)

@@ -34,8 +34,8 @@ constexpr int kMaxClasses = 16;
 struct ClassState {
   const tlr_grid_class *gc = nullptr;
   std::unique_ptr<Symbolic> sym;
-  int cuda_core_schur = 0, solve_block = 0;
-  double factor_ms[2] = {0, 0}, trisolve_ms[2] = {0, 0};
+  int cuda_core_schur = 0, solve_block = 0, panel_width = 0;
+  double factor_ms[2] = {0, 0}, trisolve_ms[2] = {0, 0}, wide_factor_ms = 0;
 };
 
 int make_context(const tlr_grid_class &gc, int device, tlr_ctx **out) {
@@ -81,7 +81,8 @@ double elapsed_ms(tlr_ctx *ctx) {
 
 // Time factorisations and triangular solves of the mixed form on the staged
 // point: Schur kernel on the 256 block, then the 128 block with the faster
-// kernel.  Leaves ctx without a factor.
+// kernel, then the faster kernel with 128-column panels (the depth K of the
+// Schur-update tiles) instead of 64.  Leaves ctx without a factor.
 int autotune(tlr_ctx *ctx, ClassState &cs) {
   double anorm = 0.0;
   int rc = frobenius(ctx, ctx->A, ctx->nnzb * 25, &anorm);
@@ -117,6 +118,26 @@ int autotune(tlr_ctx *ctx, ClassState &cs) {
       }
     }
     if (rc) break;
+    if (bi == 0) {  // the winning kernel with 128-column panels
+      Factor *W = new Factor();
+      if ((rc = W->setup(ctx, 1, 48, blocks[bi], 128))) {
+        W->release();
+        delete W;
+        break;
+      }
+      W->tensor_cores = !cs.cuda_core_schur;
+      Factor *keep = ctx->factor;
+      ctx->factor = W;
+      cudaEventRecord(ctx->ev0, ctx->stream);
+      rc = W->factor(ctx, sr, si, tiny);
+      cudaEventRecord(ctx->ev1, ctx->stream);
+      cs.wide_factor_ms = rc ? 1e300 : elapsed_ms(ctx);
+      cs.panel_width = cs.wide_factor_ms < fbest ? 128 : 64;
+      W->release();
+      delete W;
+      ctx->factor = keep;
+      if (rc) break;
+    }
     cudaMemcpyAsync(dx, hx.data(), n * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream);
     if ((rc = F->solve(ctx, dx))) break;  // first replay instantiates the graph
     F->take_solve_time(nullptr);
@@ -191,7 +212,7 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
     }
     Factor *F = new Factor();
     ctx->factor = F;
-    if ((rc = F->setup(ctx, prec, 48, cs[c].solve_block))) {
+    if ((rc = F->setup(ctx, prec, 48, cs[c].solve_block, cs[c].panel_width))) {
       err = ctx->last_error;
       break;
     }
@@ -239,6 +260,7 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
         so.nev = nev;
         so.cuda_core_schur = cs[c].cuda_core_schur;
         so.solve_block = cs[c].solve_block;
+        if (cs[c].panel_width) so.panel_width = cs[c].panel_width;
         so.start = pt.start;
         so.nstart = pt.start ? 1 : 0;
         // concurrent contexts replay solve graphs: a cooperative grid per
@@ -281,6 +303,8 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
       d.tune_factor_ms[c][1] = cs[c].factor_ms[1];
       d.tune_trisolve_ms[c][0] = cs[c].trisolve_ms[0];
       d.tune_trisolve_ms[c][1] = cs[c].trisolve_ms[1];
+      d.panel_width[c] = cs[c].panel_width ? cs[c].panel_width : base.panel_width;
+      d.tune_wide_factor_ms[c] = cs[c].wide_factor_ms;
     }
     *diag = d;
   }
