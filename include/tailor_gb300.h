@@ -202,7 +202,9 @@ typedef struct {
                              operands (the same bits as 0); FP64 form on the
                              FP64 tensor cores (DMMA, mma.sync m8n8k4 f64;
                              GB300's FP64 tensor rate is no higher than its
-                             FP64 FMA rate, and measured 13% slower)         */
+                             FP64 FMA rate, and measured 13% slower).  3:
+                             mixed form, the bulk-copy kernel with a two-
+                             stage ring and three CTAs per SM                */
   int solve_block;        /* mixed form: diagonal-block size of the
                              triangular solves, 128, 256 or 512 (0: 256)     */
   int refinement;         /* mixed form: 0 (default) classic iterative

@@ -206,7 +206,7 @@ struct DevFront;
 int launch_gemm_tc_bulk(tlr_ctx *ctx, const int *fl, const int *prefix, const int *pa,
                         const int *pb, int nf, int s, int w, float2 *pool, const DevFront *fr,
                         int tiles, int atiles, int btiles, unsigned char *planes, int *err,
-                        cudaStream_t st);
+                        cudaStream_t st, int variant = 0);
 size_t tc_chunk_image_bytes();
 int launch_gemm_tc(tlr_ctx *ctx, const int *fl, const int *prefix, int nf, int s, int w,
                    float2 *pool, const DevFront *fr, int tiles, int *err, cudaStream_t st,

@@ -623,6 +623,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   // staging their own operands; complex128: DMMA)
   const bool tc = prec == 1 ? o.cuda_core_schur != 1 : o.cuda_core_schur == 2;
   const bool tc_bulk = o.cuda_core_schur != 2;
+  const int tc_variant = o.cuda_core_schur == 3 ? 1 : 0;
   const int sblock = prec == 0 ? 128
                      : (o.solve_block == 128 || o.solve_block == 512 ? o.solve_block : 256);
   const int pwidth =
@@ -633,8 +634,8 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   // factorisation (reused when sigma, precision and Schur kernel are unchanged)
   Factor *F = ctx->factor;
   if (F && (F->prec != prec || F->sigma_re != sigma.real() || F->sigma_im != sigma.imag() ||
-            F->tensor_cores != tc || F->tc_bulk != tc_bulk || F->sw != sblock || F->w != pwidth ||
-            !F->factored)) {
+            F->tensor_cores != tc || F->tc_bulk != tc_bulk || F->tc_variant != tc_variant ||
+            F->sw != sblock || F->w != pwidth || !F->factored)) {
     if (F->prec != prec || F->sw != sblock || F->w != pwidth) {
       free_factor(ctx);
       F = nullptr;
@@ -658,6 +659,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   if (F->cluster_rows != crows) F->factored = false;
   F->tensor_cores = tc;
   F->tc_bulk = tc_bulk;
+  F->tc_variant = tc_variant;
   F->cluster_rows = crows;
   F->persistent = o.persistent_solve != 0;
   if (!F->factored) {

@@ -2204,7 +2204,7 @@ int Factor::factor_impl(tlr_ctx *ctx, double sr, double si, double tiny) {
               const int rc = launch_gemm_tc_bulk(
                   ctx, fl, d_sched + S.prefix_off, d_sched + S.pa_off, d_sched + S.pb_off, S.nf,
                   s, w, reinterpret_cast<float2 *>(P), d_fronts, S.tiles, S.atiles, S.btiles,
-                  tc_planes, d_tc_err, st);
+                  tc_planes, d_tc_err, st, tc_variant);
               if (rc) return rc;
             } else if (tensor_cores) {
               const int rc = launch_gemm_tc(ctx, fl, d_sched + S.prefix_off, S.nf, s, w,

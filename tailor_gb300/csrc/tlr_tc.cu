@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(256)
 // MMAs; completion by mbarrier transaction counts), while the other
 // threads prefetch the F22 tile into registers for the epilogue.
 constexpr int kChunkImg = 2 * kPlane;  // one operand chunk: hi + lo planes
-constexpr int kBulkStages = 3;
+constexpr int kBulkStages = 3;  // the default ring: three stages, two CTAs per SM
 
 __device__ __forceinline__ int find_front(const int *__restrict__ prefix, int nf, int t) {
   int lo = 0, hi = nf;
@@ -423,7 +423,11 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
       : "memory");
 }
 
-__global__ void __launch_bounds__(256, 2)
+// S: ring stages (shared memory S x 32 KB), MINB: CTAs per SM the register
+// budget must allow, PF: F22 columns per thread prefetched during the MMAs
+// (the rest is read in the epilogue)
+template <int S, int MINB, int PF>
+__global__ void __launch_bounds__(256, MINB)
     k_gemm_tc_bulk(const int *__restrict__ fl, const int *__restrict__ prefix,
                    const int *__restrict__ pa, const int *__restrict__ pb, int nf, int s, int w,
                    float2 *__restrict__ pool, const DevFront *__restrict__ fr,
@@ -431,7 +435,7 @@ __global__ void __launch_bounds__(256, 2)
                    const unsigned char *__restrict__ planes_b, int nchmax, int *__restrict__ err,
                    uint32_t lbo, uint32_t sbo) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
-  __shared__ __align__(8) uint64_t full[kBulkStages], empty[kBulkStages];
+  __shared__ __align__(8) uint64_t full[S], empty[S];
   __shared__ uint32_t tmem_slot;
   __shared__ int wait_ok;
   unsigned char *ring = tc_smem + ((1024 - (smem_addr(tc_smem) & 1023)) & 1023);
@@ -458,7 +462,7 @@ __global__ void __launch_bounds__(256, 2)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    for (int q = 0; q < kBulkStages; ++q) {
+    for (int q = 0; q < S; ++q) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full[q])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty[q])));
     }
@@ -469,16 +473,16 @@ __global__ void __launch_bounds__(256, 2)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
 
-  auto issue = [&](int c) {  // chunk c into stage c % kBulkStages
-    unsigned char *st = ring + (c % kBulkStages) * kStage;
-    uint64_t *bar = &full[c % kBulkStages];
+  auto issue = [&](int c) {  // chunk c into stage c % S
+    unsigned char *st = ring + (c % S) * kStage;
+    uint64_t *bar = &full[c % S];
     mbar_expect_tx(bar, 2 * kChunkImg);
     bulk_g2s(st, ga + (long long)c * kChunkImg, kChunkImg, bar);
     bulk_g2s(st + kChunkImg, gb + (long long)c * kChunkImg, kChunkImg, bar);
   };
   int issued = 0;
   if (tid == 0)
-    for (; issued < nch && issued < kBulkStages; ++issued) issue(issued);
+    for (; issued < nch && issued < S; ++issued) issue(issued);
 
   // the F22 entries of the epilogue: warp w owns tile rows 32 (w % 4) + lane
   // and the 32 columns 32 (w / 4) .. +31.  Warps 1..7 fetch theirs while the
@@ -487,10 +491,10 @@ __global__ void __launch_bounds__(256, 2)
   const int q4 = warp & 3, h2 = warp >> 2;
   const int row = 32 * q4 + (tid & 31);
   const bool row_ok = R0 + row < m;
-  float2 f22[32];
+  float2 f22[PF > 0 ? PF : 1];
   auto fetch_f22 = [&]() {
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
+    for (int j = 0; j < PF; ++j) {
       const int n = 32 * h2 + j;
       f22[j] = (row_ok && C0 + n < m) ? F[(long long)(C0 + n) * m + R0 + row]
                                       : make_float2(0.f, 0.f);
@@ -502,8 +506,8 @@ __global__ void __launch_bounds__(256, 2)
     bool ok = true;
     int done = 0;  // chunks whose MMAs were issued
     for (int c = 0; c < nch && ok; ++c) {
-      const int sb = c % kBulkStages;
-      if (!mbar_wait(&full[sb], (c / kBulkStages) & 1)) {
+      const int sb = c % S;
+      if (!mbar_wait(&full[sb], (c / S) & 1)) {
         ok = false;
         break;
       }
@@ -521,7 +525,7 @@ __global__ void __launch_bounds__(256, 2)
       mma_commit(&empty[sb]);
       done = c + 1;
       if (issued < nch) {  // refill this stage once its MMAs have read it
-        if (!mbar_wait(&empty[sb], (c / kBulkStages) & 1)) {
+        if (!mbar_wait(&empty[sb], (c / S) & 1)) {
           ok = false;
           break;
         }
@@ -530,16 +534,16 @@ __global__ void __launch_bounds__(256, 2)
     }
     // the last commit covers every MMA issued before it
     bool fine = ok && done == nch &&
-                (nch == 0 || mbar_wait(&empty[(nch - 1) % kBulkStages],
-                                       ((nch - 1) / kBulkStages) & 1));
+                (nch == 0 || mbar_wait(&empty[(nch - 1) % S],
+                                       ((nch - 1) / S) & 1));
     if (!fine) {
       atomicExch(err, 1);
       // let copies and MMAs still in flight land before the memory is
       // released: every issued chunk's copy, then the last commit
       for (int c = done; c < issued; ++c)
-        mbar_wait(&full[c % kBulkStages], (c / kBulkStages) & 1);
+        mbar_wait(&full[c % S], (c / S) & 1);
       if (done > 0)
-        mbar_wait(&empty[(done - 1) % kBulkStages], ((done - 1) / kBulkStages) & 1);
+        mbar_wait(&empty[(done - 1) % S], ((done - 1) / S) & 1);
     }
     wait_ok = fine;
   }
@@ -561,7 +565,11 @@ __global__ void __launch_bounds__(256, 2)
         for (int j = 0; j < 8; ++j) {
           const int n = n0 + j;
           if (C0 + n < m) {
-            float2 d = f22[8 * part + j];
+            float2 d;
+            if (8 * part + j < PF)
+              d = f22[(8 * part + j) % (PF > 0 ? PF : 1)];
+            else
+              d = F[(long long)(C0 + n) * m + R0 + row];
             d.x -= __uint_as_float(cr[j]);
             d.y -= __uint_as_float(ci[j]);
             F[(long long)(C0 + n) * m + R0 + row] = d;
@@ -581,22 +589,31 @@ __global__ void __launch_bounds__(256, 2)
 
 size_t gemm_tc_smem() { return 2 * kStage + 1024; }
 
-size_t gemm_tc_bulk_smem() { return kBulkStages * kStage + 1024; }
+size_t gemm_tc_bulk_smem(int stages) { return stages * kStage + 1024; }
 size_t tc_chunk_image_bytes() { return kChunkImg; }
 
 int launch_gemm_tc_bulk(tlr_ctx *ctx, const int *fl, const int *prefix, const int *pa,
                         const int *pb, int nf, int s, int w, float2 *pool, const DevFront *fr,
                         int tiles, int atiles, int btiles, unsigned char *planes, int *err,
-                        cudaStream_t st) {
+                        cudaStream_t st, int variant) {
   const int nchmax = (w + kTcKC - 1) / kTcKC;
   if (atiles + btiles > 0)
     { k_tc_split<<<dim3(atiles + btiles, nchmax), 256, 0, st>>>(fl, pa, pb, nf, s, w, pool, fr,
                                                                planes, atiles, nchmax); count_launches(); }
-  TLR_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tc_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)gemm_tc_bulk_smem()));
   const unsigned char *pbp = planes + (long long)atiles * nchmax * kChunkImg;
-  { k_gemm_tc_bulk<<<tiles, 256, gemm_tc_bulk_smem(), st>>>(fl, prefix, pa, pb, nf, s, w, pool, fr,
-                                                            planes, pbp, nchmax, err, 128u, 256u); count_launches(); }
+  if (variant == 1) {  // two stages, three CTAs per SM, half the F22 prefetched
+    auto k = k_gemm_tc_bulk<2, 3, 16>;
+    TLR_CUDA(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)gemm_tc_bulk_smem(2)));
+    { k<<<tiles, 256, gemm_tc_bulk_smem(2), st>>>(fl, prefix, pa, pb, nf, s, w, pool, fr, planes,
+                                                 pbp, nchmax, err, 128u, 256u); count_launches(); }
+  } else {
+    auto k = k_gemm_tc_bulk<kBulkStages, 2, 32>;
+    TLR_CUDA(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)gemm_tc_bulk_smem(kBulkStages)));
+    { k<<<tiles, 256, gemm_tc_bulk_smem(kBulkStages), st>>>(fl, prefix, pa, pb, nf, s, w, pool, fr,
+                                                           planes, pbp, nchmax, err, 128u, 256u); count_launches(); }
+  }
   TLR_CUDA(ctx, cudaGetLastError());
   return TLR_OK;
 }
