@@ -204,7 +204,9 @@ typedef struct {
                              GB300's FP64 tensor rate is no higher than its
                              FP64 FMA rate, and measured 13% slower).  3:
                              mixed form, the bulk-copy kernel with a two-
-                             stage ring and three CTAs per SM                */
+                             stage ring and three CTAs per SM (the same
+                             bits as 0; measured 11% slower: 513 vs 460 ms
+                             for a 300 x 192 factorisation)                 */
   int solve_block;        /* mixed form: diagonal-block size of the
                              triangular solves, 128, 256 or 512 (0: 256)     */
   int refinement;         /* mixed form: 0 (default) classic iterative
@@ -246,6 +248,12 @@ typedef struct {
                              neighbouring point of a sweep), vector i of the
                              start block the sum of Ritz vectors i, i +
                              block, ...                                     */
+  int ring_slack_percent; /* nested-dissection ordering of the factor: a box
+                             of the periodic ring is cut across xi when that
+                             separator has at most ring_slack_percent / 100
+                             times the ring cut's nodes (0: 100, the
+                             smallest separator; range [100, 1000]); see
+                             tlr_symbolic_analyze                          */
 } tlr_solve_opts;
 
 typedef struct {

@@ -78,7 +78,8 @@ class SolveOpts(ctypes.Structure):
                 ("solve_block", ctypes.c_int), ("refinement", ctypes.c_int),
                 ("panel_width", ctypes.c_int), ("cluster_panel", ctypes.c_int),
                 ("persistent_solve", ctypes.c_int), ("block", ctypes.c_int),
-                ("nstart", ctypes.c_int), ("warm_start", ctypes.c_int)]
+                ("nstart", ctypes.c_int), ("warm_start", ctypes.c_int),
+                ("ring_slack_percent", ctypes.c_int)]
 
 
 class EigDiag(ctypes.Structure):

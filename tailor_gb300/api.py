@@ -227,7 +227,7 @@ class EigenSolver:
               solve_block: int = 0, refinement: str = "ir",
               panel_width: int = 0, cluster_panel: int = 0,
               fallback: bool = True, block: int = 0,
-              warm_start: bool = False) -> EigenSolution:
+              warm_start: bool = False, ring_slack_percent: int = 0) -> EigenSolution:
         """With fallback, a mixed-form solve (precision 1) that fails to
         converge (or hits a singular pivot or a timed-out device wait) is
         repeated in the plain FP64 form; diag["fallback"] is 1 then.
@@ -235,12 +235,13 @@ class EigenSolver:
         start: one start vector [5N], or several [k][5N] (up to the block
         size); block: Krylov block size (1, 2, 4 or 8; 0 = 1); warm_start:
         without start, begin from the previous solve's Ritz vectors on this
-        problem."""
+        problem.  ring_slack_percent: the factor's nested-dissection
+        ordering (tlr_solve_opts; 0: the smallest separator)."""
         kw = dict(nev=nev, ncv=ncv, tol=tol, max_it=max_it, sigma=sigma, start=start,
                   modes=modes, cuda_core_schur=cuda_core_schur,
                   persistent_solve=persistent_solve, solve_block=solve_block,
                   refinement=refinement, panel_width=panel_width, cluster_panel=cluster_panel,
-                  block=block, warm_start=warm_start)
+                  block=block, warm_start=warm_start, ring_slack_percent=ring_slack_percent)
         if precision == 1 and fallback:
             try:
                 sol = self._solve(precision=1, **kw)
@@ -257,7 +258,8 @@ class EigenSolver:
 
     def _solve(self, nev, ncv, tol, max_it, precision, sigma, start, modes, cuda_core_schur,
                persistent_solve, solve_block, refinement, panel_width,
-               cluster_panel, block=0, warm_start=False) -> EigenSolution:
+               cluster_panel, block=0, warm_start=False,
+               ring_slack_percent=0) -> EigenSolution:
         ph = self.p.case.physics
         k = nev or ph.nev
         opts = L.SolveOpts(nev, ncv, tol, max_it, precision,
@@ -269,7 +271,7 @@ class EigenSolver:
                            int(solve_block), 1 if refinement == "gmres" else 0,
                            int(panel_width), int(cluster_panel),
                            int(bool(persistent_solve)), int(block), 0,
-                           int(bool(warm_start)))
+                           int(bool(warm_start)), int(ring_slack_percent))
         if start is not None:
             st = np.atleast_2d(np.asarray(start, dtype=np.complex128))
             s = np.ascontiguousarray(np.stack([st.real, st.imag], -1), dtype=np.float64)
@@ -353,7 +355,8 @@ class SweepResult:
 def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
           autotune: bool = True, tol: float = 0.0, ncv: int = 0, max_it: int = 0,
           starts=None, device: int = 0, raise_on_error: bool = True,
-          fallback: bool = True, block: int = 0, warm_start: bool = False) -> SweepResult:
+          fallback: bool = True, block: int = 0, warm_start: bool = False,
+          ring_slack_percent: int = 0) -> SweepResult:
     """Batched alpha-sweep (tlr_sweep): points are (class index, alpha) or
     (class index, alpha, Re); each class is a Case (grid, base flow,
     physics) whose alpha (and Re when given) is overridden.  With fallback,
@@ -361,7 +364,8 @@ def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
     the plain FP64 form (diag["fallback_points"] counts them).  block: the
     Krylov block size of every solve; warm_start: each worker takes a
     contiguous run of the points and starts every point but the run's first
-    from its predecessor's Ritz vectors (starts[i], when given, wins)."""
+    from its predecessor's Ritz vectors (starts[i], when given, wins);
+    ring_slack_percent: the factor ordering of every class (tlr_solve_opts)."""
     lib = L.load()
     keep = []
     holder = Problem.__new__(Problem)  # reuse the rule marshalling
@@ -389,7 +393,8 @@ def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
         pts[i] = L.SweepPoint(int(c), complex(a).real, complex(a).imag, s, re_ov)
     k = nev or cases[0].physics.nev
     opts = L.SweepOpts(L.SolveOpts(k, ncv, tol, max_it, precision, 0.0, 0.0, 0, None, 0, 0, 0, 0,
-                                   0, 0, int(block), 0, int(bool(warm_start))),
+                                   0, 0, int(block), 0, int(bool(warm_start)),
+                                   int(ring_slack_percent)),
                        workers, int(bool(autotune)), device)
     lam = np.zeros((max(npts, 1), k, 2))
     res = np.zeros((max(npts, 1), k))

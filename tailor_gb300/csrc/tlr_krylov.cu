@@ -630,13 +630,16 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
       o.panel_width == 32 || o.panel_width == 64 || (o.panel_width == 128 && prec == 1)
           ? o.panel_width
           : (prec == 0 ? 32 : 64);
+  if (o.ring_slack_percent != 0 && (o.ring_slack_percent < 100 || o.ring_slack_percent > 1000))
+    return fail(ctx, TLR_ERR_ARG, "ring_slack_percent must lie in [100, 1000]");
+  const int rslack = o.ring_slack_percent ? o.ring_slack_percent : 100;
 
   // factorisation (reused when sigma, precision and Schur kernel are unchanged)
   Factor *F = ctx->factor;
   if (F && (F->prec != prec || F->sigma_re != sigma.real() || F->sigma_im != sigma.imag() ||
             F->tensor_cores != tc || F->tc_bulk != tc_bulk || F->tc_variant != tc_variant ||
-            F->sw != sblock || F->w != pwidth || !F->factored)) {
-    if (F->prec != prec || F->sw != sblock || F->w != pwidth) {
+            F->sw != sblock || F->w != pwidth || F->ring_slack != rslack || !F->factored)) {
+    if (F->prec != prec || F->sw != sblock || F->w != pwidth || F->ring_slack != rslack) {
       free_factor(ctx);
       F = nullptr;
     } else {
@@ -648,7 +651,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   if (!F) {
     F = new Factor();
     ctx->factor = F;
-    int rc = F->setup(ctx, prec, 48, sblock, pwidth);
+    int rc = F->setup(ctx, prec, 48, sblock, pwidth, rslack);
     if (rc) {
       free_factor(ctx);
       return rc;

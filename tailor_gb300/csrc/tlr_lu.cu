@@ -1773,8 +1773,10 @@ cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block
 
 // ------------------------------------------------------------------- host
 
-int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int panel_width) {
+int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int panel_width,
+                  int ring_slack_percent) {
   prec = precision;
+  ring_slack = ring_slack_percent > 0 ? ring_slack_percent : 100;
   // complex128 panels stop at 64 columns: the TRSM tiles (w x w + w x 33
   // values) must fit in shared memory
   w = panel_width == 32 || panel_width == 64 || (panel_width == 128 && precision == 1)
@@ -1791,7 +1793,7 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int pa
     TLR_CUDA(ctx, cudaMemcpy(cl.data(), ctx->col, cl.size() * sizeof(int),
                              cudaMemcpyDeviceToHost));
     rc = build_symbolic(ctx->ny, ctx->nz, ctx->h_xi_idx, ctx->sx, ctx->h_eta_off, ctx->se, rp,
-                        cl, leaf, sym);
+                        cl, leaf, sym, ring_slack);
     if (rc) {
       char buf[96];
       snprintf(buf, sizeof(buf), "symbolic analysis failed (code %d)", rc);

@@ -58,6 +58,7 @@ struct Factor {
   unsigned char *tc_planes = nullptr;
   int w = 32;    // panel width
   int sw = 128;  // rows of a diagonal block of the solves (128 or 256)
+  int ring_slack = 100;  // nested-dissection ring slack of the ordering, percent
   std::vector<Level> levels;
   void *pool = nullptr, *work = nullptr, *work2 = nullptr, *vec_a = nullptr;
   DevFront *d_fronts = nullptr;
@@ -112,7 +113,8 @@ struct Factor {
   template <int SW, int NR> int solve_impl_m(tlr_ctx *ctx);
   int solve_impl_m_dispatch(tlr_ctx *ctx, int nr);
 
-  int setup(tlr_ctx *ctx, int precision, int leaf, int solve_block = 0, int panel_width = 0);
+  int setup(tlr_ctx *ctx, int precision, int leaf, int solve_block = 0, int panel_width = 0,
+            int ring_slack_percent = 0);
   void release();
   int factor(tlr_ctx *ctx, double sr, double si, double tiny);
   // In-place x <- K^-1 x on a device vector in the factor's precision.

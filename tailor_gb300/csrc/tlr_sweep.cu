@@ -9,9 +9,10 @@
 // starts, a contiguous run of neighbouring points each), so the kernels of
 // several instances overlap on the GPU while each instance's Krylov-Schur
 // driver runs on its own host thread.  With autotuning on, the first
-// context of a class times the factorisation with both Schur-update kernels
-// (tensor cores / CUDA cores) and the triangular solves with both diagonal-
-// block sizes on the class's first point and keeps the fastest pair.
+// context of a class times, on the class's first point, the factorisation
+// with both Schur-update kernels (tensor cores / CUDA cores), the winning
+// kernel with 128-column panels, and the triangular solves with both
+// diagonal-block sizes, and keeps the fastest combination.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -83,7 +84,7 @@ double elapsed_ms(tlr_ctx *ctx) {
 // point: Schur kernel on the 256 block, then the 128 block with the faster
 // kernel, then the faster kernel with 128-column panels (the depth K of the
 // Schur-update tiles) instead of 64.  Leaves ctx without a factor.
-int autotune(tlr_ctx *ctx, ClassState &cs) {
+int autotune(tlr_ctx *ctx, ClassState &cs, int ring_slack) {
   double anorm = 0.0;
   int rc = frobenius(ctx, ctx->A, ctx->nnzb * 25, &anorm);
   if (rc) return rc;
@@ -101,7 +102,7 @@ int autotune(tlr_ctx *ctx, ClassState &cs) {
   for (int bi = 0; bi < 2 && !rc; ++bi) {
     Factor *F = new Factor();
     ctx->factor = F;
-    if ((rc = F->setup(ctx, 1, 48, blocks[bi]))) break;
+    if ((rc = F->setup(ctx, 1, 48, blocks[bi], 0, ring_slack))) break;
     const int ntc = bi == 0 ? 2 : 1;
     for (int k = 0; k < ntc && !rc; ++k) {
       F->tensor_cores = bi == 0 ? k == 0 : !cs.cuda_core_schur;
@@ -120,7 +121,7 @@ int autotune(tlr_ctx *ctx, ClassState &cs) {
     if (rc) break;
     if (bi == 0) {  // the winning kernel with 128-column panels
       Factor *W = new Factor();
-      if ((rc = W->setup(ctx, 1, 48, blocks[bi], 128))) {
+      if ((rc = W->setup(ctx, 1, 48, blocks[bi], 128, ring_slack))) {
         W->release();
         delete W;
         break;
@@ -172,6 +173,11 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
       set_global_error("sweep point with an invalid grid class");
       return TLR_ERR_ARG;
     }
+  const int rs = opts->solve.ring_slack_percent;
+  if (rs != 0 && (rs < 100 || rs > 1000)) {
+    set_global_error("ring_slack_percent must lie in [100, 1000]");
+    return TLR_ERR_ARG;
+  }
   const auto t0 = clock::now();
   const tlr_solve_opts base = opts->solve;
   const int nev = base.nev > 0 ? base.nev : classes[0].recipe->nev;
@@ -202,7 +208,7 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
     }
     const int prec = base.precision == 1 ? 1 : 0;
     if (prec == 1 && opts->autotune) {
-      if ((rc = autotune(ctx, cs[c]))) {
+      if ((rc = autotune(ctx, cs[c], base.ring_slack_percent))) {
         err = ctx->last_error;
         break;
       }
@@ -212,7 +218,8 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
     }
     Factor *F = new Factor();
     ctx->factor = F;
-    if ((rc = F->setup(ctx, prec, 48, cs[c].solve_block, cs[c].panel_width))) {
+    if ((rc = F->setup(ctx, prec, 48, cs[c].solve_block, cs[c].panel_width,
+                       base.ring_slack_percent))) {
       err = ctx->last_error;
       break;
     }
