@@ -75,6 +75,9 @@ DLAM_TOL = 1e-8
 C5_NEV = 8
 C5_BLOCK = 1
 C5_NCV = 64
+# concurrent chains of sweep points on the one GPU (one context and one host
+# thread each; each chain walks its own stretch of the snake)
+C5_CHAINS = 1
 PLAIN_NCV = 32
 # C2: mixed vs plain FP64 at 200 x 128
 C2 = dict(ny=200, nz=128, amplitude=0.08, alpha=1.8, omega=complex(0.3, 0.01), nev=16)
@@ -225,6 +228,77 @@ def plain_step(api, prob, point):
     return sol.lam, sol.residual, sol.diag
 
 
+class Chains:
+    """W concurrent chains of sweep points on one GPU: chain w owns one
+    Problem (its own context and CUDA stream) and one host thread (the
+    library releases the GIL in every call), and warm-starts each point from
+    its own previous point."""
+
+    def __init__(self, api, case_fn, width, device, proposal, block):
+        self.api, self.proposal, self.block = api, proposal, block
+        self.probs = [api.Problem(case_fn(), device=device) for _ in range(width)]
+        self.streams = [p.lib.tlr_stream(p.ctx) for p in self.probs]
+        self.first = [True] * width
+
+    def run(self, seqs, before=None):
+        """seqs[w]: the points of chain w, in order.  before(w, prob) runs
+        ahead of each point (e.g. a host->device field load).  Returns, per
+        chain, [(point, lam, res, diag)]."""
+        out = [[] for _ in self.probs]
+        errors = []
+
+        def work(w):
+            try:
+                for pt in seqs[w]:
+                    if before is not None:
+                        before(w, self.probs[w])
+                    lam, res, diag = c5_step(self.api, self.probs[w], pt, self.first[w],
+                                             self.proposal, self.block)
+                    self.first[w] = False
+                    out[w].append((pt, lam, res, diag))
+            except BaseException as e:  # re-raised on the calling thread
+                errors.append(e)
+
+        if len(self.probs) == 1:
+            work(0)
+        else:
+            threads = [threading.Thread(target=work, args=(w,)) for w in range(len(self.probs))]
+            for t in threads:
+                t.start()
+            for t in threads:
+                t.join()
+        if errors:
+            raise errors[0]
+        return out
+
+    def timed(self, ev, fn):
+        """fn() between CUDA events: the start event on chain 0's stream,
+        which every other chain's stream waits on; every other stream's end
+        is joined into chain 0's stream before the end event."""
+        rt = ev.rt
+        ev.record(ev.a, self.streams[0])
+        for st in self.streams[1:]:
+            rt.cudaStreamWaitEvent(ctypes.c_void_p(st), ev.a, 0)
+        out = fn()
+        for st in self.streams[1:]:
+            e = ctypes.c_void_p()
+            rt.cudaEventCreateWithFlags(ctypes.byref(e), 2)  # cudaEventDisableTiming
+            rt.cudaEventRecord(e, ctypes.c_void_p(st))
+            rt.cudaStreamWaitEvent(ctypes.c_void_p(self.streams[0]), e, 0)
+            rt.cudaEventDestroy(e)
+        ev.record(ev.b, self.streams[0])
+        return out, ev.elapsed_ms()
+
+    def close(self):
+        for p in self.probs:
+            p.close()
+
+
+def split_steps(total, width):
+    """total points over width chains, the first chains taking the remainder."""
+    return [total // width + (1 if w < total % width else 0) for w in range(width)]
+
+
 def run_c2(api, ref_file=GOLDEN / "c2_200x128_eigs.txt"):
     """C2: mixed (single-vector, the bench's earlier headline form) vs plain
     FP64, one pass each after a warm-up, eigenvalues against the oracle."""
@@ -371,6 +445,8 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="first point from a random start")
     ap.add_argument("--block", type=int, default=C5_BLOCK, choices=[1, 2, 4, 8],
                     help="Krylov block size of the combined form")
+    ap.add_argument("--chains", type=int, default=C5_CHAINS,
+                    help="concurrent chains of sweep points of the combined form")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -389,9 +465,22 @@ def main():
     tb.build()
     ref = load_c5_reference()
     pts = c5_points(snake=True)
-    # replicas: each rank walks the sweep from its own offset
+    width = max(1, args.chains)
+    # replicas: each rank walks the sweep from its own offset; chain w of a
+    # rank starts its own stretch of the snake from there
     off = (rank * len(pts)) // max(world, 1)
-    seq = [pts[(off + i) % len(pts)] for i in range(args.warmup + 3 * args.steps)]
+    nstep = split_steps(args.steps, width)
+    per_chain = args.warmup + 2 * max(nstep) + 1
+    seqs = [[pts[(off + (w * len(pts)) // width + i) % len(pts)] for i in range(per_chain)]
+            for w in range(width)]
+    pos = [0] * width
+
+    def take(counts):
+        out = []
+        for w in range(width):
+            out.append(seqs[w][pos[w]:pos[w] + counts[w]])
+            pos[w] += counts[w]
+        return out
 
     proposal, train_s = (None, 0.0)
     if not args.no_learned:
@@ -399,39 +488,35 @@ def main():
 
     case = c5_case()
     ev = Events()
-    prob = api.Problem(case, device=local)
-    stream = prob.lib.tlr_stream(prob.ctx)
-    g = 0
-    for i in range(args.warmup):
-        c5_step(api, prob, seq[g], g == 0, proposal, args.block)
-        g += 1
+    chains = Chains(api, c5_case, width, local, proposal, args.block)
+    prob, stream = chains.probs[0], chains.streams[0]
+    # warm-up: every chain's first point starts from the learned proposal
+    chains.run(take([args.warmup] * width))
 
     def barrier():
         if dist:
             dist.barrier()
+
+    def tally(results):
+        good, worst = 0, None
+        for (pt, lam, res, *_) in results:
+            rl = ref.get((round(pt[1], 9), round(pt[2], 6))) if ref else None
+            gd, w = count_pairs(lam, res, rl)
+            good += gd
+            worst = w if worst is None else (worst if w is None else max(worst, w))
+        return good, worst
 
     # ---- device-resident timing
     clocks = ClockSampler()
     clocks.start()
     barrier()
     launches0 = prob.lib.tlr_kernel_launches()
-    ev.record(ev.a, stream)
-    steps = []
-    for _ in range(args.steps):
-        lam, res, diag = c5_step(api, prob, seq[g], g == 0, proposal, args.block)
-        steps.append((seq[g], lam, res, diag))
-        g += 1
-    ev.record(ev.b, stream)
-    ms = ev.elapsed_ms()
+    per, ms = chains.timed(ev, lambda: chains.run(take(nstep)))
     launches = prob.lib.tlr_kernel_launches() - launches0
     barrier()
     clk = clocks.stop()
-    good_total, worst = 0, None
-    for (pt, lam, res, _) in steps:
-        rl = ref.get((round(pt[1], 9), round(pt[2], 6))) if ref else None
-        gd, w = count_pairs(lam, res, rl)
-        good_total = good_total + gd
-        worst = w if worst is None else (worst if w is None else max(worst, w))
+    steps = [x for chain in per for x in chain]
+    good_total, worst = tally(steps)
     ms, good_total = replicas.reduce_timing(ms, good_total)  # slowest rank, all pairs
     value = good_total / (ms / 1e3)
 
@@ -440,24 +525,27 @@ def main():
     pg, pb = ev.pinned(gbytes), ev.pinned(bbytes)
     ctypes.memmove(pg, case.grid.ctypes.data, gbytes)
     ctypes.memmove(pb, case.baseflow.ctypes.data, bbytes)
+
+    def load(w, p):
+        p.check(p.lib.tlr_load_fields(p.ctx, pg, pb))
+
     barrier()
-    ev.record(ev.a, stream)
-    e2e_steps = []
-    for _ in range(args.steps):
-        prob.check(prob.lib.tlr_load_fields(prob.ctx, pg, pb))
-        lam, res, _ = c5_step(api, prob, seq[g], False, proposal, args.block)
-        e2e_steps.append((seq[g], lam, res))
-        g += 1
-    ev.record(ev.b, stream)
-    ms_e2e = ev.elapsed_ms()
+    per_e2e, ms_e2e = chains.timed(ev, lambda: chains.run(take(nstep), before=load))
     barrier()
-    good_e2e = 0
-    for (pt, lam, res) in e2e_steps:
-        rl = ref.get((round(pt[1], 9), round(pt[2], 6))) if ref else None
-        good_e2e += count_pairs(lam, res, rl)[0]
+    good_e2e = tally([x for chain in per_e2e for x in chain])[0]
     ms_e2e, good_e2e = replicas.reduce_timing(ms_e2e, good_e2e)
     e2e = good_e2e / (ms_e2e / 1e3)
     d2h = C5_NEV * (16 + 8)
+
+    # ---- the solve kernels alone: with concurrent chains, chain 0 solves one
+    # more point by itself, so the per-solve times the roofline uses carry no
+    # other chain's kernels
+    if width > 1:
+        solo = chains.run(take([1] + [0] * (width - 1)))[0]
+        rsteps = solo
+    else:
+        rsteps = steps
+    last = rsteps[-1][3]
 
     # ---- plain FP64 on a stated subset of the same points (rank 0)
     plain = None
@@ -467,12 +555,7 @@ def main():
         pres = [plain_step(api, prob, pt) for pt in sub]
         ev.record(ev.b, stream)
         pms = ev.elapsed_ms()
-        pgood, pworst = 0, None
-        for pt, (lam, res, _) in zip(sub, pres):
-            rl = ref.get((round(pt[1], 9), round(pt[2], 6))) if ref else None
-            gd, w = count_pairs(lam, res, rl)
-            pgood = pgood + gd
-            pworst = w if pworst is None else (pworst if w is None else max(pworst, w))
+        pgood, pworst = tally([(pt, lam, res) for pt, (lam, res, _) in zip(sub, pres)])
         pv = pgood / (pms / 1e3)
         plain = {"value": pv, "unit": UNIT, "points": [[p[1], p[2]] for p in sub],
                  "ms_per_point": pms / len(sub), "eigenpairs": pgood,
@@ -480,8 +563,7 @@ def main():
                  "factor_ms": [r[2]["factor_ms"] for r in pres],
                  "krylov_ms": [r[2]["krylov_ms"] for r in pres],
                  "combined_vs_plain": value / pv if pv > 0 else None}
-    last = steps[-1][3]
-    prob.close()
+    chains.close()
 
     c2 = None if (args.no_c2 or rank != 0) else run_c2(api)
     sweep = None
@@ -502,8 +584,8 @@ def main():
     # block's vectors), CUDA events around every replay
     nvec = last.get("block", 1)
     tri_bytes = last["factor_bytes"] + 2 * nvec * 5 * case.nodes * 8
-    tri_ms = sum(s[3]["trisolve_ms"] for s in steps)
-    tri_n = sum(s[3]["trisolves"] for s in steps)
+    tri_ms = sum(s[3]["trisolve_ms"] for s in rsteps)
+    tri_n = sum(s[3]["trisolves"] for s in rsteps)
     tri_avg_ms = tri_ms / max(tri_n, 1)
     achieved = tri_bytes / (tri_avg_ms * 1e-3) / 1e9 if tri_avg_ms > 0 else 0.0
     traffic = None
@@ -522,10 +604,11 @@ def main():
                                "alpha x Re on 8x4 in [0.5,3.5]x[800,2400], snake order, one "
                                "point per step, nev 8, target 0",
                    "form": "learned + mixed + batched", "block": args.block,
-                   "ncv": c5_ncv(args.block),
+                   "ncv": c5_ncv(args.block), "chains": width,
                    "points": [[s[0][1], s[0][2]] for s in steps],
                    "l2": "operator 1.8 GB and factor 10 GB per point, larger than L2 (no flush)",
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "replicas" if world > 1 else
+                   ("single" if width == 1 else "%d concurrent chains on one GPU" % width)},
         "parity": {"reference": "tests/golden/c5_300x192_plain_eigs.txt" if ref else None,
                    "max_dlambda_rel": worst, "resid_tol": RESID_TOL, "dlambda_tol": DLAM_TOL},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": gbytes + bbytes,

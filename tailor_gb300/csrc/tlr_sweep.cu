@@ -103,6 +103,10 @@ int autotune(tlr_ctx *ctx, ClassState &cs, int ring_slack) {
     Factor *F = new Factor();
     ctx->factor = F;
     if ((rc = F->setup(ctx, 1, 48, blocks[bi], 0, ring_slack))) break;
+    if (!cs.sym) {  // one symbolic analysis for every factor of the class
+      cs.sym.reset(new Symbolic(F->sym));
+      ctx->shared_sym = cs.sym.get();
+    }
     const int ntc = bi == 0 ? 2 : 1;
     for (int k = 0; k < ntc && !rc; ++k) {
       F->tensor_cores = bi == 0 ? k == 0 : !cs.cuda_core_schur;
@@ -223,7 +227,7 @@ extern "C" int tlr_sweep(const tlr_grid_class *classes, int nclass, const tlr_sw
       err = ctx->last_error;
       break;
     }
-    cs[c].sym.reset(new Symbolic(F->sym));
+    if (!cs[c].sym) cs[c].sym.reset(new Symbolic(F->sym));
   }
   if (rc) {
     for (auto &w : ctxs)
