@@ -251,9 +251,17 @@ typedef struct {
   int ring_slack_percent; /* nested-dissection ordering of the factor: a box
                              of the periodic ring is cut across xi when that
                              separator has at most ring_slack_percent / 100
-                             times the ring cut's nodes (0: 100, the
-                             smallest separator; range [100, 1000]); see
-                             tlr_symbolic_analyze                          */
+                             times the ring cut's nodes (0: 110, slightly
+                             wider separators for shallower top fronts; 100:
+                             the smallest separator; range [100, 1000]);
+                             see tlr_symbolic_analyze                      */
+  int conv_check;         /* > 0: also test convergence inside a Krylov-
+                             Schur expansion, every conv_check operator
+                             applications once the basis holds more than
+                             nev vectors, and stop as soon as nev Ritz pairs
+                             meet the tolerance (estimates, then explicit
+                             residuals); 0: only when the basis is full, as
+                             SLEPc                                          */
 } tlr_solve_opts;
 
 typedef struct {
@@ -275,6 +283,7 @@ typedef struct {
                              first solve, the first and the second correction */
   int block;              /* Krylov block size used (vectors per triangular
                              solve in the mixed form)                       */
+  int conv_checks;        /* convergence checks made inside expansions      */
 } tlr_eig_diag;
 
 /* lambda [nev] complex, residual [nev]; modes [nev][5N] complex or NULL. */
@@ -421,7 +430,7 @@ int tlr_pencil_create(const tlr_recipe *recipe, int n, const double *A, const do
  * fronts (0: the solver's 48).  ring_slack_percent: a box of the periodic
  * ring is cut across xi instead of across the ring when that separator
  * has at most this percentage of the ring cut's nodes (0: the solver's
- * 100; 100..1000).  Optional outputs: node_rank[Ny*Nz] (elimination
+ * 110; 100..1000).  Optional outputs: node_rank[Ny*Nz] (elimination
  * position of node j*Ny + i), node_front[Ny*Nz] (front that eliminates
  * it), front_parent[front_capacity] (-1 for the root; fronts are numbered
  * in postorder).  *info is filled first, so a call with front_parent NULL

@@ -79,7 +79,7 @@ class SolveOpts(ctypes.Structure):
                 ("panel_width", ctypes.c_int), ("cluster_panel", ctypes.c_int),
                 ("persistent_solve", ctypes.c_int), ("block", ctypes.c_int),
                 ("nstart", ctypes.c_int), ("warm_start", ctypes.c_int),
-                ("ring_slack_percent", ctypes.c_int)]
+                ("ring_slack_percent", ctypes.c_int), ("conv_check", ctypes.c_int)]
 
 
 class EigDiag(ctypes.Structure):
@@ -95,7 +95,7 @@ class EigDiag(ctypes.Structure):
                 ("trisolve_ms", ctypes.c_double), ("trisolves", ctypes.c_int),
                 ("ortho_ms", ctypes.c_double), ("dense_ms", ctypes.c_double),
                 ("residual_ms", ctypes.c_double), ("refine_res", ctypes.c_double * 3),
-                ("block", ctypes.c_int)]
+                ("block", ctypes.c_int), ("conv_checks", ctypes.c_int)]
 
 
 class GridClass(ctypes.Structure):

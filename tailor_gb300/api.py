@@ -227,7 +227,8 @@ class EigenSolver:
               solve_block: int = 0, refinement: str = "ir",
               panel_width: int = 0, cluster_panel: int = 0,
               fallback: bool = True, block: int = 0,
-              warm_start: bool = False, ring_slack_percent: int = 0) -> EigenSolution:
+              warm_start: bool = False, ring_slack_percent: int = 0,
+              conv_check: int = 0) -> EigenSolution:
         """With fallback, a mixed-form solve (precision 1) that fails to
         converge (or hits a singular pivot or a timed-out device wait) is
         repeated in the plain FP64 form; diag["fallback"] is 1 then.
@@ -236,12 +237,15 @@ class EigenSolver:
         size); block: Krylov block size (1, 2, 4 or 8; 0 = 1); warm_start:
         without start, begin from the previous solve's Ritz vectors on this
         problem.  ring_slack_percent: the factor's nested-dissection
-        ordering (tlr_solve_opts; 0: the smallest separator)."""
+        ordering (tlr_solve_opts; 0: the smallest separator); conv_check:
+        operator applications between convergence tests inside an
+        expansion (0: only when the basis is full)."""
         kw = dict(nev=nev, ncv=ncv, tol=tol, max_it=max_it, sigma=sigma, start=start,
                   modes=modes, cuda_core_schur=cuda_core_schur,
                   persistent_solve=persistent_solve, solve_block=solve_block,
                   refinement=refinement, panel_width=panel_width, cluster_panel=cluster_panel,
-                  block=block, warm_start=warm_start, ring_slack_percent=ring_slack_percent)
+                  block=block, warm_start=warm_start, ring_slack_percent=ring_slack_percent,
+                  conv_check=conv_check)
         if precision == 1 and fallback:
             try:
                 sol = self._solve(precision=1, **kw)
@@ -259,7 +263,7 @@ class EigenSolver:
     def _solve(self, nev, ncv, tol, max_it, precision, sigma, start, modes, cuda_core_schur,
                persistent_solve, solve_block, refinement, panel_width,
                cluster_panel, block=0, warm_start=False,
-               ring_slack_percent=0) -> EigenSolution:
+               ring_slack_percent=0, conv_check=0) -> EigenSolution:
         ph = self.p.case.physics
         k = nev or ph.nev
         opts = L.SolveOpts(nev, ncv, tol, max_it, precision,
@@ -271,7 +275,7 @@ class EigenSolver:
                            int(solve_block), 1 if refinement == "gmres" else 0,
                            int(panel_width), int(cluster_panel),
                            int(bool(persistent_solve)), int(block), 0,
-                           int(bool(warm_start)), int(ring_slack_percent))
+                           int(bool(warm_start)), int(ring_slack_percent), int(conv_check))
         if start is not None:
             st = np.atleast_2d(np.asarray(start, dtype=np.complex128))
             s = np.ascontiguousarray(np.stack([st.real, st.imag], -1), dtype=np.float64)
@@ -356,7 +360,7 @@ def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
           autotune: bool = True, tol: float = 0.0, ncv: int = 0, max_it: int = 0,
           starts=None, device: int = 0, raise_on_error: bool = True,
           fallback: bool = True, block: int = 0, warm_start: bool = False,
-          ring_slack_percent: int = 0) -> SweepResult:
+          ring_slack_percent: int = 0, conv_check: int = 0) -> SweepResult:
     """Batched alpha-sweep (tlr_sweep): points are (class index, alpha) or
     (class index, alpha, Re); each class is a Case (grid, base flow,
     physics) whose alpha (and Re when given) is overridden.  With fallback,
@@ -365,7 +369,7 @@ def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
     Krylov block size of every solve; warm_start: each worker takes a
     contiguous run of the points and starts every point but the run's first
     from its predecessor's Ritz vectors (starts[i], when given, wins);
-    ring_slack_percent: the factor ordering of every class (tlr_solve_opts)."""
+    ring_slack_percent, conv_check: as for EigenSolver.solve, for every point."""
     lib = L.load()
     keep = []
     holder = Problem.__new__(Problem)  # reuse the rule marshalling
@@ -394,7 +398,7 @@ def sweep(cases, points, nev: int = 0, precision: int = 1, workers: int = 0,
     k = nev or cases[0].physics.nev
     opts = L.SweepOpts(L.SolveOpts(k, ncv, tol, max_it, precision, 0.0, 0.0, 0, None, 0, 0, 0, 0,
                                    0, 0, int(block), 0, int(bool(warm_start)),
-                                   int(ring_slack_percent)),
+                                   int(ring_slack_percent), int(conv_check)),
                        workers, int(bool(autotune)), device)
     lam = np.zeros((max(npts, 1), k, 2))
     res = np.zeros((max(npts, 1), k))

@@ -632,7 +632,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
           : (prec == 0 ? 32 : 64);
   if (o.ring_slack_percent != 0 && (o.ring_slack_percent < 100 || o.ring_slack_percent > 1000))
     return fail(ctx, TLR_ERR_ARG, "ring_slack_percent must lie in [100, 1000]");
-  const int rslack = o.ring_slack_percent ? o.ring_slack_percent : 100;
+  const int rslack = o.ring_slack_percent ? o.ring_slack_percent : kRingSlackDefault;
 
   // factorisation (reused when sigma, precision and Schur kernel are unchanged)
   Factor *F = ctx->factor;
@@ -821,15 +821,15 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   auto ms_since = [](clock::time_point t) {
     return std::chrono::duration<double, std::milli>(clock::now() - t).count();
   };
-  auto finalize = [&](const dense::Mat &Tq, const dense::Mat &Qq) -> int {
+  auto finalize = [&](const dense::Mat &Tq, const dense::Mat &Qq, int m) -> int {
     const auto tf = clock::now();
-    std::vector<double2> yh((size_t)ncv * nout);
+    std::vector<double2> yh((size_t)m * nout);
     for (int i = 0; i < nout; ++i) {
       const auto yv = dense::tri_eigvec(Tq, i);
-      for (int q = 0; q < ncv; ++q) {
+      for (int q = 0; q < m; ++q) {
         cd sacc = 0.0;
         for (int t = 0; t <= i; ++t) sacc += Qq(q, t) * yv[t];
-        yh[(size_t)i * ncv + q] = make_double2(sacc.real(), sacc.imag());
+        yh[(size_t)i * m + q] = make_double2(sacc.real(), sacc.imag());
       }
     }
     // the host writes the pinned stage only after the stream has drained
@@ -837,7 +837,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     std::copy(yh.begin(), yh.end(), ws->ypin);
     TLR_CUDA(ctx, cudaMemcpyAsync(ws->ybuf, ws->ypin, yh.size() * sizeof(double2),
                                   cudaMemcpyHostToDevice, ctx->stream));
-    int rc = kv_combine(ctx, n, S.V, n, ncv, ws->ybuf, ncv, nout, S.tmp, n);
+    int rc = kv_combine(ctx, n, S.V, n, m, ws->ybuf, m, nout, S.tmp, n);
     if (rc) return rc;
     const int nb = ctx->partial_blocks;
     for (int i = 0; i < nout; ++i) {
@@ -872,10 +872,84 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   // projected matrix H is (ncv + bsz) x ncv, block upper Hessenberg with
   // lower bandwidth bsz during an expansion
   dense::Mat H(ncv + bsz, ncv);
-  int k = 0, nconv = 0, it = 0, reason = 0;
+  int k = 0, nconv = 0, it = 0, reason = 0, checks = 0;
+  bool early = false;
   // device coefficient columns: pass p, column j at hd + (p * ncv + j) * ldh
   const int ldh = ncv + Factor::kMaxRhs;
   auto hcol = [&](int pass, int j) { return ws->hd + ((size_t)pass * ncv + j) * ldh; };
+  // columns k0 .. m-1 of H from the device (both Gram-Schmidt passes summed,
+  // the new vectors' norms below the diagonal)
+  auto fetch_h = [&](int k0, int m) -> int {
+    const size_t stride = (size_t)ncv * ldh;
+    double *hbeta = reinterpret_cast<double *>(ws->hpin + 2 * stride);
+    for (int pass = 0; pass < 2; ++pass)
+      TLR_CUDA(ctx, cudaMemcpyAsync(ws->hpin + pass * stride + (size_t)k0 * ldh, hcol(pass, k0),
+                                    sizeof(double2) * (m - k0) * ldh, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+    TLR_CUDA(ctx, cudaMemcpyAsync(hbeta + k0, ws->betad + k0, sizeof(double) * (m - k0),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int j = k0; j < m; ++j) {
+      const double2 *h1 = ws->hpin + (size_t)j * ldh;
+      const double2 *h2 = ws->hpin + stride + (size_t)j * ldh;
+      for (int i = 0; i < j + bsz; ++i) H(i, j) = cd(h1[i].x + h2[i].x, h1[i].y + h2[i].y);
+      for (int i = j + bsz; i < ncv + bsz; ++i) H(i, j) = 0.0;
+      H(j + bsz, j) = hbeta[j];
+      if (!(hbeta[j] > 0) || !std::isfinite(hbeta[j]))
+        return fail(ctx, TLR_ERR_NOT_CONVERGED, "Arnoldi breakdown");
+    }
+    return TLR_OK;
+  };
+  // projected problem of the leading m basis vectors: Schur form
+  // T = Q^* H(0:m, 0:m) Q with the wanted (largest |theta|) first, and the
+  // residual rows of the decomposition in the Schur basis, EQ = H(m : m +
+  // bsz, 0 : m) Q
+  auto project = [&](int m, dense::Mat &T, dense::Mat &Q, dense::Mat &EQ) -> int {
+    T = dense::Mat(m, m);
+    Q = dense::Mat(m, m);
+    for (int j = 0; j < m; ++j) {
+      for (int i = 0; i < m; ++i) T(i, j) = H(i, j);
+      Q(j, j) = 1.0;
+    }
+    dense::hessenberg(T, Q);
+    if (!dense::schur(T, Q))
+      return fail(ctx, TLR_ERR_NOT_CONVERGED, "projected Schur form did not converge");
+    for (int pos = 0; pos < m; ++pos) {  // selection by |theta|, stable
+      int best = pos;
+      for (int q = pos + 1; q < m; ++q)
+        if (std::abs(T(q, q)) > std::abs(T(best, best))) best = q;
+      for (int q = best - 1; q >= pos; --q) dense::swap_adjacent(T, Q, q);
+    }
+    EQ = dense::Mat(bsz, m);
+    for (int r = 0; r < bsz; ++r)
+      for (int i = 0; i < m; ++i) {
+        cd acc = 0.0;
+        for (int q = 0; q < m; ++q) acc += H(m + r, q) * Q(q, i);
+        EQ(r, i) = acc;
+      }
+    return TLR_OK;
+  };
+  // leading Ritz pairs whose residual estimate meets tl relative to |theta|
+  auto count_conv = [&](const dense::Mat &T, const dense::Mat &EQ, int m, double tl) {
+    int c = 0;
+    for (int i = 0; i < m; ++i) {
+      const auto yv = dense::tri_eigvec(T, i);
+      double ny = 0.0, nr = 0.0;
+      for (int q = 0; q <= i; ++q) ny += std::norm(yv[q]);
+      for (int r = 0; r < bsz; ++r) {
+        cd dot = 0.0;
+        for (int q = 0; q <= i; ++q) dot += EQ(r, q) * yv[q];
+        nr += std::norm(dot);
+      }
+      if (std::sqrt(nr / ny) <= tl * std::abs(T(i, i))) ++c;
+      else break;
+    }
+    return c;
+  };
+  // convergence checks inside an expansion: every `check` applications
+  // once the basis holds nev + 1 vectors (0: at the end of each expansion)
+  if (o.conv_check < 0) return fail(ctx, TLR_ERR_ARG, "conv_check must not be negative");
+  const int check = o.conv_check;
   while (true) {
     ++it;
     // block Arnoldi expansion of columns k .. ncv-1: OP on bsz vectors at
@@ -900,75 +974,49 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
       }
       if (rc) return rc;
       ortho_ms += ms_since(to);
+      // a convergence check on the partial decomposition of m vectors: the
+      // wanted pairs may meet the tolerance before the basis is full
+      const int m = j0 + bsz;
+      if (check > 0 && m < ncv && m > nev && (m - k) % check == 0 && (m - k) >= check) {
+        const auto tc = clock::now();
+        if ((rc = fetch_h(k, m))) return rc;
+        dense::Mat Tm, Qm, Em;
+        if ((rc = project(m, Tm, Qm, Em))) return rc;
+        const int nc = count_conv(Tm, Em, m, tol_int);
+        dense_ms += ms_since(tc);
+        ++checks;
+        if (nc >= nev) {
+          if ((rc = finalize(Tm, Qm, m))) return rc;
+          if (maxerr <= tol) {
+            nconv = nc;
+            early = true;
+            break;
+          }
+        }
+      }
+    }
+    if (early) {
+      reason = 1;
+      break;
     }
     if (k < ncv) {
       const auto to = clock::now();
-      const size_t stride = (size_t)ncv * ldh;
-      double *hbeta = reinterpret_cast<double *>(ws->hpin + 2 * stride);
-      for (int pass = 0; pass < 2; ++pass)
-        TLR_CUDA(ctx, cudaMemcpyAsync(ws->hpin + pass * stride + (size_t)k * ldh, hcol(pass, k),
-                                      sizeof(double2) * (ncv - k) * ldh, cudaMemcpyDeviceToHost,
-                                      ctx->stream));
-      TLR_CUDA(ctx, cudaMemcpyAsync(hbeta + k, ws->betad + k, sizeof(double) * (ncv - k),
-                                    cudaMemcpyDeviceToHost, ctx->stream));
-      TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-      for (int j = k; j < ncv; ++j) {
-        const double2 *h1 = ws->hpin + (size_t)j * ldh;
-        const double2 *h2 = ws->hpin + stride + (size_t)j * ldh;
-        for (int i = 0; i < j + bsz; ++i) H(i, j) = cd(h1[i].x + h2[i].x, h1[i].y + h2[i].y);
-        for (int i = j + bsz; i < ncv + bsz; ++i) H(i, j) = 0.0;
-        H(j + bsz, j) = hbeta[j];
-        if (!(hbeta[j] > 0) || !std::isfinite(hbeta[j]))
-          return fail(ctx, TLR_ERR_NOT_CONVERGED, "Arnoldi breakdown");
-      }
+      int rc = fetch_h(k, ncv);
+      if (rc) return rc;
       ortho_ms += ms_since(to);
     }
     // projected problem: Schur form, wanted first
     const auto td = clock::now();
-    dense::Mat T(ncv, ncv), Q(ncv, ncv);
-    for (int j = 0; j < ncv; ++j) {
-      for (int i = 0; i < ncv; ++i) T(i, j) = H(i, j);
-      Q(j, j) = 1.0;
+    dense::Mat T, Q, EQ;
+    {
+      const int rc = project(ncv, T, Q, EQ);
+      if (rc) return rc;
     }
-    dense::hessenberg(T, Q);
-    if (!dense::schur(T, Q))
-      return fail(ctx, TLR_ERR_NOT_CONVERGED, "projected Schur form did not converge");
-    for (int pos = 0; pos < ncv; ++pos) {  // selection by |theta|, stable
-      int best = pos;
-      for (int q = pos + 1; q < ncv; ++q)
-        if (std::abs(T(q, q)) > std::abs(T(best, best))) best = q;
-      for (int q = best - 1; q >= pos; --q) dense::swap_adjacent(T, Q, q);
-    }
-    // residual rows of the decomposition in the Schur basis: E Q, E =
-    // H(ncv : ncv + bsz, 0 : ncv)
-    dense::Mat EQ(bsz, ncv);
-    for (int r = 0; r < bsz; ++r)
-      for (int i = 0; i < ncv; ++i) {
-        cd acc = 0.0;
-        for (int q = 0; q < ncv; ++q) acc += H(ncv + r, q) * Q(q, i);
-        EQ(r, i) = acc;
-      }
-    auto count_conv = [&](double tl) {
-      int c = 0;
-      for (int i = 0; i < ncv; ++i) {
-        const auto yv = dense::tri_eigvec(T, i);
-        double ny = 0.0, nr = 0.0;
-        for (int q = 0; q <= i; ++q) ny += std::norm(yv[q]);
-        for (int r = 0; r < bsz; ++r) {
-          cd dot = 0.0;
-          for (int q = 0; q <= i; ++q) dot += EQ(r, q) * yv[q];
-          nr += std::norm(dot);
-        }
-        if (std::sqrt(nr / ny) <= tl * std::abs(T(i, i))) ++c;
-        else break;
-      }
-      return c;
-    };
-    nconv = count_conv(tol_int);
+    nconv = count_conv(T, EQ, ncv, tol_int);
     dense_ms += ms_since(td);
     bool done = false;
     if (nconv >= nev) {
-      int rc = finalize(T, Q);
+      int rc = finalize(T, Q, ncv);
       if (rc) return rc;
       if (maxerr <= tol || tighten >= 4 || tol_int <= 1e-14) {
         done = true;
@@ -978,11 +1026,11 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
         // tolerance: tighten the internal criterion and keep iterating.
         tol_int = std::max(tol_int * 0.05, 1e-14);
         ++tighten;
-        nconv = count_conv(tol_int);
+        nconv = count_conv(T, EQ, ncv, tol_int);
       }
     }
     if (!done && it >= max_it) {
-      int rc = finalize(T, Q);
+      int rc = finalize(T, Q, ncv);
       if (rc) return rc;
       reason = -1;
       done = true;
@@ -1057,6 +1105,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     d.residual_ms = residual_ms;
     for (int q = 0; q < 3; ++q) d.refine_res[q] = S.refine_res[q];
     d.block = bsz;
+    d.conv_checks = checks;
     *diag = d;
   }
   if (reason != 1) {

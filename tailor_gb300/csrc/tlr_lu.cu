@@ -1776,7 +1776,7 @@ cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block
 int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int panel_width,
                   int ring_slack_percent) {
   prec = precision;
-  ring_slack = ring_slack_percent > 0 ? ring_slack_percent : 100;
+  ring_slack = ring_slack_percent > 0 ? ring_slack_percent : kRingSlackDefault;
   // complex128 panels stop at 64 columns: the TRSM tiles (w x w + w x 33
   // values) must fit in shared memory
   w = panel_width == 32 || panel_width == 64 || (panel_width == 128 && precision == 1)

@@ -58,7 +58,7 @@ struct Factor {
   unsigned char *tc_planes = nullptr;
   int w = 32;    // panel width
   int sw = 128;  // rows of a diagonal block of the solves (128 or 256)
-  int ring_slack = 100;  // nested-dissection ring slack of the ordering, percent
+  int ring_slack = kRingSlackDefault;  // nested-dissection ring slack, percent
   std::vector<Level> levels;
   void *pool = nullptr, *work = nullptr, *work2 = nullptr, *vec_a = nullptr;
   DevFront *d_fronts = nullptr;

@@ -255,7 +255,7 @@ extern "C" int tlr_symbolic_analyze(const tlr_rule *xi, const tlr_rule *eta, int
     return bad(TLR_ERR_SIZE, "FD-q node counts or degrees out of range");
   if ((long long)ny * nz > INT_MAX / 128) return bad(TLR_ERR_SIZE, "grid too large");
   if (leaf_nodes == 0) leaf_nodes = 48;
-  if (ring_slack_percent == 0) ring_slack_percent = 100;
+  if (ring_slack_percent == 0) ring_slack_percent = tlr::kRingSlackDefault;
   if (leaf_nodes < 1) return bad(TLR_ERR_ARG, "leaf_nodes must be positive");
   if (ring_slack_percent < 100 || ring_slack_percent > 1000)
     return bad(TLR_ERR_ARG, "ring_slack_percent must lie in [100, 1000]");

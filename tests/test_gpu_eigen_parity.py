@@ -65,6 +65,19 @@ def test_c1_eigenvalues_match_the_oracle(c1_problem, precision, block):
     _check(sol, ref, 8)
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_convergence_checks_inside_the_expansion(c1_problem, precision):
+    """conv_check = 4: convergence is also tested every four applications
+    inside an expansion, and the solve stops at the first basis size where
+    all eight pairs meet the tolerance; the eigenpairs are still the
+    oracle's."""
+    ref = _oracle("c1_100x50_eigs.txt")
+    sol = api.EigenSolver(c1_problem).solve(nev=8, precision=precision, conv_check=4,
+                                            fallback=False)
+    _check(sol, ref, 8)
+    assert sol.diag["conv_checks"] > 0
+
+
 def test_c2_eigenvalues_match_the_oracle(gpu_lib):
     """C2 (200 x 128, bump 0.08, alpha 1.8, omega 0.3 + 0.01i, nev 16) in
     both forms: the mixed form's eigenvalues are within 1e-8 of the FP64

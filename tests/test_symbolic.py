@@ -119,27 +119,28 @@ def test_tree_is_a_valid_multifrontal_structure(ny, nz, leaf, slack):
 
 def test_default_ordering_is_the_solvers():
     """200 x 128 (128 000 unknowns): the flops and complex64 factor bytes
-    tlr_solve reports for this grid's factorisation."""
+    tlr_solve reports for this grid's factorisation (ring slack 110)."""
     xi, eta = _grid_rules(200, 128)
     res = api.symbolic_analysis(xi, eta)
-    assert res["flops"] == pytest.approx(5986159153333.333, rel=1e-12)
-    assert res["factor_elems"] * 8 == 3884108000
-    assert res["fronts"] == 672 and res["levels"] == 11
-    same = api.symbolic_analysis(xi, eta, 48, 100)
+    assert res["flops"] == pytest.approx(5428264403333.333, rel=1e-12)
+    assert res["factor_elems"] * 8 == 3784518000
+    assert res["fronts"] == 673 and res["levels"] == 11
+    same = api.symbolic_analysis(xi, eta, 48, 110)
     assert np.array_equal(same["node_rank"], res["node_rank"])
 
 
 def test_ring_slack_trades_separators():
-    """Accepting xi-cuts of ring boxes up to 1.2x the ring cut lowers the
-    200 x 128 factorisation by about 9% and leaves 60 x 32 unchanged."""
+    """Accepting xi-cuts of ring boxes up to 1.1x the ring cut (the solver's
+    ordering) lowers the 200 x 128 factorisation by about 9% against the
+    smallest separators, and leaves 60 x 32 unchanged."""
     xi, eta = _grid_rules(200, 128)
-    base = api.symbolic_analysis(xi, eta)
-    wide = api.symbolic_analysis(xi, eta, 0, 120)
+    base = api.symbolic_analysis(xi, eta, 0, 100)
+    wide = api.symbolic_analysis(xi, eta)
     assert wide["flops"] < 0.92 * base["flops"]
     assert wide["factor_elems"] < base["factor_elems"]
     xs, es = _grid_rules(60, 32)
     assert np.array_equal(api.symbolic_analysis(xs, es)["node_rank"],
-                          api.symbolic_analysis(xs, es, 0, 120)["node_rank"])
+                          api.symbolic_analysis(xs, es, 0, 100)["node_rank"])
 
 
 def test_argument_errors():
