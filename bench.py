@@ -626,8 +626,8 @@ def main():
                    if last["factor_ms"] > 0 else 0.0},
         "solve": {k: last[k] for k in ("iterations", "solves", "refinement_steps", "factor_ms",
                                        "krylov_ms", "total_ms", "max_relative_error",
-                                       "trisolve_ms", "trisolves", "ortho_ms", "dense_ms",
-                                       "residual_ms")},
+                                       "solve_ms", "trisolve_ms", "trisolves", "ortho_ms",
+                                       "dense_ms", "residual_ms", "conv_checks")},
         "learned": {"train_points": 48, "grid": [60, 32], "train_s": train_s}
         if proposal is not None else None,
         "plain_fp64": plain,

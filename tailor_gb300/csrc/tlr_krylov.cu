@@ -25,6 +25,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <functional>
 #include <vector>
 
 #include "tlr_complex.cuh"
@@ -135,6 +136,18 @@ struct Solver {
         cudaStreamSynchronize(ctx->stream) != cudaSuccess)
       return NAN;
     return hnorm[2];
+  }
+
+  // host work to run while the GPU applies K^-1 (a convergence check of the
+  // partial decomposition): started after the application's launches and
+  // before its synchronisation, once
+  std::function<void()> while_waiting;
+  void host_work() {
+    if (while_waiting) {
+      auto f = std::move(while_waiting);
+      while_waiting = nullptr;
+      f();
+    }
   }
 
   double solve_ms = 0.0;
@@ -466,6 +479,7 @@ struct Solver {
       TLR_CUDA(ctx, cudaMemcpyAsync(out, in, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
       int rc = F->solve(ctx, out);
       ++solves;
+      host_work();
       return rc;
     }
     // FP32 factor + FP64 iterative refinement
@@ -477,6 +491,7 @@ struct Solver {
       count_launches(ref_kernels);
       solves += 3;
       refine += 2;
+      host_work();
       TLR_CUDA(ctx, cudaStreamSynchronize(st));
       const double nr = hnorm[0], ny = hnorm[1];
       for (int q = 0; q < 3; ++q) {
@@ -879,16 +894,11 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   auto hcol = [&](int pass, int j) { return ws->hd + ((size_t)pass * ncv + j) * ldh; };
   // columns k0 .. m-1 of H from the device (both Gram-Schmidt passes summed,
   // the new vectors' norms below the diagonal)
-  auto fetch_h = [&](int k0, int m) -> int {
-    const size_t stride = (size_t)ncv * ldh;
-    double *hbeta = reinterpret_cast<double *>(ws->hpin + 2 * stride);
-    for (int pass = 0; pass < 2; ++pass)
-      TLR_CUDA(ctx, cudaMemcpyAsync(ws->hpin + pass * stride + (size_t)k0 * ldh, hcol(pass, k0),
-                                    sizeof(double2) * (m - k0) * ldh, cudaMemcpyDeviceToHost,
-                                    ctx->stream));
-    TLR_CUDA(ctx, cudaMemcpyAsync(hbeta + k0, ws->betad + k0, sizeof(double) * (m - k0),
-                                  cudaMemcpyDeviceToHost, ctx->stream));
-    TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const size_t hstride = (size_t)ncv * ldh;
+  double *hbeta = reinterpret_cast<double *>(ws->hpin + 2 * hstride);
+  // columns k0 .. m-1 of H from their pinned copies
+  auto fill_h = [&](int k0, int m) -> int {
+    const size_t stride = hstride;
     for (int j = k0; j < m; ++j) {
       const double2 *h1 = ws->hpin + (size_t)j * ldh;
       const double2 *h2 = ws->hpin + stride + (size_t)j * ldh;
@@ -900,6 +910,27 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
     }
     return TLR_OK;
   };
+  // asynchronous copies of columns k0 .. m-1 to the pinned stage
+  auto copy_h = [&](int k0, int m) -> int {
+    for (int pass = 0; pass < 2; ++pass)
+      TLR_CUDA(ctx, cudaMemcpyAsync(ws->hpin + pass * hstride + (size_t)k0 * ldh, hcol(pass, k0),
+                                    sizeof(double2) * (m - k0) * ldh, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+    TLR_CUDA(ctx, cudaMemcpyAsync(hbeta + k0, ws->betad + k0, sizeof(double) * (m - k0),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    return TLR_OK;
+  };
+  auto fetch_h = [&](int k0, int m) -> int {
+    int rc = copy_h(k0, m);
+    if (rc) return rc;
+    TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return fill_h(k0, m);
+  };
+  // completion of the latest column copies (convergence checks)
+  struct EventGuard {
+    cudaEvent_t e = nullptr;
+    ~EventGuard() { if (e) cudaEventDestroy(e); }
+  } hev;
   // projected problem of the leading m basis vectors: Schur form
   // T = Q^* H(0:m, 0:m) Q with the wanted (largest |theta|) first, and the
   // residual rows of the decomposition in the Schur basis, EQ = H(m : m +
@@ -950,16 +981,47 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   // once the basis holds nev + 1 vectors (0: at the end of each expansion)
   if (o.conv_check < 0) return fail(ctx, TLR_ERR_ARG, "conv_check must not be negative");
   const int check = o.conv_check;
+  if (check > 0) TLR_CUDA(ctx, cudaEventCreateWithFlags(&hev.e, cudaEventDisableTiming));
   while (true) {
     ++it;
     // block Arnoldi expansion of columns k .. ncv-1: OP on bsz vectors at
     // once, then every new vector orthogonalised in order against all
     // earlier ones (two passes of classical Gram-Schmidt); nothing comes
     // back to the host until the expansion is complete
+    int pend_m = 0;  // basis size whose convergence check is due
     for (int j0 = k; j0 < ncv; j0 += bsz) {
+      // the check of basis size am runs on the host while the GPU applies
+      // the operator to the next vector (in the mixed form between the
+      // refinement graph's launch and its synchronisation)
+      dense::Mat Tm, Qm, Em;
+      int am = 0, nc = 0, prc = TLR_OK;
+      if (pend_m) {
+        am = pend_m;
+        pend_m = 0;
+        S.while_waiting = [&, am]() {
+          const auto tc = clock::now();
+          if (cudaEventSynchronize(hev.e) != cudaSuccess)
+            prc = fail(ctx, TLR_ERR_CUDA, "convergence check: column copies failed");
+          if (!prc) prc = fill_h(k, am);
+          if (!prc) prc = project(am, Tm, Qm, Em);
+          if (!prc) nc = count_conv(Tm, Em, am, tol_int);
+          dense_ms += ms_since(tc);
+          ++checks;
+        };
+      }
       int rc = bsz == 1 ? S.op(S.V + (size_t)j0 * n, S.w)
                         : S.op_block(S.V + (size_t)j0 * n);
+      S.host_work();  // operator paths that did not run it
       if (rc) return rc;
+      if (prc) return prc;
+      if (am && nc >= nev) {
+        if ((rc = finalize(Tm, Qm, am))) return rc;
+        if (maxerr <= tol) {
+          nconv = nc;
+          early = true;
+          break;
+        }
+      }
       const auto to = clock::now();
       for (int i = 0; i < bsz && !rc; ++i) {
         const int j = j0 + i, nk = j + bsz;
@@ -974,25 +1036,15 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
       }
       if (rc) return rc;
       ortho_ms += ms_since(to);
-      // a convergence check on the partial decomposition of m vectors: the
-      // wanted pairs may meet the tolerance before the basis is full
+      // a convergence check on the partial decomposition of m vectors (the
+      // wanted pairs may meet the tolerance before the basis is full): its
+      // columns go to the host now, the check runs during the next
+      // application
       const int m = j0 + bsz;
-      if (check > 0 && m < ncv && m > nev && (m - k) % check == 0 && (m - k) >= check) {
-        const auto tc = clock::now();
-        if ((rc = fetch_h(k, m))) return rc;
-        dense::Mat Tm, Qm, Em;
-        if ((rc = project(m, Tm, Qm, Em))) return rc;
-        const int nc = count_conv(Tm, Em, m, tol_int);
-        dense_ms += ms_since(tc);
-        ++checks;
-        if (nc >= nev) {
-          if ((rc = finalize(Tm, Qm, m))) return rc;
-          if (maxerr <= tol) {
-            nconv = nc;
-            early = true;
-            break;
-          }
-        }
+      if (check > 0) {
+        if ((rc = copy_h(j0, m))) return rc;
+        TLR_CUDA(ctx, cudaEventRecord(hev.e, ctx->stream));
+        if (m < ncv && m > nev && (m - k) % check == 0 && (m - k) >= check) pend_m = m;
       }
     }
     if (early) {
