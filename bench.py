@@ -77,7 +77,7 @@ C5_BLOCK = 1
 C5_NCV = 64
 # concurrent chains of sweep points on the one GPU (one context and one host
 # thread each; each chain walks its own stretch of the snake)
-C5_CHAINS = 1
+C5_CHAINS = 3
 PLAIN_NCV = 32
 # C2: mixed vs plain FP64 at 200 x 128
 C2 = dict(ny=200, nz=128, amplitude=0.08, alpha=1.8, omega=complex(0.3, 0.01), nev=16)
@@ -434,7 +434,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=32)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--plain-points", type=int, default=2,

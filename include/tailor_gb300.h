@@ -255,13 +255,21 @@ typedef struct {
                              wider separators for shallower top fronts; 100:
                              the smallest separator; range [100, 1000]);
                              see tlr_symbolic_analyze                      */
-  int conv_check;         /* > 0: also test convergence inside a Krylov-
-                             Schur expansion, every conv_check operator
+  int conv_check;         /* convergence tests inside a Krylov-Schur
+                             expansion: every conv_check operator
                              applications once the basis holds more than
-                             nev vectors, and stop as soon as nev Ritz pairs
-                             meet the tolerance (estimates, then explicit
-                             residuals); 0: only when the basis is full, as
+                             nev vectors, the solve stops as soon as nev
+                             Ritz pairs meet the tolerance (estimates, then
+                             explicit residuals); the test of one basis
+                             size runs on the host while the GPU applies
+                             the operator to the next vector.  0: every 4
+                             (default); -1: only when the basis is full, as
                              SLEPc                                          */
+  int step_launches;      /* triangular solves: 0 (default) one dependency-
+                             driven launch per direction for every level
+                             whose fronts have several diagonal blocks (32-
+                             row tiles wait only for the blocks they need);
+                             1 one launch per block step.  Same bits.       */
 } tlr_solve_opts;
 
 typedef struct {

@@ -79,7 +79,8 @@ class SolveOpts(ctypes.Structure):
                 ("panel_width", ctypes.c_int), ("cluster_panel", ctypes.c_int),
                 ("persistent_solve", ctypes.c_int), ("block", ctypes.c_int),
                 ("nstart", ctypes.c_int), ("warm_start", ctypes.c_int),
-                ("ring_slack_percent", ctypes.c_int), ("conv_check", ctypes.c_int)]
+                ("ring_slack_percent", ctypes.c_int), ("conv_check", ctypes.c_int),
+                ("step_launches", ctypes.c_int)]
 
 
 class EigDiag(ctypes.Structure):

@@ -1170,6 +1170,150 @@ __global__ void __launch_bounds__(256, (SW <= 256 && sizeof(C) == 8) ? 3 : 1)
   }
 }
 
+// ---- dependency-driven level solve ---------------------------------------
+// A level whose fronts have several diagonal blocks needs, step by step,
+// one launch per block, and the top of the elimination tree is a chain of
+// such launches with little work in each.  k_wave solves a whole level in
+// one launch.  CTAs take 32-row tiles from a counter, in dependency order;
+// a tile applies the updates of the blocks it depends on one after the
+// other, each as soon as that block is final, and a tile of block b counts
+// itself into done[front][b] once its own rows are final.  Block b is final
+// when all of its tiles have counted in.
+//   forward:  rows of block bt (border rows: bt = number of blocks) take
+//             the updates of blocks 0 .. bt-1;
+//   backward: pivot rows of block bt take the updates of blocks nblk-1 down
+//             to bt+1 and are then written to the solution.
+// Tiles are numbered forward by block and backward by decreasing block, so
+// a tile waits only for tiles taken before it, by CTAs that are already
+// running: the level completes with any number of CTAs resident.  Each row
+// takes the same updates in the same order with the same arithmetic as in
+// k_blk_update, so the results are bitwise those of the step launches.
+// Waits are bounded: a wait that runs out raises the solve's error flag and
+// the abort word, and every CTA stops waiting (the host rejects the solve).
+// ctr: [0] next tile, [1] CTAs done, [2] abort, [4 + q maxblk + b] final
+// tiles of block b of the level's front q; the last CTA out clears them.
+constexpr unsigned kWaveLimit = 1u << 22;
+
+__device__ __forceinline__ int ld_acquire_int(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+template <class C, int SW, bool BWD>
+__global__ void __launch_bounds__(256, (SW <= 256 && sizeof(C) == 8) ? 2 : 1)
+    k_wave(const int *__restrict__ fl, const int4 *__restrict__ tiles, int ntiles,
+           int *__restrict__ ctr, int nctr, int maxblk, const C *__restrict__ pool,
+           const DevFront *__restrict__ fr, C *__restrict__ work, const int *__restrict__ nodes,
+           C *__restrict__ x, int *__restrict__ err) {
+  __shared__ __align__(16) C vs[SW];
+  __shared__ C red[8][32];
+  __shared__ int s_tile, s_abort;
+  pdl_launch_dependents();
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  constexpr int kQ = SW / 8;
+  const int q0 = wp * kQ;
+  int *done = ctr + 4;
+  bool waited = false, aborted = false;
+  while (!aborted) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(ctr, 1);
+    __syncthreads();
+    const int ti = s_tile;
+    if (ti >= ntiles) break;
+    const int4 tl = tiles[ti];  // {front slot, first row, rows, block}
+    const DevFront f = fr[fl[tl.x]];
+    const int nblk = (f.p + SW - 1) / SW;
+    C *t = work + f.toff;
+    const bool rowok = lane < tl.z;
+    const int r = tl.y + lane;
+    const int nupd = BWD ? nblk - 1 - tl.w : min(tl.w, nblk);
+    C v = czero<C>();
+    for (int u = 0; u < nupd; ++u) {
+      const int b = BWD ? nblk - 1 - u : u;
+      const int b0 = b * SW, b1 = min(f.p, b0 + SW), nb = b1 - b0;
+      const C *F = pool + f.off + (long long)b0 * f.m;
+      const bool full = q0 + kQ <= nb;
+      // the factor does not depend on earlier kernels: its loads go out
+      // before any wait
+      C fv[kQ];
+      if (full && rowok) {
+        const C *Fp = F + (long long)q0 * f.m + r;
+#pragma unroll
+        for (int k = 0; k < kQ; ++k, Fp += f.m) fv[k] = *Fp;
+      } else {
+#pragma unroll
+        for (int k = 0; k < kQ; ++k)
+          fv[k] = (rowok && q0 + k < nb) ? F[(long long)(q0 + k) * f.m + r] : czero<C>();
+      }
+      if (!waited) {
+        pdl_wait();
+        waited = true;
+      }
+      if (u == 0 && wp == 0 && rowok) v = __ldcg(t + r);
+      if (threadIdx.x == 0) {
+        const int *c = done + tl.x * maxblk + b;
+        const int target = (nb + 31) / 32;
+        unsigned it = 0;
+        int ab = 0;
+        while (ld_acquire_int(c) < target) {
+          if (*reinterpret_cast<volatile int *>(ctr + 2)) {
+            ab = 1;
+            break;
+          }
+          if (++it > kWaveLimit) {
+            atomicExch(ctr + 2, 1);
+            atomicExch(err, 1);
+            ab = 1;
+            break;
+          }
+          __nanosleep(32);
+        }
+        s_abort = ab;
+      }
+      __syncthreads();
+      if (s_abort) {
+        aborted = true;
+        break;
+      }
+      for (int q = threadIdx.x; q < nb; q += blockDim.x) vs[q] = __ldcg(t + b0 + q);
+      __syncthreads();
+      const C acc = dot_cols<C, kQ>(fv, vs + q0, full, nb - q0);
+      red[wp][lane] = acc;
+      __syncthreads();
+      if (wp == 0 && rowok) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v = csub(v, red[k][lane]);
+      }
+      __syncthreads();  // vs and red are reused
+    }
+    if (aborted) break;
+    if (nupd > 0 && wp == 0 && rowok) {
+      t[r] = v;
+      if (BWD) x[(long long)nodes[f.node_off + r / 5] * 5 + r % 5] = v;
+    }
+    if (tl.w < nblk) {  // a pivot tile: its rows are final
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(done + tl.x * maxblk + tl.w, 1);
+      }
+    }
+    __syncthreads();  // s_tile is rewritten
+  }
+  // the last CTA out clears the counters for the next replay
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(ctr + 1, 1) == (int)gridDim.x - 1) {
+      ctr[0] = 0;
+      ctr[2] = 0;
+      for (int i = 4; i < nctr; ++i) ctr[i] = 0;
+      __threadfence();
+      ctr[1] = 0;
+    }
+  }
+}
+
 // Backward border product, pass 1: partial[front][chunk][i] = sum over a
 // kBC-column chunk of the border of U'(i, c) x[unknown of border row c],
 // pivot rows i (the border unknowns belong to ancestors, already solved).
@@ -1926,6 +2070,47 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int pa
     }
     partial_elems = std::max(partial_elems, (long long)L.nfronts * L.nck_b * std::max(L.pmax, 1));
   }
+  // dependency-driven level solves: 32-row tiles of every level with two or
+  // more diagonal blocks, forward in block order (border rows last),
+  // backward in decreasing block order; tile = {front slot, first row, rows,
+  // block}
+  std::vector<int4> wtiles;
+  long long wctr = 0;
+  for (auto &L : levels) {
+    L.wave = L.blk_nf.size() >= 2;
+    if (!L.wave) continue;
+    L.maxblk = (int)L.blk_nf.size();
+    std::vector<std::pair<int, int4>> fw, bw;
+    for (int q = 0; q < L.nfronts; ++q) {
+      const FrontInfo &f = sym.fronts[sched[L.fronts_off + q]];
+      const int nblk = (f.p + sw - 1) / sw;
+      for (int bt = 0; bt < nblk; ++bt) {
+        const int b0 = bt * sw, b1 = std::min(f.p, b0 + sw);
+        for (int r = b0; r < b1; r += 32) {
+          const int4 tl = make_int4(q, r, std::min(32, b1 - r), bt);
+          fw.push_back({bt, tl});
+          bw.push_back({-bt, tl});
+        }
+      }
+      for (int r = f.p; r < f.m; r += 32)
+        fw.push_back({nblk, make_int4(q, r, std::min(32, f.m - r), nblk)});
+    }
+    auto by_key = [](const std::pair<int, int4> &x, const std::pair<int, int4> &y) {
+      return x.first < y.first;
+    };
+    std::stable_sort(fw.begin(), fw.end(), by_key);
+    std::stable_sort(bw.begin(), bw.end(), by_key);
+    L.wf_off = (long long)wtiles.size();
+    L.wf_n = (int)fw.size();
+    for (auto &e : fw) wtiles.push_back(e.second);
+    L.wb_off = (long long)wtiles.size();
+    L.wb_n = (int)bw.size();
+    for (auto &e : bw) wtiles.push_back(e.second);
+    L.wctr_n = 4 + L.nfronts * L.maxblk;
+    L.wcf_off = wctr;
+    L.wcb_off = wctr + L.wctr_n;
+    wctr += 2LL * L.wctr_n;
+  }
   // diagonal blocks (full blocks sw x sw, the last one nb x nb) and the
   // tiles of the factor rewrite L' = L Dl^-1, U' = Du^-1 U, D = Du^-1 Dl^-1
   std::vector<long long> inv_off(nf);
@@ -1978,8 +2163,19 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int pa
       (rc = alloc((void **)&d_utiles, utiles.size() * sizeof(int4))) ||
       (rc = alloc((void **)&d_inv_off, nf * sizeof(long long))) ||
       (rc = alloc((void **)&d_inv_blocks, inv_blocks.size() * sizeof(int2))) ||
-      (rc = alloc(&vec_a, (size_t)ctx->nn * 5 * csize)))
+      (rc = alloc(&vec_a, (size_t)ctx->nn * 5 * csize)) ||
+      (rc = alloc((void **)&d_wave_tiles, wtiles.size() * sizeof(int4))) ||
+      (rc = alloc((void **)&d_wave_ctr, (size_t)wctr * sizeof(int))))
     return rc;
+  {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    wave_grid = std::max(1, sms) * (prec == 1 && sw <= 256 ? 2 : 1);
+  }
+  if (!wtiles.empty())
+    TLR_CUDA(ctx, cudaMemcpy(d_wave_tiles, wtiles.data(), wtiles.size() * sizeof(int4),
+                             cudaMemcpyHostToDevice));
+  if (wctr) TLR_CUDA(ctx, cudaMemset(d_wave_ctr, 0, (size_t)wctr * sizeof(int)));
   if (prec == 1 &&
       (rc = alloc((void **)&tc_planes, (size_t)max_plane_tiles * ((w + 7) / 8) *
                                            tc_chunk_image_bytes())))
@@ -2047,7 +2243,7 @@ int Factor::take_solve_error(tlr_ctx *ctx) {
   TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (!h) return TLR_OK;
   TLR_CUDA(ctx, cudaMemsetAsync(d_solve_err, 0, sizeof(int), ctx->stream));
-  return fail(ctx, TLR_ERR_CUDA, "persistent solve: a grid barrier timed out");
+  return fail(ctx, TLR_ERR_TIMEOUT, "triangular solve: a bounded wait between CTAs timed out");
 }
 
 template <class C, int SW>
@@ -2105,6 +2301,9 @@ void Factor::release() {
   cudaFree(vec_a); cudaFree(linv); cudaFree(uinv); cudaFree(dmat);
   cudaFree(d_inv_off); cudaFree(d_inv_blocks); cudaFree(d_ltiles); cudaFree(d_utiles);
   cudaFree(d_phases); cudaFree(d_barrier); cudaFree(d_solve_err); cudaFree(tc_planes);
+  cudaFree(d_wave_tiles); cudaFree(d_wave_ctr);
+  d_wave_tiles = nullptr;
+  d_wave_ctr = nullptr;
   tc_planes = nullptr;
   d_phases = nullptr;
   d_barrier = nullptr;
@@ -2318,6 +2517,15 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
                              st, fl, (const DevFront *)d_fronts, (const int *)d_nodes,
                              (const int *)d_perm, (const int2 *)d_cinv, (const C *)x, W));
     count_launches();
+    if (wave && L.wave) {
+      TLR_CUDA(ctx, launch_pdl(pdl, k_wave<C, SW, false>, dim3(std::min(L.wf_n, wave_grid)),
+                               dim3(256), st, fl, (const int4 *)(d_wave_tiles + L.wf_off), L.wf_n,
+                               d_wave_ctr + L.wcf_off, L.wctr_n, L.maxblk, P,
+                               (const DevFront *)d_fronts, W, (const int *)d_nodes, x,
+                               d_solve_err));
+      count_launches();
+      continue;
+    }
     for (int b = 0; b < (int)L.blk_nf.size(); ++b) {
       const int rows = L.fwd_rows[b];
       if (rows > 0) {
@@ -2350,6 +2558,15 @@ int Factor::solve_impl(tlr_ctx *ctx, void *xv) {
                              (const double2 *)d_partial, L.nck_b, L.pmax, (const int *)d_nodes,
                              x));
     count_launches();
+    if (wave && L.wave) {
+      TLR_CUDA(ctx, launch_pdl(pdl, k_wave<C, SW, true>, dim3(std::min(L.wb_n, wave_grid)),
+                               dim3(256), st, fl, (const int4 *)(d_wave_tiles + L.wb_off), L.wb_n,
+                               d_wave_ctr + L.wcb_off, L.wctr_n, L.maxblk, P,
+                               (const DevFront *)d_fronts, W2, (const int *)d_nodes, x,
+                               d_solve_err));
+      count_launches();
+      continue;
+    }
     for (int b = (int)L.blk_nf.size() - 1; b >= 1; --b) {
       TLR_CUDA(ctx, launch_pdl(pdl, k_blk_update<C, SW>, dim3(blocks_for(b * SW, 32), L.blk_nf[b]),
                                dim3(256), st, fl, b, 1, P, (const DevFront *)d_fronts, W2,

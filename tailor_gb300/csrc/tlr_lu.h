@@ -32,6 +32,15 @@ struct Level {
   std::vector<Step> steps;
   std::vector<int> blk_nf;    // blk_nf[b]: fronts of the level with p > b sw
   std::vector<int> fwd_rows;  // rows below block b, largest over those fronts
+  // dependency-driven solve of the level (levels with two or more blocks):
+  // forward and backward 32-row tiles in dependency order, and their
+  // counters (4 + nfronts * maxblk each)
+  bool wave = false;
+  int maxblk = 0;
+  long long wf_off = 0, wb_off = 0;
+  int wf_n = 0, wb_n = 0;
+  long long wcf_off = 0, wcb_off = 0;
+  int wctr_n = 0;
 };
 
 // One phase of the persistent solve: a kind of work item over a level's
@@ -83,6 +92,12 @@ struct Factor {
   unsigned *d_barrier = nullptr;
   int *d_solve_err = nullptr;
   long long graph_kernels = 0;           // kernel nodes of graph_exec
+  // levels with several diagonal blocks per front solved by one dependency-
+  // driven launch each way (false: one launch per block step)
+  bool wave = true;
+  int4 *d_wave_tiles = nullptr;
+  int *d_wave_ctr = nullptr;
+  int wave_grid = 0;                     // CTAs of a wave launch (at most)
   double2 *d_partial = nullptr;
   int perturbed = 0;
   // CUDA events around every replayed solve graph (device time of the

@@ -66,16 +66,30 @@ def test_c1_eigenvalues_match_the_oracle(c1_problem, precision, block):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-def test_convergence_checks_inside_the_expansion(c1_problem, precision):
-    """conv_check = 4: convergence is also tested every four applications
-    inside an expansion, and the solve stops at the first basis size where
-    all eight pairs meet the tolerance; the eigenpairs are still the
-    oracle's."""
+@pytest.mark.parametrize("conv_check", [0, 2, -1])
+def test_convergence_checks_inside_the_expansion(c1_problem, precision, conv_check):
+    """Convergence tested every four (the default) or two applications inside
+    an expansion, the solve stopping at the first basis size where all eight
+    pairs meet the tolerance, or only when the basis is full (-1): the
+    eigenpairs are the oracle's either way."""
     ref = _oracle("c1_100x50_eigs.txt")
-    sol = api.EigenSolver(c1_problem).solve(nev=8, precision=precision, conv_check=4,
+    sol = api.EigenSolver(c1_problem).solve(nev=8, precision=precision, conv_check=conv_check,
                                             fallback=False)
     _check(sol, ref, 8)
-    assert sol.diag["conv_checks"] > 0
+    assert (sol.diag["conv_checks"] > 0) == (conv_check >= 0)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_level_launches_are_bitwise_the_step_launches(c1_problem, precision):
+    """The triangular solves with one dependency-driven launch per level
+    (the default) and with one launch per block step apply the same updates
+    in the same order: identical eigenpairs."""
+    wave = api.EigenSolver(c1_problem).solve(nev=8, precision=precision, fallback=False)
+    step = api.EigenSolver(c1_problem).solve(nev=8, precision=precision, step_launches=True,
+                                             fallback=False)
+    assert np.array_equal(wave.lam, step.lam)
+    assert np.array_equal(wave.residual, step.residual)
+    assert np.all(wave.residual <= 1e-10)
 
 
 def test_c2_eigenvalues_match_the_oracle(gpu_lib):
