@@ -8,19 +8,22 @@ tol 1e-10, points on the 8 x 4 grid of alpha in [0.5, 3.5] and Re in
 next) so that consecutive points are neighbours.  One "step" is one point:
 metrics, base-flow derivatives, assembly of M_Gamma and L at the point's
 (alpha, Re), wall and far-field rows, factorisation of A - sigma B and the
-shift-and-invert Krylov-Schur solve, on one persistent context.
+shift-and-invert Krylov-Schur solve.  The default 32 steps are the whole
+sweep.
 
 The combined form (the line's value) is
   * mixed: complex64 multifrontal factor with tensor-core Schur updates,
     every K^-1 application refined in FP64 against the FP64 operator;
-  * batched: one context for the whole sweep (one symbolic analysis, one
-    set of factor buffers, captured solve and refinement graphs);
-  * learned: the first point of the run starts from the learned proposal
-    (an MLP trained, before the timed region, on eigenpairs the solver
-    computed at 60 x 32 over the sweep's parameter range, its start vector
-    carried to 300 x 192 by the spline operators); every later point starts
-    from its predecessor's Ritz vectors (their sum: the wanted modes of the
-    neighbouring point).
+  * batched: the sweep runs as --chains (default 3) concurrent chains on
+    the one GPU, each a persistent context (one symbolic analysis, one set
+    of factor buffers, captured solve and refinement graphs) with its own
+    stream and host thread, walking its own stretch of the snake;
+  * learned: the first point of every chain starts from the learned
+    proposal (an MLP trained, before the timed region, on eigenpairs the
+    solver computed at 60 x 32 over the sweep's parameter range, its start
+    vector carried to 300 x 192 by the spline operators); every later point
+    starts from its predecessor's Ritz vectors (their sum: the wanted modes
+    of the neighbouring point).
 The plain FP64 form (complex128 factor, single-vector Krylov-Schur from a
 pseudo-random start, the reference's EigenSolver) solves a stated subset of
 the same points in the same run.
@@ -31,8 +34,9 @@ reference eigenvalues of its point (tests/golden/c5_300x192_plain_eigs.txt,
 the plain FP64 form's, which is pinned to the CPU oracle at 100 x 50 and
 200 x 128).
 
-value: device-resident (grid and base flow in HBM), CUDA events on the
-context's stream around the K timed steps.  e2e: the next K points through
+value: device-resident (grid and base flow in HBM), CUDA events around the
+K timed steps: the start event on chain 0's stream, which the other chains'
+streams wait on, the end event after every chain's stream has joined it.  e2e: the next K points through
 the public API from pinned host buffers (host->device copy of the grid and
 base flow and device->host read of eigenvalues and residuals inside the
 timed region).  The operator (1.8 GB) and the factor (10 GB) are far larger

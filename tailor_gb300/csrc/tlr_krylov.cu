@@ -685,8 +685,8 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   F->tc_variant = tc_variant;
   F->cluster_rows = crows;
   F->persistent = o.persistent_solve != 0;
-  if (F->wave != (o.step_launches == 0)) {  // the captured solve graph changes
-    F->wave = o.step_launches == 0;
+  if (F->wave != (o.solve_wave != 0)) {  // the captured solve graph changes
+    F->wave = o.solve_wave != 0;
     if (F->graph_exec) cudaGraphExecDestroy(F->graph_exec);
     F->graph_exec = nullptr;
   }

@@ -1190,6 +1190,10 @@ __global__ void __launch_bounds__(256, (SW <= 256 && sizeof(C) == 8) ? 3 : 1)
 // k_blk_update, so the results are bitwise those of the step launches.
 // Waits are bounded: a wait that runs out raises the solve's error flag and
 // the abort word, and every CTA stops waiting (the host rejects the solve).
+// Measured slower than the step launches (option solve_wave): with
+// programmatic dependent launch a step already costs little more than the
+// memory round trips of a hand-over (flag, vector, reduction), which the
+// wave pays too, and its CTAs stream less of the factor at a time.
 // ctr: [0] next tile, [1] CTAs done, [2] abort, [4 + q maxblk + b] final
 // tiles of block b of the level's front q; the last CTA out clears them.
 constexpr unsigned kWaveLimit = 1u << 22;

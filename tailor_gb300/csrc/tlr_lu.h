@@ -93,8 +93,8 @@ struct Factor {
   int *d_solve_err = nullptr;
   long long graph_kernels = 0;           // kernel nodes of graph_exec
   // levels with several diagonal blocks per front solved by one dependency-
-  // driven launch each way (false: one launch per block step)
-  bool wave = true;
+  // driven launch each way (false, the default: one launch per block step)
+  bool wave = false;
   int4 *d_wave_tiles = nullptr;
   int *d_wave_ctr = nullptr;
   int wave_grid = 0;                     // CTAs of a wave launch (at most)

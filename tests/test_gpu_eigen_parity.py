@@ -82,11 +82,11 @@ def test_convergence_checks_inside_the_expansion(c1_problem, precision, conv_che
 @pytest.mark.parametrize("precision", [0, 1])
 def test_level_launches_are_bitwise_the_step_launches(c1_problem, precision):
     """The triangular solves with one dependency-driven launch per level
-    (the default) and with one launch per block step apply the same updates
-    in the same order: identical eigenpairs."""
-    wave = api.EigenSolver(c1_problem).solve(nev=8, precision=precision, fallback=False)
-    step = api.EigenSolver(c1_problem).solve(nev=8, precision=precision, step_launches=True,
+    (solve_wave) and with one launch per block step (the default) apply the
+    same updates in the same order: identical eigenpairs."""
+    wave = api.EigenSolver(c1_problem).solve(nev=8, precision=precision, solve_wave=True,
                                              fallback=False)
+    step = api.EigenSolver(c1_problem).solve(nev=8, precision=precision, fallback=False)
     assert np.array_equal(wave.lam, step.lam)
     assert np.array_equal(wave.residual, step.residual)
     assert np.all(wave.residual <= 1e-10)
