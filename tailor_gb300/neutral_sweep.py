@@ -7,8 +7,9 @@ lambda_s = 0, nev 8, tol 1e-10; points on an 8 x 4 grid of alpha in
 [0.5, 3.5] and Re in [800, 2400], in snake order.  The mixed + batched
 form (complex64 fronts with tensor-core Schur updates and FP64
 refinement, the sweep engine's shared symbolic analysis and autotuned
-kernels, every point warm-started from its predecessor's Ritz vectors)
-solves every point; the plain FP64 form
+kernels, --workers concurrent instances each taking a contiguous run of
+the points, every point but a run's first warm-started from its
+predecessor's Ritz vectors) solves every point; the plain FP64 form
 solves the first --plain-points points one at a time, and their
 eigenvalues are compared.  Prints one JSON line with
 eigenpairs at resid <= 1e-10 per wall second for each form and the
@@ -53,7 +54,7 @@ def main() -> None:
     ap.add_argument("--ny", type=int, default=300)
     ap.add_argument("--nz", type=int, default=192)
     ap.add_argument("--nev", type=int, default=8)
-    ap.add_argument("--workers", type=int, default=1)
+    ap.add_argument("--workers", type=int, default=4)
     ap.add_argument("--plain-points", type=int, default=2)
     ap.add_argument("--ncv", type=int, default=64)
     a = ap.parse_args()
