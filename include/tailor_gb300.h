@@ -272,6 +272,15 @@ typedef struct {
                              for the blocks they need, bounded waits).  Same
                              bits; measured 6% slower per solve at 300 x
                              192 and 12% at 200 x 128                      */
+  int fp64_acceptance;    /* mixed form: the residual that accepts each
+                             refined K^-1 application (||r|| <= 1e-12 ||y||)
+                             -- 0 (default): a float-float residual (the
+                             operator as FP32 hi/lo pairs, 48-bit products
+                             and sums on the FP32 pipe, combined in FP64);
+                             1: an FP64 residual (FP64 pipe).  A rejected
+                             application continues with float-float
+                             corrections and an FP64 acceptance either way;
+                             eigen residuals are always FP64               */
 } tlr_solve_opts;
 
 typedef struct {

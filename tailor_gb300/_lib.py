@@ -80,7 +80,7 @@ class SolveOpts(ctypes.Structure):
                 ("persistent_solve", ctypes.c_int), ("block", ctypes.c_int),
                 ("nstart", ctypes.c_int), ("warm_start", ctypes.c_int),
                 ("ring_slack_percent", ctypes.c_int), ("conv_check", ctypes.c_int),
-                ("solve_wave", ctypes.c_int)]
+                ("solve_wave", ctypes.c_int), ("fp64_acceptance", ctypes.c_int)]
 
 
 class EigDiag(ctypes.Structure):

@@ -228,7 +228,8 @@ class EigenSolver:
               panel_width: int = 0, cluster_panel: int = 0,
               fallback: bool = True, block: int = 0,
               warm_start: bool = False, ring_slack_percent: int = 0,
-              conv_check: int = 0, solve_wave: bool = False) -> EigenSolution:
+              conv_check: int = 0, solve_wave: bool = False,
+              fp64_acceptance: bool = False) -> EigenSolution:
         """With fallback, a mixed-form solve (precision 1) that fails to
         converge (or hits a singular pivot or a timed-out device wait) is
         repeated in the plain FP64 form; diag["fallback"] is 1 then.
@@ -241,13 +242,16 @@ class EigenSolver:
         applications between convergence tests inside an expansion (0: the
         solver's 4; -1: only when the basis is full); solve_wave: one
         dependency-driven launch per level of the triangular solves instead
-        of one launch per block step (the same bits, measured slower)."""
+        of one launch per block step (the same bits, measured slower);
+        fp64_acceptance: accept each refined application on an FP64
+        residual instead of a float-float one (mixed form)."""
         kw = dict(nev=nev, ncv=ncv, tol=tol, max_it=max_it, sigma=sigma, start=start,
                   modes=modes, cuda_core_schur=cuda_core_schur,
                   persistent_solve=persistent_solve, solve_block=solve_block,
                   refinement=refinement, panel_width=panel_width, cluster_panel=cluster_panel,
                   block=block, warm_start=warm_start, ring_slack_percent=ring_slack_percent,
-                  conv_check=conv_check, solve_wave=solve_wave)
+                  conv_check=conv_check, solve_wave=solve_wave,
+                  fp64_acceptance=fp64_acceptance)
         if precision == 1 and fallback:
             try:
                 sol = self._solve(precision=1, **kw)
@@ -265,7 +269,8 @@ class EigenSolver:
     def _solve(self, nev, ncv, tol, max_it, precision, sigma, start, modes, cuda_core_schur,
                persistent_solve, solve_block, refinement, panel_width,
                cluster_panel, block=0, warm_start=False,
-               ring_slack_percent=0, conv_check=0, solve_wave=False) -> EigenSolution:
+               ring_slack_percent=0, conv_check=0, solve_wave=False,
+               fp64_acceptance=False) -> EigenSolution:
         ph = self.p.case.physics
         k = nev or ph.nev
         opts = L.SolveOpts(nev, ncv, tol, max_it, precision,
@@ -278,7 +283,7 @@ class EigenSolver:
                            int(panel_width), int(cluster_panel),
                            int(bool(persistent_solve)), int(block), 0,
                            int(bool(warm_start)), int(ring_slack_percent), int(conv_check),
-                           int(bool(solve_wave)))
+                           int(bool(solve_wave)), int(bool(fp64_acceptance)))
         if start is not None:
             st = np.atleast_2d(np.asarray(start, dtype=np.complex128))
             s = np.ascontiguousarray(np.stack([st.real, st.imag], -1), dtype=np.float64)

@@ -187,6 +187,10 @@ struct Solver {
   // application so far needed exactly two corrections; when the accepted
   // residual is still too large, the dynamic loop continues.
   bool use_ref_graph = true;
+  // the graph's acceptance residual: FP64 (A w and B w on the FP64 pipe) or
+  // a third float-float residual (A as FP32 hi/lo pairs, 48-bit products
+  // and sums, combined with y and sigma B w in FP64)
+  bool fp64_accept = false;
   cudaGraphExec_t ref_exec = nullptr;
   long long ref_kernels = 0;
   const double2 *ref_in = nullptr;
@@ -329,7 +333,7 @@ struct Solver {
         rc = F->enqueue_solve(ctx, x32, rev[2 * q], rev[2 * q + 1]);
         if (!rc) k_add32<<<blocks, 256, 0, st>>>(n, x32, out);
       }
-      if (!rc) rc = residual64(in, out);
+      if (!rc) rc = fp64_accept ? residual64(in, out) : residual_ff(ctx, in, out, sr, si, r);
       // ||r|| and ||in|| to pinned host memory: one synchronisation per application
       const int nb = ctx->partial_blocks;
       double *s0 = nscratch, *s1 = nscratch + nb + 1;
@@ -781,6 +785,7 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   S.kpart = ws->kpart;
   S.npart = ws->npart;
   S.gmres = o.refinement == 1;
+  S.fp64_accept = o.fp64_acceptance != 0;
   S.nb_rhs = bsz;
   if (bsz > 1) {
     const size_t bv = (size_t)Factor::kMaxRhs * n;

@@ -92,6 +92,15 @@ def test_level_launches_are_bitwise_the_step_launches(c1_problem, precision):
     assert np.all(wave.residual <= 1e-10)
 
 
+def test_fp64_acceptance_residual(c1_problem):
+    """The mixed form's refined applications accepted on an FP64 residual
+    instead of the default float-float one: the oracle's eigenpairs too."""
+    ref = _oracle("c1_100x50_eigs.txt")
+    sol = api.EigenSolver(c1_problem).solve(nev=8, precision=1, fp64_acceptance=True,
+                                            fallback=False)
+    _check(sol, ref, 8)
+
+
 def test_c2_eigenvalues_match_the_oracle(gpu_lib):
     """C2 (200 x 128, bump 0.08, alpha 1.8, omega 0.3 + 0.01i, nev 16) in
     both forms: the mixed form's eigenvalues are within 1e-8 of the FP64
