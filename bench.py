@@ -470,13 +470,18 @@ def main():
     ref = load_c5_reference()
     pts = c5_points(snake=True)
     width = max(1, args.chains)
-    # replicas: each rank walks the sweep from its own offset; chain w of a
-    # rank starts its own stretch of the snake from there
+    # replicas: each rank walks the sweep from its own offset.  Chain w times
+    # the stretch [T_w, T_w + n_w) of the snake, T_w = warmup + n_0 + ... +
+    # n_(w-1), after warming up on the points just before it; its end-to-end
+    # pass continues with the next chain's stretch, so with 32 steps both
+    # passes cover the 32 points once and every point is warm-started from
+    # its neighbour
     off = (rank * len(pts)) // max(world, 1)
     nstep = split_steps(args.steps, width)
-    per_chain = args.warmup + 2 * max(nstep) + 1
-    seqs = [[pts[(off + (w * len(pts)) // width + i) % len(pts)] for i in range(per_chain)]
-            for w in range(width)]
+    nnext = [nstep[(w + 1) % width] for w in range(width)]
+    starts = [args.warmup + sum(nstep[:w]) for w in range(width)]
+    seqs = [[pts[(off + starts[w] - args.warmup + i) % len(pts)]
+             for i in range(args.warmup + nstep[w] + nnext[w] + 1)] for w in range(width)]
     pos = [0] * width
 
     def take(counts):
@@ -534,7 +539,7 @@ def main():
         p.check(p.lib.tlr_load_fields(p.ctx, pg, pb))
 
     barrier()
-    per_e2e, ms_e2e = chains.timed(ev, lambda: chains.run(take(nstep), before=load))
+    per_e2e, ms_e2e = chains.timed(ev, lambda: chains.run(take(nnext), before=load))
     barrier()
     good_e2e = tally([x for chain in per_e2e for x in chain])[0]
     ms_e2e, good_e2e = replicas.reduce_timing(ms_e2e, good_e2e)
