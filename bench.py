@@ -87,6 +87,7 @@ PLAIN_NCV = 32
 C2 = dict(ny=200, nz=128, amplitude=0.08, alpha=1.8, omega=complex(0.3, 0.01), nev=16)
 C2_NCV = 64
 GOLDEN = ROOT / "tests" / "golden"
+TRISOLVE_TRAFFIC_RATIO = 538.1 / 518.3
 
 
 def c2_case(ny=None, nz=None):
@@ -597,13 +598,10 @@ def main():
     tri_n = sum(s[3]["trisolves"] for s in rsteps)
     tri_avg_ms = tri_ms / max(tri_n, 1)
     achieved = tri_bytes / (tri_avg_ms * 1e-3) / 1e9 if tri_avg_ms > 0 else 0.0
-    traffic = None
-    tf = ROOT / "profiles" / "trisolve_traffic.json"
-    if tf.exists():
-        # ncu DRAM bytes / algorithmic bytes of the same solve graph measured
-        # on a 100 x 50 capture, applied to this solve's algorithmic bytes
-        ratio = json.loads(tf.read_text()).get("c64", {}).get("ratio")
-        traffic = ratio * tri_bytes if ratio else None
+    # ncu DRAM bytes / algorithmic bytes of the same solve graph, measured on
+    # a 100 x 50 capture (538.1 / 518.3 MB per solve: the factor read once,
+    # plus the D_b blocks), applied to this solve's algorithmic bytes
+    traffic = TRISOLVE_TRAFFIC_RATIO * tri_bytes
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
