@@ -212,6 +212,15 @@ int launch_gemm_tc(tlr_ctx *ctx, const int *fl, const int *prefix, int nf, int s
                    float2 *pool, const DevFront *fr, int tiles, int *err, cudaStream_t st,
                    uint32_t lbo = 128, uint32_t sbo = 256);
 
+// The complex64 factor rewrite of the block-scaled solves (256-row diagonal
+// blocks) on the tensor cores: U' and D_b from utiles {front, block, first
+// column, kind} (64 columns each), then L' from ltiles {front, block, first
+// row, -} (128 rows each), in place.
+int launch_rewrite_tc(tlr_ctx *ctx, const int4 *ltiles, long long nl, const int4 *utiles,
+                      long long nu, float2 *pool, const DevFront *fr, const long long *inv_off,
+                      const float2 *Linv, const float2 *Uinv, float2 *dmat, int *err,
+                      cudaStream_t st);
+
 inline int blocks_for(long long n, int threads) {
   return static_cast<int>((n + threads - 1) / threads);
 }

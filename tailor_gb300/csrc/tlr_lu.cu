@@ -2119,7 +2119,7 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int pa
   // tiles of the factor rewrite L' = L Dl^-1, U' = Du^-1 U, D = Du^-1 Dl^-1
   std::vector<long long> inv_off(nf);
   std::vector<int2> inv_blocks;
-  std::vector<int4> ltiles, utiles;
+  std::vector<int4> ltiles, utiles, ltiles_tc, utiles_tc;
   inv_elems = 0;
   for (int t = 0; t < nf; ++t) {
     const int p = sym.fronts[t].p, m = sym.fronts[t].m;
@@ -2131,10 +2131,17 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int pa
       for (int r = b1; r < m; r += kRT) ltiles.push_back(make_int4(t, b, r, 0));
       for (int c = b1; c < m; c += kRT) utiles.push_back(make_int4(t, b, c, 0));
       for (int c = 0; c < nb; c += kRT) utiles.push_back(make_int4(t, b, c, 1));
+      if (prec == 1 && sw == 256) {
+        for (int r = b1; r < m; r += 128) ltiles_tc.push_back(make_int4(t, b, r, 0));
+        for (int c = b1; c < m; c += 64) utiles_tc.push_back(make_int4(t, b, c, 0));
+        for (int c = 0; c < nb; c += 64) utiles_tc.push_back(make_int4(t, b, c, 1));
+      }
     }
   }
   n_ltiles = (long long)ltiles.size();
   n_utiles = (long long)utiles.size();
+  n_ltiles_tc = (long long)ltiles_tc.size();
+  n_utiles_tc = (long long)utiles_tc.size();
   n_inv_blocks = (int)inv_blocks.size();
   const size_t csize = prec == 0 ? sizeof(double2) : sizeof(float2);
   auto alloc = [&](void **p, size_t bytes) -> int {
@@ -2168,6 +2175,8 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int pa
       (rc = alloc((void **)&d_inv_off, nf * sizeof(long long))) ||
       (rc = alloc((void **)&d_inv_blocks, inv_blocks.size() * sizeof(int2))) ||
       (rc = alloc(&vec_a, (size_t)ctx->nn * 5 * csize)) ||
+      (rc = alloc((void **)&d_ltiles_tc, ltiles_tc.size() * sizeof(int4))) ||
+      (rc = alloc((void **)&d_utiles_tc, utiles_tc.size() * sizeof(int4))) ||
       (rc = alloc((void **)&d_wave_tiles, wtiles.size() * sizeof(int4))) ||
       (rc = alloc((void **)&d_wave_ctr, (size_t)wctr * sizeof(int))))
     return rc;
@@ -2193,6 +2202,12 @@ int Factor::setup(tlr_ctx *ctx, int precision, int leaf, int solve_block, int pa
                            cudaMemcpyHostToDevice));
   TLR_CUDA(ctx, cudaMemcpy(d_inv_blocks, inv_blocks.data(), inv_blocks.size() * sizeof(int2),
                            cudaMemcpyHostToDevice));
+  if (!ltiles_tc.empty())
+    TLR_CUDA(ctx, cudaMemcpy(d_ltiles_tc, ltiles_tc.data(), ltiles_tc.size() * sizeof(int4),
+                             cudaMemcpyHostToDevice));
+  if (!utiles_tc.empty())
+    TLR_CUDA(ctx, cudaMemcpy(d_utiles_tc, utiles_tc.data(), utiles_tc.size() * sizeof(int4),
+                             cudaMemcpyHostToDevice));
   TLR_CUDA(ctx, cudaMemcpy(d_fronts, df.data(), nf * sizeof(DevFront), cudaMemcpyHostToDevice));
   TLR_CUDA(ctx, cudaMemcpy(d_entries, sym.entries.data(), sym.entries.size() * sizeof(AsmEntry),
                            cudaMemcpyHostToDevice));
@@ -2305,7 +2320,8 @@ void Factor::release() {
   cudaFree(vec_a); cudaFree(linv); cudaFree(uinv); cudaFree(dmat);
   cudaFree(d_inv_off); cudaFree(d_inv_blocks); cudaFree(d_ltiles); cudaFree(d_utiles);
   cudaFree(d_phases); cudaFree(d_barrier); cudaFree(d_solve_err); cudaFree(tc_planes);
-  cudaFree(d_wave_tiles); cudaFree(d_wave_ctr);
+  cudaFree(d_wave_tiles); cudaFree(d_wave_ctr); cudaFree(d_ltiles_tc); cudaFree(d_utiles_tc);
+  d_ltiles_tc = d_utiles_tc = nullptr;
   d_wave_tiles = nullptr;
   d_wave_ctr = nullptr;
   tc_planes = nullptr;
@@ -2336,6 +2352,14 @@ int Factor::rewrite_factors(tlr_ctx *ctx) {
   C *Li = static_cast<C *>(linv), *Ui = static_cast<C *>(uinv);
   { k_tri_inv<C, SW><<<dim3(n_inv_blocks, 2), SW, 0, st>>>(d_inv_blocks, P, d_fronts, d_inv_off,
                                                           Li, Ui); count_launches(); }
+  if constexpr (sizeof(C) == sizeof(float2) && SW == 256) {
+    if (tensor_cores)  // the products on the tensor cores, like the Schur updates
+      return launch_rewrite_tc(ctx, d_ltiles_tc, n_ltiles_tc, d_utiles_tc, n_utiles_tc,
+                               reinterpret_cast<float2 *>(P), d_fronts, d_inv_off,
+                               reinterpret_cast<const float2 *>(Li),
+                               reinterpret_cast<const float2 *>(Ui),
+                               static_cast<float2 *>(dmat), d_tc_err, st);
+  }
   const size_t ssm = sizeof(C) * SW * kRT;
   TLR_CUDA(ctx, cudaFuncSetAttribute(k_scale_u<C, SW>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
@@ -2459,7 +2483,8 @@ int Factor::factor(tlr_ctx *ctx, double sr, double si, double tiny) {
                                 ctx->stream));
   TLR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (tc_err)
-    return fail(ctx, TLR_ERR_CUDA, "tensor-core Schur update: an mbarrier wait timed out");
+    return fail(ctx, TLR_ERR_TIMEOUT,
+                "tensor-core kernel of the factorisation: an mbarrier wait timed out");
   const int nf = (int)sym.fronts.size();
   std::vector<int> inv;
   for (int t = 0; t < nf; ++t) {

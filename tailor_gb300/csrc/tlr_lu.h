@@ -81,6 +81,10 @@ struct Factor {
   long long *d_inv_off = nullptr;
   int2 *d_inv_blocks = nullptr;
   int4 *d_ltiles = nullptr, *d_utiles = nullptr;
+  // the same rewrite on the tensor cores (complex64, 256-row blocks, when
+  // the Schur updates run there too): 128-row L tiles, 64-column U tiles
+  int4 *d_ltiles_tc = nullptr, *d_utiles_tc = nullptr;
+  long long n_ltiles_tc = 0, n_utiles_tc = 0;
   int n_inv_blocks = 0;
   long long inv_elems = 0, n_ltiles = 0, n_utiles = 0;
   cudaGraphExec_t graph_exec = nullptr;  // captured solve, replayed per call

@@ -592,6 +592,363 @@ size_t gemm_tc_smem() { return 2 * kStage + 1024; }
 size_t gemm_tc_bulk_smem(int stages) { return stages * kStage + 1024; }
 size_t tc_chunk_image_bytes() { return kChunkImg; }
 
+namespace {
+
+// ---- factor rewrite on the tensor cores -------------------------------------
+// The block-scaled solves need L' = L inv(L_bb) below every 256-row diagonal
+// block, U' = inv(U_bb) U right of it and D_b = inv(U_bb) inv(L_bb).  On the
+// CUDA cores each output entry costs about 128 complex FMAs, every one fed by
+// a load of the inverse (k_scale_l / k_scale_u).  Here the same products run
+// as tcgen05 MMAs with the 3xTF32 split and FP32 accumulation in TMEM, the
+// operands staged per 8-column K chunk as in k_gemm_tc.  Each CTA owns a
+// whole output band and writes it only after its last MMA has read the
+// band, so the rewrite stays in place.  The inverses are triangular: output
+// tiles that only see zeros of a chunk skip its MMAs.
+//   k_scale_l_tc: CTA = 128 rows below block b; C (128 x nb) = L(rows,
+//     block) inv(L_bb) as four 64-column tiles in 512 TMEM columns; tile t
+//     needs K rows q >= 64 t only (inv(L_bb) is lower triangular).
+//   k_scale_u_tc: CTA = 64 columns: kind 0 right of block b, in place
+//     (X = U(block rows, cols)); kind 1 of D_b (X = inv(L_bb), written to
+//     dmat); C (nb x 64) = inv(U_bb) X as two 128-row tiles in 256 TMEM
+//     columns; the second needs K columns q >= 128 only (inv(U_bb) is upper
+//     triangular).
+// tiles: {front, block, first row (L) / first column (U), kind}.
+constexpr int kRwSW = 256;                          // diagonal-block size
+constexpr int kRwLStage = 10 * kPlane;              // A hi/lo + four B tiles hi/lo
+constexpr int kRwUStage = 6 * kPlane;               // two A tiles hi/lo + B hi/lo
+
+__device__ __forceinline__ void split4_tf32(const float *x, uint4 &hi4, uint4 &lo4) {
+  uint32_t h[4], l[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    h[j] = to_tf32(x[j]);
+    l[j] = to_tf32(x[j] - __uint_as_float(h[j]));
+  }
+  hi4 = make_uint4(h[0], h[1], h[2], h[3]);
+  lo4 = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// A-operand row `row` of a 128-row plane pair: K' 4 q4 .. +3 real parts and
+// 8 + 4 q4 .. +3 imaginary parts of four complex K entries
+__device__ __forceinline__ void stage_a4(unsigned char *hi, int row, int q4, const float2 *v) {
+  float re[4], im[4];
+  uint4 h, l;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    re[j] = v[j].x;
+    im[j] = v[j].y;
+  }
+  split4_tf32(re, h, l);
+  *reinterpret_cast<uint4 *>(hi + plane_off(row, 4 * q4)) = h;
+  *reinterpret_cast<uint4 *>(hi + kPlane + plane_off(row, 4 * q4)) = l;
+  split4_tf32(im, h, l);
+  *reinterpret_cast<uint4 *>(hi + plane_off(row, 8 + 4 * q4)) = h;
+  *reinterpret_cast<uint4 *>(hi + kPlane + plane_off(row, 8 + 4 * q4)) = l;
+}
+
+// B-operand column bn of a 64-column output tile (planes of 128 "rows":
+// Cr row bn = [Br ; -Bi], Ci row 64 + bn = [Bi ; Br]) for four complex K
+// entries 4 q4 .. +3
+__device__ __forceinline__ void stage_b4(unsigned char *hi, int bn, int q4, const float2 *v) {
+  float br[4], bi[4], nbi[4];
+  uint4 h, l;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    br[j] = v[j].x;
+    bi[j] = v[j].y;
+    nbi[j] = -v[j].y;
+  }
+  unsigned char *lo = hi + kPlane;
+  split4_tf32(br, h, l);
+  *reinterpret_cast<uint4 *>(hi + plane_off(bn, 4 * q4)) = h;
+  *reinterpret_cast<uint4 *>(lo + plane_off(bn, 4 * q4)) = l;
+  *reinterpret_cast<uint4 *>(hi + plane_off(64 + bn, 8 + 4 * q4)) = h;
+  *reinterpret_cast<uint4 *>(lo + plane_off(64 + bn, 8 + 4 * q4)) = l;
+  split4_tf32(nbi, h, l);
+  *reinterpret_cast<uint4 *>(hi + plane_off(bn, 8 + 4 * q4)) = h;
+  *reinterpret_cast<uint4 *>(lo + plane_off(bn, 8 + 4 * q4)) = l;
+  split4_tf32(bi, h, l);
+  *reinterpret_cast<uint4 *>(hi + plane_off(64 + bn, 4 * q4)) = h;
+  *reinterpret_cast<uint4 *>(lo + plane_off(64 + bn, 4 * q4)) = l;
+}
+
+// the three MMAs of one K step (A_lo B_hi + A_hi B_lo + A_hi B_hi)
+__device__ __forceinline__ void mma3(uint32_t tmem, uint32_t a_hi, uint32_t b_hi, uint32_t acc0) {
+  const uint32_t a_lo = a_hi + kPlane, b_lo = b_hi + kPlane;
+  mma_tf32(tmem, smem_desc(a_lo, 128u, 256u), smem_desc(b_hi, 128u, 256u), acc0);
+  mma_tf32(tmem, smem_desc(a_hi, 128u, 256u), smem_desc(b_lo, 128u, 256u), 1u);
+  mma_tf32(tmem, smem_desc(a_hi, 128u, 256u), smem_desc(b_hi, 128u, 256u), 1u);
+}
+
+// waits for the MMAs of the last chunk (bounded); on a timeout the error is
+// recorded and the MMAs still in flight are awaited once more before the
+// caller frees TMEM.  Returns whether the results may be written.
+__device__ __forceinline__ bool finish_mmas(uint64_t *bars, int nch, bool ok, int *err,
+                                            int *wait_ok) {
+  if (threadIdx.x == 0) {
+    const int fine = ok && nch > 0 ? mbar_wait(&bars[(nch - 1) & 1], ((nch - 1) >> 1) & 1) : ok;
+    if (!fine) {
+      atomicExch(err, 1);
+      if (nch > 0) mbar_wait(&bars[(nch - 1) & 1], ((nch - 1) >> 1) & 1);
+    }
+    *wait_ok = fine;
+  }
+  __syncthreads();
+  const bool r = *wait_ok != 0;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  return r;
+}
+
+template <int COLS>
+__device__ __forceinline__ void tc_setup(uint32_t *tmem_slot, uint64_t *bars) {
+  if ((threadIdx.x >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(tmem_slot)),
+                 "r"(COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+template <int COLS>
+__device__ __forceinline__ void tc_teardown(uint32_t tmem) {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(COLS));
+}
+
+__global__ void __launch_bounds__(256, 1)
+    k_scale_l_tc(const int4 *__restrict__ tiles, float2 *__restrict__ pool,
+                 const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
+                 const float2 *__restrict__ Linv, int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int wait_ok;
+  unsigned char *stage0 = tc_smem + ((1024 - (smem_addr(tc_smem) & 1023)) & 1023);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int4 tl = tiles[blockIdx.x];
+  const DevFront f = fr[tl.x];
+  const int m = f.m, b0 = tl.y * kRwSW, nb = min(kRwSW, f.p - b0), R0 = tl.z;
+  float2 *F = pool + f.off;
+  const float2 *Li = Linv + inv_off[tl.x] + (long long)tl.y * kRwSW * kRwSW;  // (q, j) at j nb + q
+  tc_setup<512>(&tmem_slot, bars);
+  const uint32_t tmem = tmem_slot;
+  const int nch = (nb + kTcKC - 1) / kTcKC;
+  const int ntile = (nb + 63) / 64;
+  // A: thread (ar, aq) stages K columns 4 aq .. +3 of row ar; B: thread n
+  // stages output column n (tile n / 64) for all 8 K rows of the chunk
+  const int ar = tid & 127, aq = tid >> 7;
+  const int n = tid, bt = n >> 6, bn = n & 63;
+  float2 va[4], vb[8];
+  auto load = [&](int c) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int kc = c * kTcKC + 4 * aq + j;
+      va[j] = (R0 + ar < m && kc < nb) ? F[(long long)(b0 + kc) * m + R0 + ar]
+                                        : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int q = c * kTcKC + k;
+      vb[k] = (n < nb && q < nb && q >= n) ? Li[(long long)n * nb + q] : make_float2(0.f, 0.f);
+    }
+  };
+  bool ok = true;
+  if (nch > 0) load(0);
+  for (int c = 0; c < nch; ++c) {
+    const int sb = c & 1;
+    unsigned char *st = stage0 + sb * kRwLStage;
+    if (c >= 2) {  // the MMAs of chunk c - 2 read this buffer
+      if (tid == 0) wait_ok = mbar_wait(&bars[sb], ((c - 2) >> 1) & 1);
+      __syncthreads();
+      if (!wait_ok) {
+        ok = false;
+        break;
+      }
+    }
+    stage_a4(st, ar, aq, va);
+    if (bt < ntile && c >= 8 * bt) {  // tile bt reads this chunk
+      unsigned char *bh = st + (2 + 2 * bt) * kPlane;
+      stage_b4(bh, bn, 0, vb);
+      stage_b4(bh, bn, 1, vb + 4);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a_hi = smem_addr(st);
+      for (int t = 0; t < ntile; ++t) {
+        if (c < 8 * t) continue;  // inv(L_bb)(q, j) = 0 for q < j
+        const uint32_t b_hi = a_hi + (2 + 2 * t) * kPlane;
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+          mma3(tmem + 128 * t, a_hi + j * 4096, b_hi + j * 4096, (c > 8 * t || j > 0) ? 1u : 0u);
+      }
+      mma_commit(&bars[sb]);
+    }
+    if (c + 1 < nch) load(c + 1);  // the next chunk's loads overlap these MMAs
+  }
+  ok = finish_mmas(bars, nch, ok, err, &wait_ok);
+  if (ok) {
+    // warp w: TMEM lanes 32 (w % 4) .. +31 (rows), column half w / 4 of each tile
+    const int q = warp & 3, h = warp >> 2;
+    const int row = 32 * q + (tid & 31);
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
+    for (int t = 0; t < ntile; ++t) {
+#pragma unroll
+      for (int part = 0; part < 2; ++part) {
+        uint32_t cr[16], ci[16];
+        const int n0 = 32 * h + 16 * part;
+        TLR_TC_LD16(lane_addr + 128 * t + n0, cr);
+        TLR_TC_LD16(lane_addr + 128 * t + 64 + n0, ci);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (R0 + row < m) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = 64 * t + n0 + j;
+            if (col < nb)
+              F[(long long)(b0 + col) * m + R0 + row] =
+                  make_float2(__uint_as_float(cr[j]), __uint_as_float(ci[j]));
+          }
+        }
+      }
+    }
+  }
+  tc_teardown<512>(tmem);
+}
+
+__global__ void __launch_bounds__(256, 1)
+    k_scale_u_tc(const int4 *__restrict__ tiles, float2 *__restrict__ pool,
+                 const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
+                 const float2 *__restrict__ Linv, const float2 *__restrict__ Uinv,
+                 float2 *__restrict__ dmat, int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int wait_ok;
+  unsigned char *stage0 = tc_smem + ((1024 - (smem_addr(tc_smem) & 1023)) & 1023);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int4 tl = tiles[blockIdx.x];
+  const DevFront f = fr[tl.x];
+  const int b0 = tl.y * kRwSW, nb = min(kRwSW, f.p - b0), col0 = tl.z;
+  const long long io = inv_off[tl.x] + (long long)tl.y * kRwSW * kRwSW;
+  const float2 *Ui = Uinv + io;  // (i, q) at q nb + i, upper triangular
+  // X(q, col) at src[col * ld + q]; the result goes to dst at the same place
+  const float2 *src;
+  float2 *dst;
+  long long ld, ncol;
+  if (tl.w == 0) {
+    dst = pool + f.off + b0;
+    src = dst;
+    ld = f.m;
+    ncol = f.m;
+  } else {
+    src = Linv + io;
+    dst = dmat + io;
+    ld = nb;
+    ncol = nb;
+  }
+  tc_setup<256>(&tmem_slot, bars);
+  const uint32_t tmem = tmem_slot;
+  const int nch = (nb + kTcKC - 1) / kTcKC;
+  const int nmt = (nb + 127) / 128;
+  // A: thread i stages row i of inv(U_bb) (tile i / 128) for all 8 K
+  // columns; B: thread (bn, bq), tid < 128, stages K rows 4 bq .. +3 of
+  // output column bn
+  const int ai = tid, bn = tid & 63, bq = (tid >> 6) & 1;
+  const bool bact = tid < 128;
+  float2 va[8], vb[4];
+  auto load = [&](int c) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int q = c * kTcKC + k;
+      va[k] = (ai < nb && q < nb && q >= ai) ? Ui[(long long)q * nb + ai] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int q = c * kTcKC + 4 * bq + j;
+      vb[j] = (bact && col0 + bn < ncol && q < nb) ? src[(long long)(col0 + bn) * ld + q]
+                                                   : make_float2(0.f, 0.f);
+    }
+  };
+  bool ok = true;
+  if (nch > 0) load(0);
+  for (int c = 0; c < nch; ++c) {
+    const int sb = c & 1;
+    unsigned char *st = stage0 + sb * kRwUStage;
+    if (c >= 2) {
+      if (tid == 0) wait_ok = mbar_wait(&bars[sb], ((c - 2) >> 1) & 1);
+      __syncthreads();
+      if (!wait_ok) {
+        ok = false;
+        break;
+      }
+    }
+    {
+      const int mt = ai >> 7;
+      if (mt < nmt && (mt == 0 || c >= 16)) {  // tile mt reads this chunk
+        unsigned char *ah = st + 2 * mt * kPlane;
+        stage_a4(ah, ai & 127, 0, va);
+        stage_a4(ah, ai & 127, 1, va + 4);
+      }
+    }
+    if (bact) stage_b4(st + 4 * kPlane, bn, bq, vb);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t base = smem_addr(st), b_hi = base + 4 * kPlane;
+      for (int mt = 0; mt < nmt; ++mt) {
+        const int cfirst = mt == 0 ? 0 : 16;  // inv(U_bb)(i, q) = 0 for q < i
+        if (c < cfirst) continue;
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+          mma3(tmem + 128 * mt, base + 2 * mt * kPlane + j * 4096, b_hi + j * 4096,
+               (c > cfirst || j > 0) ? 1u : 0u);
+      }
+      mma_commit(&bars[sb]);
+    }
+    if (c + 1 < nch) load(c + 1);
+  }
+  ok = finish_mmas(bars, nch, ok, err, &wait_ok);
+  if (ok) {
+    const int q = warp & 3, h = warp >> 2;
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
+    for (int mt = 0; mt < nmt; ++mt) {
+      const int row = 128 * mt + 32 * q + (tid & 31);
+#pragma unroll
+      for (int part = 0; part < 2; ++part) {
+        uint32_t cr[16], ci[16];
+        const int n0 = 32 * h + 16 * part;
+        TLR_TC_LD16(lane_addr + 128 * mt + n0, cr);
+        TLR_TC_LD16(lane_addr + 128 * mt + 64 + n0, ci);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (row < nb) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = col0 + n0 + j;
+            if (col < ncol)
+              dst[(long long)col * ld + row] =
+                  make_float2(__uint_as_float(cr[j]), __uint_as_float(ci[j]));
+          }
+        }
+      }
+    }
+  }
+  tc_teardown<256>(tmem);
+}
+
+}  // namespace
+
 int launch_gemm_tc_bulk(tlr_ctx *ctx, const int *fl, const int *prefix, const int *pa,
                         const int *pb, int nf, int s, int w, float2 *pool, const DevFront *fr,
                         int tiles, int atiles, int btiles, unsigned char *planes, int *err,
@@ -624,6 +981,24 @@ int launch_gemm_tc(tlr_ctx *ctx, const int *fl, const int *prefix, int nf, int s
   TLR_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)gemm_tc_smem()));
   { k_gemm_tc<<<tiles, 256, gemm_tc_smem(), st>>>(fl, prefix, nf, s, w, pool, fr, err, lbo, sbo); count_launches(); }
+  return TLR_OK;
+}
+
+int launch_rewrite_tc(tlr_ctx *ctx, const int4 *ltiles, long long nl, const int4 *utiles,
+                      long long nu, float2 *pool, const DevFront *fr, const long long *inv_off,
+                      const float2 *Linv, const float2 *Uinv, float2 *dmat, int *err,
+                      cudaStream_t st) {
+  const size_t lsm = 2 * kRwLStage + 1024, usm = 2 * kRwUStage + 1024;
+  TLR_CUDA(ctx, cudaFuncSetAttribute(k_scale_l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)lsm));
+  TLR_CUDA(ctx, cudaFuncSetAttribute(k_scale_u_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)usm));
+  if (nu > 0)
+    { k_scale_u_tc<<<(unsigned)nu, 256, usm, st>>>(utiles, pool, fr, inv_off, Linv, Uinv, dmat,
+                                                  err); count_launches(); }
+  if (nl > 0)
+    { k_scale_l_tc<<<(unsigned)nl, 256, lsm, st>>>(ltiles, pool, fr, inv_off, Linv, err); count_launches(); }
+  TLR_CUDA(ctx, cudaGetLastError());
   return TLR_OK;
 }
 
