@@ -304,6 +304,20 @@ def split_steps(total, width):
     return [total // width + (1 if w < total % width else 0) for w in range(width)]
 
 
+def chain_sequences(npoints, steps, width, warmup, offset=0):
+    """Point indices each chain visits, in order: warmup points, its timed
+    stretch [T_w, T_w + n_w) (T_w = warmup + n_0 + ... + n_(w-1)), the next
+    chain's stretch (the end-to-end pass) and one more point.  Returns
+    (sequences, timed counts n_w, end-to-end counts).  With steps equal to
+    npoints both passes cover every point once."""
+    nstep = split_steps(steps, width)
+    nnext = [nstep[(w + 1) % width] for w in range(width)]
+    starts = [warmup + sum(nstep[:w]) for w in range(width)]
+    seqs = [[(offset + starts[w] - warmup + i) % npoints
+             for i in range(warmup + nstep[w] + nnext[w] + 1)] for w in range(width)]
+    return seqs, nstep, nnext
+
+
 def run_c2(api, ref_file=GOLDEN / "c2_200x128_eigs.txt"):
     """C2: mixed (single-vector, the bench's earlier headline form) vs plain
     FP64, one pass each after a warm-up, eigenvalues against the oracle."""
@@ -478,11 +492,8 @@ def main():
     # passes cover the 32 points once and every point is warm-started from
     # its neighbour
     off = (rank * len(pts)) // max(world, 1)
-    nstep = split_steps(args.steps, width)
-    nnext = [nstep[(w + 1) % width] for w in range(width)]
-    starts = [args.warmup + sum(nstep[:w]) for w in range(width)]
-    seqs = [[pts[(off + starts[w] - args.warmup + i) % len(pts)]
-             for i in range(args.warmup + nstep[w] + nnext[w] + 1)] for w in range(width)]
+    idx, nstep, nnext = chain_sequences(len(pts), args.steps, width, args.warmup, off)
+    seqs = [[pts[i] for i in seq] for seq in idx]
     pos = [0] * width
 
     def take(counts):
