@@ -14,7 +14,7 @@ sweep.
 The combined form (the line's value) is
   * mixed: complex64 multifrontal factor with tensor-core Schur updates,
     every K^-1 application refined in FP64 against the FP64 operator;
-  * batched: the sweep runs as --chains (default 3) concurrent chains on
+  * batched: the sweep runs as --chains (default 4) concurrent chains on
     the one GPU, each a persistent context (one symbolic analysis, one set
     of factor buffers, captured solve and refinement graphs) with its own
     stream and host thread, walking its own stretch of the snake;
@@ -81,7 +81,7 @@ C5_BLOCK = 1
 C5_NCV = 64
 # concurrent chains of sweep points on the one GPU (one context and one host
 # thread each; each chain walks its own stretch of the snake)
-C5_CHAINS = 3
+C5_CHAINS = 4
 PLAIN_NCV = 32
 # C2: mixed vs plain FP64 at 200 x 128
 C2 = dict(ny=200, nz=128, amplitude=0.08, alpha=1.8, omega=complex(0.3, 0.01), nev=16)

@@ -1457,10 +1457,23 @@ __global__ void __launch_bounds__(256)
   const int r = b0 + rr;
   double2 s = make_double2(0, 0);
   if (wp == 0 && rr < nb) {
+    // up to 36 chunks at the top of the tree: the loads go out 8 at a time,
+    // the sums stay in chunk order
     const int nchf = f.m > f.p ? (f.m - f.p + kBC - 1) / kBC : 0;
-#pragma unroll 4
-    for (int k = 0; k < nchf; ++k) {
-      const double2 pv = partial[((long long)fq * nck + k) * pmax + r];
+    const double2 *pp = partial + (long long)fq * nck * pmax + r;
+    int k = 0;
+    for (; k + 8 <= nchf; k += 8) {
+      double2 pv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) pv[u] = pp[(long long)(k + u) * pmax];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        s.x += pv[u].x;
+        s.y += pv[u].y;
+      }
+    }
+    for (; k < nchf; ++k) {
+      const double2 pv = pp[(long long)k * pmax];
       s.x += pv.x;
       s.y += pv.y;
     }

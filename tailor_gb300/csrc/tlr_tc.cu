@@ -826,7 +826,7 @@ __global__ void __launch_bounds__(256, 1)
   tc_teardown<512>(tmem);
 }
 
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(256, 2)
     k_scale_u_tc(const int4 *__restrict__ tiles, float2 *__restrict__ pool,
                  const DevFront *__restrict__ fr, const long long *__restrict__ inv_off,
                  const float2 *__restrict__ Linv, const float2 *__restrict__ Uinv,
