@@ -18,12 +18,12 @@ The combined form (the line's value) is
     the one GPU, each a persistent context (one symbolic analysis, one set
     of factor buffers, captured solve and refinement graphs) with its own
     stream and host thread, walking its own stretch of the snake;
-  * learned: the first point of every chain starts from the learned
-    proposal (an MLP trained, before the timed region, on eigenpairs the
-    solver computed at 60 x 32 over the sweep's parameter range, its start
-    vector carried to 300 x 192 by the spline operators); every later point
-    starts from its predecessor's Ritz vectors (their sum: the wanted modes
-    of the neighbouring point).
+  * learned: in every timed pass the first point of every chain starts
+    from the learned proposal (an MLP trained, before the timed region, on
+    eigenpairs the solver computed at 60 x 32 over the sweep's parameter
+    range, its start vector carried to 300 x 192 by the spline operators);
+    every later point starts from its predecessor's Ritz vectors (their
+    sum: the wanted modes of the neighbouring point).
 The plain FP64 form (complex128 factor, single-vector Krylov-Schur from a
 pseudo-random start, the reference's EigenSolver) solves a stated subset of
 the same points in the same run.
@@ -276,6 +276,11 @@ class Chains:
             raise errors[0]
         return out
 
+    def restart(self):
+        """The next point of every chain starts from the learned proposal
+        (a random start without one) instead of its predecessor's vectors."""
+        self.first = [True] * len(self.probs)
+
     def timed(self, ev, fn):
         """fn() between CUDA events: the start event on chain 0's stream,
         which every other chain's stream waits on; every other stream's end
@@ -511,7 +516,8 @@ def main():
     ev = Events()
     chains = Chains(api, c5_case, width, local, proposal, args.block)
     prob, stream = chains.probs[0], chains.streams[0]
-    # warm-up: every chain's first point starts from the learned proposal
+    # warm-up on the points before each chain's stretch; the timed passes
+    # then start every chain afresh from the learned proposal
     chains.run(take([args.warmup] * width))
 
     def barrier():
@@ -532,6 +538,7 @@ def main():
     clocks.start()
     barrier()
     launches0 = prob.lib.tlr_kernel_launches()
+    chains.restart()
     per, ms = chains.timed(ev, lambda: chains.run(take(nstep)))
     launches = prob.lib.tlr_kernel_launches() - launches0
     barrier()
@@ -551,6 +558,7 @@ def main():
         p.check(p.lib.tlr_load_fields(p.ctx, pg, pb))
 
     barrier()
+    chains.restart()
     per_e2e, ms_e2e = chains.timed(ev, lambda: chains.run(take(nnext), before=load))
     barrier()
     good_e2e = tally([x for chain in per_e2e for x in chain])[0]
