@@ -1,6 +1,6 @@
 """The CPU reference arm of bench.py.  The reference's CPU path cannot solve
 one point of the headline workload (300 x 192) within the step budget, so
-the arm prints the reason and no value (the driver then forms no ratio),
+the arm prints the reason and no value (so no ratio across sizes is formed),
 with one measured 60 x 32 sample of the same physics through the oracle's
 CPU path (C assembly, LAPACK boundary rows, SuperLU + ARPACK).  Needs no
 GPU."""

@@ -5,7 +5,7 @@ The reference solves with SLEPc Krylov-Schur + shift-and-invert LU and keeps
 the nev eigenvalues nearest the target (EigenSolver.cpp:58-59, 77-82).  The
 reference stores no spectrum for any case, so the CPU oracle's FP64
 eigenvalues (SuperLU + ARPACK on the oracle's own assembly and boundary
-rows, tests/golden/make_eig_golden.py) are the judge: every eigenpair
+rows, tests/golden/make_eig_golden.py) decide: every eigenpair
 returned must have relative residual <= 1e-10 and lie within 1e-8 relative
 of one of the oracle's nev nearest eigenvalues, and the returned set must be
 those nev (each oracle eigenvalue matched once).
