@@ -471,7 +471,12 @@ def main():
                     help="Krylov block size of the combined form")
     ap.add_argument("--chains", type=int, default=C5_CHAINS,
                     help="concurrent chains of sweep points of the combined form")
+    ap.add_argument("--ncv", type=int, default=0,
+                    help="Krylov basis size of the combined form (0: 64)")
     args = ap.parse_args()
+    if args.ncv > 0:
+        global C5_NCV
+        C5_NCV = args.ncv
     if args.impl == "reference":
         run_reference(args)
         return
