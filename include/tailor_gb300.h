@@ -196,7 +196,12 @@ typedef struct {
   int cuda_core_schur;    /* Schur-update kernel.  0 (default): the fastest
                              measured -- mixed form: tcgen05 (3xTF32) fed by
                              bulk copies of operand planes split once per
-                             panel step; FP64 form: CUDA-core FP64 FMA.
+                             panel step, in a persistent warp-specialised
+                             kernel (one CTA per SM: a copy thread, an MMA
+                             thread and eight epilogue warps, two TMEM
+                             accumulators, so a tile's F22 update overlaps
+                             the next tile's MMAs); FP64 form: CUDA-core
+                             FP64 FMA.
                              1: CUDA cores (FP32 / FP64 FMA).  2: mixed form
                              on tcgen05 with every tile staging its own
                              operands (the same bits as 0); FP64 form on the
@@ -206,7 +211,10 @@ typedef struct {
                              mixed form, the bulk-copy kernel with a two-
                              stage ring and three CTAs per SM (the same
                              bits as 0; measured 11% slower: 513 vs 460 ms
-                             for a 300 x 192 factorisation)                 */
+                             for a 300 x 192 factorisation).  4: mixed
+                             form, the bulk-copy kernel with one tile per
+                             CTA, two CTAs per SM (the same bits as 0;
+                             measured 6% slower: 351 vs 331 ms)            */
   int solve_block;        /* mixed form: diagonal-block size of the
                              triangular solves, 128, 256 or 512 (0: 256)     */
   int refinement;         /* mixed form: 0 (default) classic iterative

@@ -647,7 +647,9 @@ int run_solve(tlr_ctx *ctx, const tlr_solve_opts *opts, double *lambda,
   // staging their own operands; complex128: DMMA)
   const bool tc = prec == 1 ? o.cuda_core_schur != 1 : o.cuda_core_schur == 2;
   const bool tc_bulk = o.cuda_core_schur != 2;
-  const int tc_variant = o.cuda_core_schur == 3 ? 1 : 0;
+  // bulk-copy kernels: 0 the persistent warp-specialised one (default), 3
+  // the two-stage ring at three CTAs per SM, 4 one tile per CTA
+  const int tc_variant = o.cuda_core_schur == 3 ? 1 : (o.cuda_core_schur == 4 ? 0 : 2);
   const int sblock = prec == 0 ? 128
                      : (o.solve_block == 128 || o.solve_block == 512 ? o.solve_block : 256);
   const int pwidth =

@@ -63,7 +63,9 @@ struct Factor {
   // complex64 Schur updates: operand plane images of one panel step, read
   // by bulk copies (tc_bulk), else staged by every tile's own threads
   bool tc_bulk = true;
-  int tc_variant = 0;  // bulk kernel: 0 three stages / two CTAs per SM, 1 two / three
+  // bulk kernel: 2 persistent warp-specialised (default), 0 one tile per CTA
+  // with three stages / two CTAs per SM, 1 two stages / three CTAs per SM
+  int tc_variant = 2;
   unsigned char *tc_planes = nullptr;
   int w = 32;    // panel width
   int sw = 128;  // rows of a diagonal block of the solves (128 or 256)

@@ -585,6 +585,216 @@ __global__ void __launch_bounds__(256, MINB)
                  "r"(kTmemCols));
 }
 
+// Persistent, warp-specialised variant of k_gemm_tc_bulk.  In the kernel
+// above a CTA stages one tile's operands, runs its MMAs and then reads the
+// accumulator back for the F22 update, so the copies, the tensor pipe and
+// the epilogue of one CTA never overlap.  Here one CTA per SM walks the
+// tiles blockIdx.x, blockIdx.x + gridDim.x, ... with three roles:
+//   warp 8 (one thread): bulk copies of every chunk of every tile into the
+//     S-stage ring (full[] / empty[] mbarriers);
+//   warp 9 (one thread): the MMAs of a tile into one of two TMEM
+//     accumulators (128 columns each), committing the ring stages (empty[])
+//     and, after the tile's last chunk, the accumulator (tfull[]);
+//   warps 0..7: the epilogue.  Warp w owns tile rows 32 (w % 4) + lane
+//     (its TMEM lane quarter) and the 32 complex columns 32 (w / 4) .. +31;
+//     it loads its F22 entries of a tile before that tile's accumulator is
+//     ready, then subtracts the accumulator and releases it (tempty[]),
+//     while the MMAs of the next tile run on the other accumulator.
+// The MMAs and the epilogue arithmetic are those of k_gemm_tc_bulk, so the
+// factors are bitwise the same.  Every wait is bounded: a wait that runs
+// out raises the error flag and the CTA's abort word, every role stops
+// waiting, and the copies and MMAs already issued are awaited (bounded)
+// before TMEM is released.
+constexpr int kPersistThreads = 320;
+
+template <int S>
+__global__ void __launch_bounds__(kPersistThreads, 1)
+    k_gemm_tc_persist(const int *__restrict__ fl, const int *__restrict__ prefix,
+                      const int *__restrict__ pa, const int *__restrict__ pb, int nf, int s, int w,
+                      int tiles, float2 *__restrict__ pool, const DevFront *__restrict__ fr,
+                      const unsigned char *__restrict__ planes_a,
+                      const unsigned char *__restrict__ planes_b, int nchmax,
+                      int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  __shared__ __align__(8) uint64_t full[S], empty[S], tfull[2], tempty[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+  __shared__ int issued_g, consumed_g, committed_g;  // chunk counters at exit
+  unsigned char *ring = tc_smem + ((1024 - (smem_addr(tc_smem) & 1023)) & 1023);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 8) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(&tmem_slot)),
+                 "r"(256));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int q = 0; q < S; ++q) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full[q])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty[q])));
+    }
+    for (int q = 0; q < 2; ++q) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&tfull[q])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;" ::"r"(smem_addr(&tempty[q])));
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_flag = 0;
+    issued_g = consumed_g = committed_g = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  // tile t -> front, its first row / column and the operand images
+  struct Tile {
+    float2 *F;
+    int m, R0, C0, nch;
+    const unsigned char *ga, *gb;
+  };
+  auto decode = [&](int t) {
+    Tile d;
+    const int lo = find_front(prefix, nf, t);
+    const DevFront f = fr[fl[lo]];
+    const int k0 = s * w, ww = min(w, f.p - k0);
+    const int base = k0 + ww, ext = f.m - base;
+    const int ntm = (ext + kTcM - 1) / kTcM;
+    const int lt = t - prefix[lo];
+    const int rt = lt % ntm, ct = lt / ntm;
+    d.F = pool + f.off;
+    d.m = f.m;
+    d.R0 = base + rt * kTcM;
+    d.C0 = base + ct * kTcN;
+    d.nch = (ww + kTcKC - 1) / kTcKC;
+    d.ga = planes_a + (long long)(pa[lo] + rt) * nchmax * kChunkImg;
+    d.gb = planes_b + (long long)(pb[lo] + ct) * nchmax * kChunkImg;
+    return d;
+  };
+  // bounded wait that also gives up once another role has aborted
+  auto wait_bar = [&](uint64_t *bar, uint32_t parity) -> bool {
+    for (unsigned it = 0; it < kWaitLimit; ++it) {
+      if (mbar_test(bar, parity)) return true;
+      if (abort_flag) return false;
+    }
+    abort_flag = 1;
+    atomicExch(err, 1);
+    return false;
+  };
+
+  if (warp == 8) {
+    if (lane == 0) {  // producer
+      int g = 0;
+      for (int t = blockIdx.x; t < tiles && !abort_flag; t += gridDim.x) {
+        const Tile d = decode(t);
+        for (int c = 0; c < d.nch; ++c, ++g) {
+          const int st = g % S;
+          if (g >= S && !wait_bar(&empty[st], ((g / S) & 1) ^ 1)) break;
+          unsigned char *dst = ring + st * kStage;
+          mbar_expect_tx(&full[st], 2 * kChunkImg);
+          bulk_g2s(dst, d.ga + (long long)c * kChunkImg, kChunkImg, &full[st]);
+          bulk_g2s(dst + kChunkImg, d.gb + (long long)c * kChunkImg, kChunkImg, &full[st]);
+        }
+      }
+      issued_g = g;
+    }
+  } else if (warp == 9) {
+    if (lane == 0) {  // MMA issuer
+      int g = 0, ti = 0, committed = 0;
+      for (int t = blockIdx.x; t < tiles && !abort_flag; t += gridDim.x, ++ti) {
+        const Tile d = decode(t);
+        const int acc = ti & 1;
+        if (ti >= 2 && !wait_bar(&tempty[acc], ((ti >> 1) - 1) & 1)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t tacc = tmem + 128 * acc;
+        bool ok = true;
+        for (int c = 0; c < d.nch; ++c, ++g) {
+          const int st = g % S;
+          if (!wait_bar(&full[st], (g / S) & 1)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t a_hi = smem_addr(ring + st * kStage), a_lo = a_hi + kPlane;
+          const uint32_t b_hi = a_hi + 2 * kPlane, b_lo = a_hi + 3 * kPlane;
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            const uint32_t o = j * 4096;
+            const uint32_t acc0 = (c > 0 || j > 0) ? 1u : 0u;
+            mma_tf32(tacc, smem_desc(a_lo + o, 128u, 256u), smem_desc(b_hi + o, 128u, 256u), acc0);
+            mma_tf32(tacc, smem_desc(a_hi + o, 128u, 256u), smem_desc(b_lo + o, 128u, 256u), 1u);
+            mma_tf32(tacc, smem_desc(a_hi + o, 128u, 256u), smem_desc(b_hi + o, 128u, 256u), 1u);
+          }
+          mma_commit(&empty[st]);
+          committed = g + 1;
+        }
+        if (!ok) break;
+        mma_commit(&tfull[acc]);  // covers every MMA of the tile
+      }
+      consumed_g = g;
+      committed_g = committed;
+    }
+  } else {  // epilogue, warps 0..7
+    const int q4 = warp & 3, h2 = warp >> 2;
+    const int row = 32 * q4 + lane;
+    int ti = 0;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++ti) {
+      const Tile d = decode(t);
+      const int acc = ti & 1;
+      const bool row_ok = d.R0 + row < d.m;
+      // this tile's F22 entries, fetched while its MMAs run
+      float2 f22[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int n = 32 * h2 + j;
+        f22[j] = (row_ok && d.C0 + n < d.m) ? d.F[(long long)(d.C0 + n) * d.m + d.R0 + row]
+                                            : make_float2(0.f, 0.f);
+      }
+      bool ok = true;
+      if (lane == 0) ok = wait_bar(&tfull[acc], (ti >> 1) & 1);
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t lane_addr = tmem + 128 * acc + ((uint32_t)(32 * q4) << 16);
+#pragma unroll
+      for (int part = 0; part < 4; ++part) {
+        uint32_t cr[8], ci[8];
+        const int n0 = 32 * h2 + 8 * part;
+        TLR_TC_LD8(lane_addr + n0, cr);
+        TLR_TC_LD8(lane_addr + 64 + n0, ci);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (row_ok) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int n = n0 + j;
+            if (d.C0 + n < d.m) {
+              float2 v = f22[8 * part + j];
+              v.x -= __uint_as_float(cr[j]);
+              v.y -= __uint_as_float(ci[j]);
+              d.F[(long long)(d.C0 + n) * d.m + d.R0 + row] = v;
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&tempty[acc]))
+                     : "memory");
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && abort_flag) {
+    // let the copies and MMAs already issued land before TMEM is released
+    for (int g = consumed_g; g < issued_g; ++g) mbar_wait(&full[g % S], (g / S) & 1);
+    if (committed_g > 0) mbar_wait(&empty[(committed_g - 1) % S], ((committed_g - 1) / S) & 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 8)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
+}
+
 }  // namespace
 
 size_t gemm_tc_smem() { return 2 * kStage + 1024; }
@@ -958,7 +1168,16 @@ int launch_gemm_tc_bulk(tlr_ctx *ctx, const int *fl, const int *prefix, const in
     { k_tc_split<<<dim3(atiles + btiles, nchmax), 256, 0, st>>>(fl, pa, pb, nf, s, w, pool, fr,
                                                                planes, atiles, nchmax); count_launches(); }
   const unsigned char *pbp = planes + (long long)atiles * nchmax * kChunkImg;
-  if (variant == 1) {  // two stages, three CTAs per SM, half the F22 prefetched
+  if (variant == 2) {  // persistent, warp-specialised: one CTA per SM, four stages
+    auto k = k_gemm_tc_persist<4>;
+    const int smem = (int)gemm_tc_bulk_smem(4);
+    TLR_CUDA(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int grid = std::max(1, std::min(tiles, std::max(sms, 1)));
+    { k<<<grid, kPersistThreads, smem, st>>>(fl, prefix, pa, pb, nf, s, w, tiles, pool, fr,
+                                             planes, pbp, nchmax, err); count_launches(); }
+  } else if (variant == 1) {  // two stages, three CTAs per SM, half the F22 prefetched
     auto k = k_gemm_tc_bulk<2, 3, 16>;
     TLR_CUDA(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)gemm_tc_bulk_smem(2)));

@@ -200,14 +200,16 @@ def test_fp64_tensor_core_schur_update_matches_cuda_cores(gpu_lib):
 
 def test_bulk_copy_schur_update_is_bitwise_the_tile_staged_one(gpu_lib):
     """The tcgen05 Schur update fed by bulk copies of operand planes split
-    once per panel step (the default) and the one whose tiles stage their
-    own operands run the same MMAs in the same order: identical factors,
-    hence identical eigenpairs."""
+    once per panel step (the default: a persistent warp-specialised kernel;
+    also one tile per CTA with two or three ring stages) and the one whose
+    tiles stage their own operands run the same MMAs in the same order:
+    identical factors, hence identical eigenpairs."""
     ph = Physics(alpha=1.9, omega=0j, nev=8, tol=1e-10)
     with api.Problem(make_case(100, 50, physics=ph)) as p:
         api.run_pipeline(p)
         bulk = api.EigenSolver(p).solve(nev=8, precision=1, fallback=False)
-        for other in (2, 3):  # tile-staged; two-stage ring at three CTAs per SM
+        # tile-staged; two-stage ring at three CTAs per SM; one tile per CTA
+        for other in (2, 3, 4):
             tile = api.EigenSolver(p).solve(nev=8, precision=1, cuda_core_schur=other,
                                             fallback=False)
             assert np.array_equal(bulk.lam, tile.lam)
