@@ -38,3 +38,19 @@ def test_fewer_steps_than_points():
     assert nstep == [4, 3, 3]
     timed = [i for w, s in enumerate(seqs) for i in s[3:3 + nstep[w]]]
     assert sorted(timed) == list(range(3, 13))
+
+
+def test_snake_order_visits_neighbours():
+    """c5_points(snake=True): the 8 x 4 (alpha, Re) grid, alpha running up on
+    even Re rows and down on odd ones, so consecutive points differ in one
+    coordinate by one grid step (the warm start's neighbour)."""
+    import numpy as np
+    from tailor_gb300.neutral_sweep import c5_points
+    pts = c5_points(snake=True)
+    assert len(pts) == 32 and len(set(pts)) == 32
+    alphas = np.linspace(0.5, 3.5, 8)
+    res = np.linspace(800, 2400, 4)
+    for (_, a0, r0), (_, a1, r1) in zip(pts, pts[1:]):
+        da = abs(np.searchsorted(alphas, a1 - 1e-9) - np.searchsorted(alphas, a0 - 1e-9))
+        dr = abs(np.searchsorted(res, r1 - 1e-9) - np.searchsorted(res, r0 - 1e-9))
+        assert (da, dr) in ((1, 0), (0, 1))
